@@ -1,0 +1,350 @@
+"""Benchmark of the GB300 halo painter on the reference's headline workload.
+
+Workload (one "step"): a synthetic catalogue of 1e7 halos (10 float32 per record, shell
+100-8000 Mpc, masses 1e12-3e15 Msun/h, seed 2) painted to two HEALPix Nside 4096 maps,
+tSZ Compton-y (nu = 0 table, profile 1) and kSZ (profile 2), zmax = 6, model 1:
+radial/mass cut, per-halo set-up, disc enumeration, profile interpolation, deposit, and
+the float32 read-out of both maps.  Inputs (400 MB) and maps (2 x 805 MB) exceed L2, so
+no explicit flush is needed between steps.
+
+  value  halos/s with the catalogue resident in HBM (CUDA events on the paint stream)
+  e2e    halos/s through the C ABI with host buffers: pinned catalogue H2D, paint, and
+         both float maps copied back to pinned host memory, every step
+
+--impl reference times the CPU implementation of the path on the host cores instead:
+the oracle (a C restatement of pks2map, threads as MPI ranks with private float maps and
+a final sum) on a bounded sample of the same catalogue.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_HALOS = 10_000_000
+NSIDE = 4096
+SHELL = (100.0, 8000.0)
+MASS = (1e12, 3e15)
+SEED = 2
+ZMAX = 6.0
+MAPS = ((0, 1), (0, 2))
+METRIC = "halos/sec & pixel-updates/sec at Nside=4096, 1 GB300; rel err vs FP64 oracle"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--halos", type=int, default=N_HALOS)
+    ap.add_argument("--nside", type=int, default=NSIDE)
+    ap.add_argument("--no-plain", action="store_true", help="skip the FP64 drop-in comparison")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--cpu-fraction", type=float, default=0.1)
+    return ap.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def catalogue(n):
+    import matt_young_mapmaking_gb300 as p2m
+    return p2m.generate_catalogue(SEED, n, 10, r=SHELL, m=MASS)
+
+
+def oracle_table():
+    """Full-size make_maptable table (model 1, nu = 0) from the oracle, cached in /tmp."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    path = "/tmp/p2m_table_model1_nu0_full.bin"
+    if os.path.exists(path) and os.path.getsize(path) == 36 + 8 * 100 * 100 * 200:
+        with open(path, "rb") as f:
+            return f.read()
+    img = oracle.make_maptable(1, 0.0, 0.0)
+    with open(path + ".tmp", "wb") as f:
+        f.write(img)
+    os.replace(path + ".tmp", path)
+    return img
+
+
+def cpu_leg(rec, nside, frac, threads=None):
+    """The oracle (threads as ranks) on a bounded sample: halos/s extrapolated to the
+    whole catalogue as N / (map set-up + reduction + paint(sample) * N / n_sample)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    threads = threads or os.cpu_count() or 1
+    tab = oracle.Table(oracle_table())
+    n = len(rec)
+    ns = max(threads, int(n * frac) // threads * threads)
+    p = oracle.params(nside=nside, npix_fs=16, maps=MAPS, zmax=ZMAX, fp32=True, nfloat=10)
+    t0 = time.perf_counter()
+    _, _, st, (t_set, t_paint, t_red) = oracle.paint_threads(p, [tab], rec[:ns], threads)
+    wall = time.perf_counter() - t0
+    t_full = t_set + t_red + t_paint * (n / ns)
+    return {"value": n / t_full, "unit": "halos/s", "cores": threads, "kind": "port",
+            "sample": "first %d of %d records (%.0f%%), %d threads each with private float "
+                      "maps (Nside %d, 2 maps) summed at the end; paint time scaled by %.1f, "
+                      "map set-up %.2fs and reduction %.2fs counted once; sample wall %.1fs"
+                      % (ns, n, 100.0 * ns / n, threads, nside, n / ns, t_set, t_red, wall),
+            "pixel_updates_per_s": 2 * st["hp_updates"] / t_paint if t_paint > 0 else None}
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    rec = catalogue(args.halos)
+    threads = os.cpu_count() or 1
+    vals = []
+    for i in range(args.warmup + args.steps):
+        r = cpu_leg(rec, args.nside, min(args.cpu_fraction, 1.0), threads)
+        if i >= args.warmup:
+            vals.append(r)
+    v = float(np.median([r["value"] for r in vals]))
+    out = {"metric": METRIC, "value": v, "unit": "halos/s", "n_gpus": args.gpus,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * args.halos / v,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+           "data": "synthetic (Philox catalogue, seed %d)" % SEED, "impl": "reference",
+           "config": {"workload": "pks2map c2: %d halos, HEALPix Nside %d, tSZ + kSZ, zmax %g"
+                                  % (args.halos, args.nside, ZMAX)},
+           "cpu_baseline": {k: vals[-1][k] for k in ("value", "unit", "cores", "kind", "sample")},
+           "e2e": {"value": v, "unit": "halos/s", "h2d_bytes_per_step": 0,
+                   "d2h_bytes_per_step": 0}}
+    out["cpu_baseline"]["value"] = v
+    print(json.dumps(out))
+
+
+def run_ours(args):
+    import torch
+
+    import matt_young_mapmaking_gb300 as p2m
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    N, nside = args.halos, args.nside
+    npix = 12 * nside * nside
+    rec = catalogue(N)
+    h_rec = torch.from_numpy(rec).pin_memory()
+    d_rec = h_rec.to(dev)
+    table = p2m.make_maptable(1, 0.0, 0.0, device=local)
+    outs = [torch.empty(npix, dtype=torch.float32, device=dev) for _ in MAPS]
+    h_outs = [torch.empty(npix, dtype=torch.float32).pin_memory() for _ in MAPS]
+    stream = torch.cuda.Stream(device=dev)
+
+    def make(precision):
+        pt = p2m.Painter(nside=nside, precision=precision, maps=MAPS, zmax=ZMAX,
+                         max_records=N, device=local, flags=p2m.FLAG_TIMING)
+        pt.load_table(0, table)
+        return pt
+
+    def step(pt):
+        pt.reset()
+        pt.paint_records_device(d_rec.data_ptr(), N, 10, stream.cuda_stream)
+        for m in range(len(MAPS)):
+            pt.healpix_device(m, outs[m].data_ptr(), stream.cuda_stream)
+
+    def barrier():
+        torch.cuda.synchronize(dev)
+        if ws > 1:
+            torch.distributed.barrier()
+
+    def timed(pt, steps, warmup, sampler=None):
+        for _ in range(warmup):
+            step(pt)
+        barrier()
+        if sampler:
+            sampler.start()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        for _ in range(steps):
+            step(pt)
+        ev1.record(stream)
+        barrier()
+        clocks = sampler.stop() if sampler else None
+        ms = ev0.elapsed_time(ev1) / steps
+        if ws > 1:
+            t = torch.tensor([ms], device=dev)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms, clocks
+
+    pt = make(args.precision)
+    sampler = ClockSampler(local)
+    ms, clocks = timed(pt, args.steps, args.warmup, sampler)
+    phases = pt.timings()
+    st = pt.stats()
+    maps_main = [o.cpu().numpy() for o in outs]
+
+    # end to end through the C ABI with host buffers
+    def e2e_step():
+        pt.reset()
+        pt.paint_records(h_rec.numpy())
+        for m in range(len(MAPS)):
+            pt.healpix_into(m, h_outs[m].data_ptr())
+    for _ in range(2):
+        e2e_step()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
+    barrier()
+    e2e_ms = 1e3 * (time.perf_counter() - t0) / args.steps
+    pt.close()
+
+    total_halos = N * ws
+    value = total_halos / (ms * 1e-3)
+    upd = st["hp_updates"] * len(MAPS)
+    # roofline of the dominant kernel (HBM-bound): algorithmic bytes per launch
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except Exception:
+        pass
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+    s_acc = 8
+    alg = {
+        "paint": upd * 2 * s_acc,                       # read-modify-write of the accumulator
+        "readout": len(MAPS) * npix * (s_acc + 4),      # accumulator read + float write
+        "cut": N * 40,                                  # one pass over the records
+    }
+    dom = max(("paint", "readout", "cut"), key=lambda k: phases.get(k, 0.0) * (
+        len(MAPS) if k == "readout" else 1))
+    dom_ms = phases[dom]
+    achieved = alg[dom] / (dom_ms * 1e-3) / 1e9 if dom_ms > 0 else None
+    roof = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak,
+            "unit": "GB/s", "frac": achieved / hbm_peak if achieved else None,
+            "peak_source": peak_src, "traffic": None,
+            "algorithmic_bytes": alg[dom], "launch_ms": dom_ms}
+
+    out = {"metric": METRIC, "value": value, "unit": "halos/s", "n_gpus": ws,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+           "data": "synthetic (Philox catalogue, seed %d; profile table from make_maptable "
+                   "on the GPU)" % SEED,
+           "config": {"workload": "pks2map c2: %d halos x 10 float, shell %g-%g Mpc, masses "
+                                  "%g-%g, HEALPix Nside %d, tSZ y + kSZ, zmax %g"
+                                  % (N, SHELL[0], SHELL[1], MASS[0], MASS[1], nside, ZMAX),
+                      "precision": args.precision, "l2": "inputs and maps larger than L2",
+                      "parallelism": "replicas" if ws > 1 else "single GPU"},
+           "pixel_updates_per_s": upd * ws / (ms * 1e-3),
+           "phases_ms": phases,
+           "counts": {k: st[k] for k in ("n_shell", "n_painted", "n_enumerated",
+                                          "hp_candidates", "hp_updates", "n_recheck")},
+           "gpu_launches": None,
+           "roofline": roof,
+           "clocks": clocks,
+           "e2e": {"value": total_halos / (e2e_ms * 1e-3), "unit": "halos/s",
+                   "ms_per_step": e2e_ms, "h2d_bytes_per_step": int(rec.nbytes),
+                   "d2h_bytes_per_step": int(len(MAPS) * npix * 4)}}
+    nlaunch = 2 + 1 + 1 + 1 + 1 + 3 + 1 + (1 if args.precision == "mixed" else 0) + len(MAPS)
+    out["gpu_launches"] = nlaunch * args.steps
+
+    if not args.no_plain and args.precision == "mixed":
+        pp = make("fp64")
+        ms64, _ = timed(pp, max(2, args.steps // 2), 1)
+        ref_maps = [o.cpu().numpy() for o in outs]
+        pp.close()
+        out["plain_fp64"] = {"value": total_halos / (ms64 * 1e-3), "ms_per_step": ms64,
+                             "speedup_of_mixed": ms64 / ms}
+        errs = {}
+        for m, name in enumerate(("tsz", "ksz")):
+            a = maps_main[m].astype(np.float64)
+            b = ref_maps[m].astype(np.float64)
+            mx = np.abs(b).max()
+            mask = np.abs(b) > 1e-3 * mx
+            rel = np.abs(a[mask] - b[mask]) / np.abs(b[mask])
+            errs[name] = {"max_rel_masked": float(rel.max()) if rel.size else 0.0,
+                          "max_abs": float(np.abs(a - b).max()),
+                          "rel_l2": float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)),
+                          "total_rel": float(abs(a.sum() - b.sum()) / max(abs(b.sum()), 1e-300))}
+        out["error_vs_fp64"] = errs
+
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        out["cpu_baseline"] = cpu_leg(rec, nside, args.cpu_fraction)
+    if rank == 0:
+        print(json.dumps(out))
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,152 @@
+/*
+ * p2m.h -- C ABI of the GB300 halo painter (drop-in for the pks2map halo loop).
+ *
+ * Plain C types and pointers only, so that Fortran (ISO_C_BINDING), C, C++ and Python
+ * (ctypes) bind it directly.  Every entry point returns a p2m_status; nothing exits,
+ * traps or prints.  A context is not thread-safe: use one per host thread.  Interface
+ * it replaces (paths relative to the reference project root):
+ *
+ *   loadmaptable(tablefile)                  maptable.f90:150-172   -> p2m_load_table
+ *   loadpksc(filein, profile)                pksc.f90:22-90         -> p2m_paint_records
+ *   halo loop + projecthalo_flatsky/healpix  pks2map.f90:276-303,   -> p2m_paint_records
+ *                                            haloproject.f90:38-156
+ *   projecthalo_flatsky(x,y,z,r,chi,m,       pks2map.f90:300-301    -> p2m_project_halo
+ *     redshift,v,profile) + _healpix(...)
+ *   MPI_Allreduce of fsmap/hpmap             pks2map.f90:313-314    -> p2m_get_healpix,
+ *                                                                      p2m_get_flatsky
+ *   halo count / moments                     pks2map.f90:310,321-327 -> p2m_get_stats
+ */
+#ifndef P2M_H
+#define P2M_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct p2m_ctx p2m_ctx;
+typedef int32_t p2m_status;
+
+enum {
+  P2M_OK = 0,
+  P2M_ERR_BADARG = 1,   /* invalid argument or configuration */
+  P2M_ERR_CUDA = 2,     /* a CUDA runtime call failed */
+  P2M_ERR_CAPACITY = 3, /* a work buffer overflowed (never truncated silently) */
+  P2M_ERR_TIMEOUT = 4,  /* a bounded device wait gave up */
+  P2M_ERR_IO = 5,       /* malformed table / catalogue image */
+  P2M_ERR_STATE = 6,    /* call out of sequence */
+  P2M_ERR_NOMEM = 7     /* device or pinned allocation failed */
+};
+
+/* precision of the per-pixel path */
+enum {
+  P2M_PREC_FP64 = 0,  /* plain drop-in: FP64 pixel geometry (pix2vec_ring + angdist) for
+                         every candidate, FP64 accumulation */
+  P2M_PREC_MIXED = 1  /* FP32 disc test and profile interpolation with an exact FP64
+                         recheck near every decision boundary; compensated two-float
+                         FP32 accumulation */
+};
+
+/* catalogue layouts (floats per record): 7 = x,y,z,vx,vy,vz,RTH after a 2-word header
+   (pksc.f90:46-66); 10 = the same plus xL,yL,zL after a 3-word header */
+enum { P2M_LAYOUT_7 = 7, P2M_LAYOUT_10 = 10 };
+
+enum {
+  P2M_FLAG_RECORD_SETS = 1, /* keep (record index, pixel) of every HEALPix deposit */
+  P2M_FLAG_ALL_HALOS = 2,   /* enumerate halos whose table value is identically zero */
+  P2M_FLAG_TIMING = 4       /* record per-phase device times (p2m_get_timings) */
+};
+
+#define P2M_MAXMAPS 8
+
+typedef struct p2m_config {
+  int32_t nside;      /* HEALPix Nside (power of 2, <= 8192); 0 = no HEALPix map
+                         (pks2map.f90:74, default 4096) */
+  int32_t npix_fs;    /* flat-sky map side; 0 = no flat-sky map (pks2map.f90:77) */
+  float fov_deg;      /* flat-sky field of view in degrees (pks2map.f90:78) */
+  float zmin, zmax;   /* radial cut in redshift (pks2map.f90:73,79) */
+  float chihview;     /* observer shift along x (pks2map.f90:80) */
+  int32_t model;      /* profile model 1..3 (pks2map.f90:81) */
+  int32_t precision;  /* P2M_PREC_* */
+  int32_t nmaps;      /* maps painted per enumeration, 1..P2M_MAXMAPS */
+  int32_t map_table[P2M_MAXMAPS];   /* table slot of each map */
+  int32_t map_profile[P2M_MAXMAPS]; /* 1 = tSZ (weight 1), 2 = kSZ (weight -v_los/c)
+                                       (pks2map.f90:82, pksc.f90:70-78) */
+  int64_t max_records; /* largest record count of one paint call */
+  int32_t device;      /* CUDA device ordinal */
+  int32_t flags;       /* P2M_FLAG_* */
+} p2m_config;
+
+typedef struct p2m_stats {
+  int64_t n_records;   /* records read */
+  int64_t n_shell;     /* inside the radial cut (pks2map.f90:144-160) */
+  int64_t n_painted;   /* passing the mass cut (pks2map.f90:296, "halos in map") */
+  int64_t n_enumerated;/* halos whose discs were enumerated */
+  int64_t hp_candidates; /* candidate HEALPix pixels tested */
+  int64_t hp_updates;  /* (halo, pixel) pairs inside the disc */
+  int64_t fs_updates;  /* flat-sky (halo, pixel) pairs inside the disc */
+  int64_t n_recheck;   /* pixels decided by the exact FP64 recheck (mixed precision) */
+  double hp_sum[P2M_MAXMAPS]; /* sum over the HEALPix map of each map (total Y, kSZ) */
+  double fs_sum[P2M_MAXMAPS];
+} p2m_stats;
+
+/* Create a painter on cfg->device; allocates device maps and work buffers. */
+p2m_status p2m_create(const p2m_config *cfg, p2m_ctx **out);
+void p2m_destroy(p2m_ctx *ctx);
+/* Human-readable description of the last error on this context (never NULL). */
+const char *p2m_last_error(const p2m_ctx *ctx);
+
+/* Load a make_maptable table file image (36-byte header + float table(2,nrt,nmht,nchit))
+   into slot 0..7.  All loaded tables must share one header. */
+p2m_status p2m_load_table(p2m_ctx *ctx, int32_t slot, const void *image, int64_t nbytes);
+
+/* Zero the accumulated maps (the reference's `fsmapl=0; hpmapl=0`, pks2map.f90:278-279). */
+p2m_status p2m_reset_maps(p2m_ctx *ctx);
+
+/* Paint nrec catalogue records (nfloat = 7 or 10 floats each, header already removed)
+   held in host memory: radial cut, mass, per-halo set-up and both projections, exactly
+   the halo loop of pks2map.f90:134-303.  Accumulates into the context's maps. */
+p2m_status p2m_paint_records(p2m_ctx *ctx, const float *records, int64_t nrec, int32_t nfloat);
+/* Same with the records already in device memory (on ctx's device), ordered on the
+   given cudaStream_t (NULL = the context's stream). */
+p2m_status p2m_paint_records_device(p2m_ctx *ctx, const float *d_records, int64_t nrec,
+                                    int32_t nfloat, void *stream);
+
+/* Per-halo entry with the reference's by-reference arguments (bind(C) friendly):
+   queues one halo whose loop quantities are already computed (pks2map.f90:284-298)
+   for projecthalo_flatsky + projecthalo_healpix.  Queued halos are painted on the next
+   read of a map or by p2m_flush.  x, y, z are divided by chi in place, as
+   projecthalo_flatsky does to its caller's variables (haloproject.f90:97-99). */
+p2m_status p2m_project_halo(p2m_ctx *ctx, float *x, float *y, float *z, const float *r,
+                            const float *chi, const float *m, const float *redshift,
+                            const float *v, const int32_t *profile);
+p2m_status p2m_flush(p2m_ctx *ctx);
+
+/* Convert the accumulated map `map` to float and copy it out: host memory
+   (12*nside^2 or npix_fs^2 floats, RING / column-major j-fastest order) ... */
+p2m_status p2m_get_healpix(p2m_ctx *ctx, int32_t map, float *out);
+p2m_status p2m_get_flatsky(p2m_ctx *ctx, int32_t map, float *out);
+/* ... or device memory, ordered on `stream` (NULL = the context's stream). */
+p2m_status p2m_get_healpix_device(p2m_ctx *ctx, int32_t map, float *d_out, void *stream);
+
+/* Counters and map sums of everything painted since the last reset. */
+p2m_status p2m_get_stats(p2m_ctx *ctx, p2m_stats *out);
+/* Wait for all work queued on the context's stream. */
+p2m_status p2m_synchronize(p2m_ctx *ctx);
+
+/* (record index, RING pixel) pairs of the HEALPix deposits of the last paint call;
+   requires P2M_FLAG_RECORD_SETS.  *n receives the total (may exceed cap). */
+p2m_status p2m_get_pixel_sets(p2m_ctx *ctx, int64_t *rec, int64_t *pix, int64_t cap, int64_t *n);
+
+/* Build a make_maptable table image on the GPU (maptable.f90:25-146).  Returns the
+   image size in *nbytes; image may be NULL to query the size.  Sizes <= 0 take the
+   reference's 100 x 100 x 200. */
+p2m_status p2m_make_maptable(int32_t device, int32_t model, float nu, float alpha_cmb,
+                             int32_t nchit, int32_t nmht, int32_t nrt, void *image,
+                             int64_t *nbytes);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* P2M_H */

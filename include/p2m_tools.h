@@ -1,0 +1,47 @@
+/*
+ * p2m_tools.h -- host-side tools that travel with the painter.  They have no
+ * counterpart in the reference, whose input catalogues come from its halo finder
+ * (hpkvd / merge_pkvd, out of scope here): they build the synthetic catalogues used
+ * for tests and benchmarks.
+ */
+#ifndef P2M_TOOLS_H
+#define P2M_TOOLS_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Synthetic halo catalogue, deterministic in (seed, record index): Philox4x32-10
+   with the record index as counter.  Positions uniform in volume in the shell
+   [r_min, r_max] Mpc with isotropic directions; masses from dN/dlnM ~ M^slope on
+   [m_min, m_max] Msun by inverse CDF; RTH = (3M / (4 pi Om 2.775e11 h^2))^(1/3) with
+   Om = 0.31, h = 0.68; velocities N(0, sigma_v) km/s per axis; Lagrangian position
+   x - 0.01 v.  Writes n records of nfloat (7: x,y,z,vx,vy,vz,RTH; 10: + xL,yL,zL)
+   starting at record index first.  Returns 0, or 1 on bad arguments. */
+int32_t p2m_generate_catalogue(uint64_t seed, int64_t first, int64_t n, int32_t nfloat,
+                               double r_min, double r_max, double m_min, double m_max,
+                               double slope, double sigma_v, float *out);
+
+/* Philox4x32-10 block for (counter c[4], key k[2]) -> out[4]. */
+void p2m_philox4x32(const uint32_t c[4], const uint32_t k[2], uint32_t out[4]);
+
+/* Device time (ms) of each phase of the last paint call and of the last map read-out,
+   for a context created with P2M_FLAG_TIMING: [0] cut, [1] per-halo set-up, [2] ring
+   histogram scan, [3] item placement, [4] ring spans, [5] candidate scan, [6] paint,
+   [7] exact recheck, [8] flat sky, [9] read-out.  Diagnostics only (the reference
+   prints no timings). */
+struct p2m_ctx;
+int32_t p2m_get_timings(struct p2m_ctx *ctx, double *ms, int32_t n);
+
+/* Self-test of the single-precision math the kernels use (fn: 0 log, 1 exp, 2 pow,
+   3 asin, 4 atan, 5 sin, 6 cos, 7 tan) evaluated on the GPU over n device floats;
+   d_y is read only for pow.  Synchronous.  Returns 0 or a CUDA error code. */
+int32_t p2m_fmath_eval_device(int32_t device, int32_t fn, const float *d_x, const float *d_y,
+                              float *d_out, int64_t n);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,295 @@
+"""ctypes binding of the C ABI (include/p2m.h, include/p2m_tools.h).
+
+The Painter class mirrors the reference's map-making interface for the hot path
+(pks2map_src/): ``load_table`` is ``loadmaptable`` (maptable.f90:150-172),
+``paint_records`` is ``loadpksc`` plus the halo loop (pksc.f90:22-90,
+pks2map.f90:134-303), ``project_halo`` is ``projecthalo_flatsky`` followed by
+``projecthalo_healpix`` (haloproject.f90:38-156), and ``healpix``/``flatsky`` return the
+summed maps (pks2map.f90:313-314).  Every failure raises P2MError; there is no CPU path.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libp2m_gb300.so")
+
+MAXMAPS = 8
+PREC_FP64, PREC_MIXED = 0, 1
+FLAG_RECORD_SETS, FLAG_ALL_HALOS, FLAG_TIMING = 1, 2, 4
+STATUS = {0: "OK", 1: "BADARG", 2: "CUDA", 3: "CAPACITY", 4: "TIMEOUT", 5: "IO", 6: "STATE",
+          7: "NOMEM"}
+
+
+class P2MError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__("p2m error %s (%d): %s" % (STATUS.get(status, "?"), status, msg))
+        self.status = status
+
+
+class P2MConfig(ctypes.Structure):
+    _fields_ = [
+        ("nside", ctypes.c_int32),
+        ("npix_fs", ctypes.c_int32),
+        ("fov_deg", ctypes.c_float),
+        ("zmin", ctypes.c_float),
+        ("zmax", ctypes.c_float),
+        ("chihview", ctypes.c_float),
+        ("model", ctypes.c_int32),
+        ("precision", ctypes.c_int32),
+        ("nmaps", ctypes.c_int32),
+        ("map_table", ctypes.c_int32 * MAXMAPS),
+        ("map_profile", ctypes.c_int32 * MAXMAPS),
+        ("max_records", ctypes.c_int64),
+        ("device", ctypes.c_int32),
+        ("flags", ctypes.c_int32),
+    ]
+
+
+class P2MStats(ctypes.Structure):
+    _fields_ = [
+        ("n_records", ctypes.c_int64),
+        ("n_shell", ctypes.c_int64),
+        ("n_painted", ctypes.c_int64),
+        ("n_enumerated", ctypes.c_int64),
+        ("hp_candidates", ctypes.c_int64),
+        ("hp_updates", ctypes.c_int64),
+        ("fs_updates", ctypes.c_int64),
+        ("n_recheck", ctypes.c_int64),
+        ("hp_sum", ctypes.c_double * MAXMAPS),
+        ("fs_sum", ctypes.c_double * MAXMAPS),
+    ]
+
+
+_lib = None
+
+
+def load_library():
+    """Load libp2m_gb300.so; raises if it has not been built (no fallback)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise P2MError(6, "%s is not built; run `python -m matt_young_mapmaking_gb300.build`"
+                       % LIB_PATH)
+    lib = ctypes.CDLL(LIB_PATH)
+    P, I32, I64, F, D, VP = (ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64, ctypes.c_float,
+                             ctypes.c_double, ctypes.c_void_p)
+    FP = ctypes.POINTER(ctypes.c_float)
+    sig = {
+        "p2m_create": (I32, [ctypes.POINTER(P2MConfig), ctypes.POINTER(VP)]),
+        "p2m_destroy": (None, [VP]),
+        "p2m_last_error": (ctypes.c_char_p, [VP]),
+        "p2m_load_table": (I32, [VP, I32, VP, I64]),
+        "p2m_reset_maps": (I32, [VP]),
+        "p2m_paint_records": (I32, [VP, VP, I64, I32]),
+        "p2m_paint_records_device": (I32, [VP, VP, I64, I32, VP]),
+        "p2m_project_halo": (I32, [VP, FP, FP, FP, FP, FP, FP, FP, FP,
+                                   ctypes.POINTER(ctypes.c_int32)]),
+        "p2m_flush": (I32, [VP]),
+        "p2m_get_healpix": (I32, [VP, I32, VP]),
+        "p2m_get_flatsky": (I32, [VP, I32, VP]),
+        "p2m_get_healpix_device": (I32, [VP, I32, VP, VP]),
+        "p2m_get_stats": (I32, [VP, ctypes.POINTER(P2MStats)]),
+        "p2m_synchronize": (I32, [VP]),
+        "p2m_get_pixel_sets": (I32, [VP, VP, VP, I64, ctypes.POINTER(ctypes.c_int64)]),
+        "p2m_make_maptable": (I32, [I32, I32, F, F, I32, I32, I32, VP,
+                                    ctypes.POINTER(ctypes.c_int64)]),
+        "p2m_generate_catalogue": (I32, [ctypes.c_uint64, I64, I64, I32, D, D, D, D, D, D, VP]),
+        "p2m_philox4x32": (None, [VP, VP, VP]),
+        "p2m_fmath_eval_device": (I32, [I32, I32, VP, VP, VP, I64]),
+        "p2m_get_timings": (I32, [VP, VP, I32]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def exported_symbols():
+    """Names the C ABI exports (include/p2m.h and include/p2m_tools.h)."""
+    return ["p2m_create", "p2m_destroy", "p2m_last_error", "p2m_load_table", "p2m_reset_maps",
+            "p2m_paint_records", "p2m_paint_records_device", "p2m_project_halo", "p2m_flush",
+            "p2m_get_healpix", "p2m_get_flatsky", "p2m_get_healpix_device", "p2m_get_stats",
+            "p2m_synchronize", "p2m_get_pixel_sets", "p2m_make_maptable",
+            "p2m_generate_catalogue", "p2m_philox4x32", "p2m_fmath_eval_device",
+            "p2m_get_timings"]
+
+
+PHASES = ["cut", "setup", "ring_scan", "emit", "rings", "count_scan", "paint", "recheck",
+          "flatsky", "readout"]
+
+
+def _ptr(a):
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+class Painter:
+    """One painter context on one GPU.
+
+    maps: sequence of (table_slot, profile) pairs; profile 1 paints the tSZ column of
+    the table with weight 1, profile 2 the optical-depth column with weight -v_los/c.
+    """
+
+    def __init__(self, nside=4096, npix_fs=0, fov_deg=10.0, zmin=0.0, zmax=1.25,
+                 chihview=0.0, model=1, precision=PREC_MIXED, maps=((0, 1),),
+                 max_records=1 << 22, device=0, flags=0):
+        self._lib = load_library()
+        cfg = P2MConfig()
+        cfg.nside, cfg.npix_fs, cfg.fov_deg = nside, npix_fs, fov_deg
+        cfg.zmin, cfg.zmax, cfg.chihview, cfg.model = zmin, zmax, chihview, model
+        if isinstance(precision, str):
+            precision = {"fp64": PREC_FP64, "mixed": PREC_MIXED}[precision]
+        cfg.precision = precision
+        maps = list(maps)
+        if not 1 <= len(maps) <= MAXMAPS:
+            raise P2MError(1, "1..%d maps" % MAXMAPS)
+        cfg.nmaps = len(maps)
+        for i, (t, p) in enumerate(maps):
+            cfg.map_table[i], cfg.map_profile[i] = t, p
+        cfg.max_records, cfg.device, cfg.flags = max_records, device, flags
+        self.cfg = cfg
+        self.nmaps = len(maps)
+        self.nside, self.npix_fs = nside, npix_fs
+        h = ctypes.c_void_p()
+        st = self._lib.p2m_create(ctypes.byref(cfg), ctypes.byref(h))
+        if st != 0:
+            msg = self._lib.p2m_last_error(h).decode() if h.value else "create failed"
+            if h.value:
+                self._lib.p2m_destroy(h)
+            raise P2MError(st, msg)
+        self._h = h
+
+    # -- plumbing ------------------------------------------------------------------
+    def _check(self, st):
+        if st != 0:
+            raise P2MError(st, self._lib.p2m_last_error(self._h).decode())
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            self._lib.p2m_destroy(self._h)
+        self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    # -- the reference's interface ---------------------------------------------------
+    def load_table(self, slot, image):
+        """loadmaptable: `image` is the table file's bytes (header + table)."""
+        buf = np.frombuffer(bytes(image) if not isinstance(image, np.ndarray) else image.tobytes(),
+                            dtype=np.uint8)
+        self._check(self._lib.p2m_load_table(self._h, slot, _ptr(buf), buf.size))
+
+    def reset(self):
+        self._check(self._lib.p2m_reset_maps(self._h))
+
+    def paint_records(self, records):
+        """Catalogue records (n, 7) or (n, 10) float32 in host memory."""
+        rec = np.ascontiguousarray(records, dtype=np.float32)
+        if rec.ndim != 2 or rec.shape[1] not in (7, 10):
+            raise P2MError(1, "records must be (n, 7) or (n, 10)")
+        self._check(self._lib.p2m_paint_records(self._h, _ptr(rec), rec.shape[0], rec.shape[1]))
+
+    def paint_records_device(self, dptr, n, nfloat, stream=None):
+        self._check(self._lib.p2m_paint_records_device(self._h, ctypes.c_void_p(dptr), n, nfloat,
+                                                       ctypes.c_void_p(stream or 0)))
+
+    def project_halo(self, x, y, z, r, chi, m, redshift, v, profile):
+        """Queue one halo with precomputed loop quantities; returns (x, y, z)/chi as the
+        reference leaves them in its caller."""
+        c = [ctypes.c_float(a) for a in (x, y, z, r, chi, m, redshift, v)]
+        p = ctypes.c_int32(profile)
+        self._check(self._lib.p2m_project_halo(self._h, *[ctypes.byref(a) for a in c],
+                                               ctypes.byref(p)))
+        return c[0].value, c[1].value, c[2].value
+
+    def flush(self):
+        self._check(self._lib.p2m_flush(self._h))
+
+    def healpix(self, m=0):
+        out = np.empty(12 * self.nside * self.nside, dtype=np.float32)
+        self._check(self._lib.p2m_get_healpix(self._h, m, _ptr(out)))
+        return out
+
+    def healpix_into(self, m, host_ptr):
+        """Read map m into host memory at host_ptr (12*nside^2 floats, e.g. pinned)."""
+        self._check(self._lib.p2m_get_healpix(self._h, m, ctypes.c_void_p(host_ptr)))
+
+    def healpix_device(self, m, dptr, stream=None):
+        self._check(self._lib.p2m_get_healpix_device(self._h, m, ctypes.c_void_p(dptr),
+                                                     ctypes.c_void_p(stream or 0)))
+
+    def flatsky(self, m=0):
+        out = np.empty(self.npix_fs * self.npix_fs, dtype=np.float32)
+        self._check(self._lib.p2m_get_flatsky(self._h, m, _ptr(out)))
+        return out
+
+    def synchronize(self):
+        self._check(self._lib.p2m_synchronize(self._h))
+
+    def stats(self):
+        s = P2MStats()
+        self._check(self._lib.p2m_get_stats(self._h, ctypes.byref(s)))
+        d = {k: getattr(s, k) for k, _ in P2MStats._fields_ if k not in ("hp_sum", "fs_sum")}
+        d["hp_sum"] = list(s.hp_sum)[: self.nmaps]
+        d["fs_sum"] = list(s.fs_sum)[: self.nmaps]
+        return d
+
+    def timings(self):
+        """Device ms per phase of the last paint call / read-out (needs FLAG_TIMING)."""
+        ms = np.zeros(len(PHASES))
+        self._check(self._lib.p2m_get_timings(self._h, _ptr(ms), len(PHASES)))
+        return dict(zip(PHASES, ms.tolist()))
+
+    def pixel_sets(self):
+        n = ctypes.c_int64()
+        self._check(self._lib.p2m_get_pixel_sets(self._h, None, None, 0, ctypes.byref(n)))
+        rec = np.empty(n.value, dtype=np.int64)
+        pix = np.empty(n.value, dtype=np.int64)
+        self._check(self._lib.p2m_get_pixel_sets(self._h, _ptr(rec), _ptr(pix), n.value,
+                                                 ctypes.byref(n)))
+        return rec, pix
+
+
+def make_maptable(model=1, nu=0.0, alpha_cmb=0.0, nchit=0, nmht=0, nrt=0, device=0):
+    """make_maptable on the GPU; returns the table file image (bytes)."""
+    lib = load_library()
+    nb = ctypes.c_int64()
+    st = lib.p2m_make_maptable(device, model, nu, alpha_cmb, nchit, nmht, nrt, None,
+                               ctypes.byref(nb))
+    if st:
+        raise P2MError(st, "make_maptable size query failed")
+    buf = np.empty(nb.value, dtype=np.uint8)
+    st = lib.p2m_make_maptable(device, model, nu, alpha_cmb, nchit, nmht, nrt, _ptr(buf),
+                               ctypes.byref(nb))
+    if st:
+        raise P2MError(st, "make_maptable failed")
+    return buf.tobytes()
+
+
+def generate_catalogue(seed, n, nfloat=10, r=(100.0, 3000.0), m=(1e12, 1e15), slope=-0.9,
+                       sigma_v=300.0, first=0):
+    """Synthetic catalogue records (n, nfloat) float32 (see include/p2m_tools.h)."""
+    lib = load_library()
+    out = np.empty((n, nfloat), dtype=np.float32)
+    st = lib.p2m_generate_catalogue(seed, first, n, nfloat, r[0], r[1], m[0], m[1], slope,
+                                    sigma_v, _ptr(out))
+    if st:
+        raise P2MError(1, "generate_catalogue: bad arguments")
+    return out

@@ -1,0 +1,718 @@
+/*
+ * p2m_capi.cu -- the C ABI of include/p2m.h: context, device buffers, and the order of
+ * kernel launches for one paint call.  The only host round trips of a paint call are
+ * two counter reads used to size the item and recheck buffers before they are filled.
+ */
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/p2m.h"
+#include "../../include/p2m_tools.h"
+#include "p2m_internal.h"
+
+enum { PH_CUT, PH_SETUP, PH_RINGSCAN, PH_EMIT, PH_RINGS, PH_COUNTSCAN, PH_PAINT, PH_RECHECK,
+       PH_FS, PH_FINAL, P2M_NPHASE };
+
+struct p2m_ctx {
+  p2m_config cfg;
+  int nsm = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  p2m_cosmo cosmo;
+  float *d_rofz = nullptr, *d_zofr = nullptr;
+  double2 *d_ringtab = nullptr;
+  p2m_tabhdr th;
+  bool th_set = false;
+  float *d_tab[P2M_MAXTABLES] = {};
+  void *d_hp_acc = nullptr, *d_fs_acc = nullptr;
+  long long hp_npix = 0, fs_npix = 0;
+  float *d_out = nullptr;
+  long long out_cap = 0;
+  /* work buffers */
+  float *d_records = nullptr;
+  long long cap_records = 0;
+  int *d_surv = nullptr;
+  HaloRec *d_halos = nullptr;
+  long long cap_halos = 0;
+  unsigned int *d_ring_hist = nullptr, *d_ring_cursor = nullptr;
+  long long *d_ring_start = nullptr;
+  RingItem *d_items = nullptr;
+  unsigned int *d_counts = nullptr;
+  long long *d_pix_off = nullptr;
+  long long cap_items = 0;
+  unsigned long long *d_fb = nullptr;
+  long long cap_fb = 0;
+  FsItem *d_fs_items = nullptr;
+  long long cap_fs = 0;
+  long long *d_set_rec = nullptr, *d_set_pix = nullptr;
+  long long cap_set = 0;
+  long long *d_scan_tmp = nullptr;
+  DevCounters *d_ctr = nullptr, *h_ctr = nullptr;
+  double *d_sums = nullptr;
+  float *d_prep = nullptr;
+  long long cap_prep = 0;
+  std::vector<float> prep;
+  std::vector<float> rofz_host, zofr_host;
+  long long cap_rec_floats = 0;
+  p2m_stats stats;
+  long long last_sets = 0;
+  /* ordering between the context stream and a caller's stream */
+  cudaEvent_t ev_join = nullptr, ev_back = nullptr;
+  /* per-phase device timing of the last paint call (P2M_FLAG_TIMING) */
+  cudaEvent_t tev[P2M_NPHASE][2] = {};
+  bool tev_used[P2M_NPHASE] = {};
+};
+
+namespace {
+
+p2m_status fail(p2m_ctx *c, p2m_status s, const std::string &msg) {
+  if (c) c->err = msg;
+  return s;
+}
+
+#define CK(call)                                                                         \
+  do {                                                                                   \
+    cudaError_t e_ = (call);                                                             \
+    if (e_ != cudaSuccess)                                                               \
+      return fail(ctx, P2M_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+template <typename T>
+cudaError_t grow(T **p, long long *cap, long long need, long long floor_n = 1024) {
+  if (need <= *cap && *p) return cudaSuccess;
+  long long n = std::max(need + need / 4, floor_n);
+  if (*p) cudaFree(*p);
+  *p = nullptr;
+  *cap = 0;
+  cudaError_t e = cudaMalloc((void **)p, sizeof(T) * (size_t)n);
+  if (e == cudaSuccess) *cap = n;
+  return e;
+}
+
+bool is_pow2(int n) { return n > 0 && (n & (n - 1)) == 0; }
+
+/* phase timing marks (no-ops unless P2M_FLAG_TIMING) */
+void tmark(p2m_ctx *ctx, int ph, int end, cudaStream_t s) {
+  if (!(ctx->cfg.flags & P2M_FLAG_TIMING)) return;
+  if (!ctx->tev[ph][end]) cudaEventCreate(&ctx->tev[ph][end]);
+  cudaEventRecord(ctx->tev[ph][end], s);
+  if (end) ctx->tev_used[ph] = true;
+}
+#define TB(ph) tmark(ctx, ph, 0, s)
+#define TE(ph) tmark(ctx, ph, 1, s)
+
+/* work queued on the context stream before this call runs first on s; work queued on
+   the context stream after this call waits for s */
+void join_in(p2m_ctx *ctx, cudaStream_t s) {
+  if (s == ctx->stream) return;
+  cudaEventRecord(ctx->ev_join, ctx->stream);
+  cudaStreamWaitEvent(s, ctx->ev_join, 0);
+}
+void join_out(p2m_ctx *ctx, cudaStream_t s) {
+  if (s == ctx->stream) return;
+  cudaEventRecord(ctx->ev_back, s);
+  cudaStreamWaitEvent(ctx->stream, ctx->ev_back, 0);
+}
+
+PaintParams make_params(const p2m_ctx *ctx, int nfloat) {
+  PaintParams P;
+  memset(&P, 0, sizeof(P));
+  const p2m_config &c = ctx->cfg;
+  P.nside = c.nside;
+  P.npix_fs = c.npix_fs;
+  P.nmaps = c.nmaps;
+  P.precision = c.precision;
+  P.flags = c.flags;
+  P.nfloat = nfloat;
+  P.model = c.model;
+  P.cosmo = ctx->cosmo;
+  const float mypi = ctx->cosmo.mypi;
+  /* pks2map.f90:92-93 */
+  P.fov = FMUL(FMUL(FDIV(c.fov_deg, 360.0f), 2.0f), mypi);
+  P.dpix = c.npix_fs > 0 ? FDIV(P.fov, (float)c.npix_fs) : 0.0f;
+  P.hf = FDIV(P.fov, 2.0f);
+  /* pks2map.f90:134-135 */
+  P.cut_low = p2m_lookup(ctx->rofz_host.data(), ctx->cosmo.drofz, c.zmin);
+  P.cut_high = p2m_lookup(ctx->rofz_host.data(), ctx->cosmo.drofz, c.zmax);
+  P.chihview = c.chihview;
+  static const float bbps_delta[3] = {200.0f, 500.0f, 200.0f}; /* bbps_profile.f90:21 */
+  P.bbps_delta = bbps_delta[c.model - 1];
+  for (int m = 0; m < P2M_MAXMAPS; m++) {
+    P.map_table[m] = m < c.nmaps ? c.map_table[m] : 0;
+    P.map_profile[m] = m < c.nmaps ? c.map_profile[m] : 1;
+    if (m < c.nmaps && c.map_profile[m] == 2) P.any_ksz = 1;
+  }
+  P.mass_fac = FMUL(FMUL(4.0f / 3.0f, mypi), ctx->cosmo.rho_0);
+  P.th = ctx->th;
+  for (int t = 0; t < P2M_MAXTABLES; t++) P.tables[t] = ctx->d_tab[t];
+  P.rofz = ctx->d_rofz;
+  P.zofr = ctx->d_zofr;
+  P.ringtab = ctx->d_ringtab;
+  if (ctx->th_set) {
+    float fr;
+    int ir;
+    p2m_rindex(&ctx->th, FMUL(ctx->th.rmint, 0.5f), &ir, &fr);
+    P.ir_c = ir;
+    P.fr_c = fr;
+  }
+  return P;
+}
+
+PaintBuffers make_buffers(const p2m_ctx *ctx, const float *records) {
+  PaintBuffers B;
+  memset(&B, 0, sizeof(B));
+  B.records = records;
+  B.surv = ctx->d_surv;
+  B.halos = ctx->d_halos;
+  B.ring_hist = ctx->d_ring_hist;
+  B.ring_cursor = ctx->d_ring_cursor;
+  B.ring_start = ctx->d_ring_start;
+  B.items = ctx->d_items;
+  B.counts = ctx->d_counts;
+  B.pix_off = ctx->d_pix_off;
+  B.fb = ctx->d_fb;
+  B.fb_cap = ctx->cap_fb;
+  B.fs_items = ctx->d_fs_items;
+  B.fs_cap = ctx->cap_fs;
+  B.hp_acc = ctx->d_hp_acc;
+  B.fs_acc = ctx->d_fs_acc;
+  B.set_rec = ctx->d_set_rec;
+  B.set_pix = ctx->d_set_pix;
+  B.set_cap = ctx->cap_set;
+  B.scan_tmp = ctx->d_scan_tmp;
+  B.ctr = ctx->d_ctr;
+  return B;
+}
+
+p2m_status check_tables(p2m_ctx *ctx) {
+  for (int m = 0; m < ctx->cfg.nmaps; m++)
+    if (!ctx->d_tab[ctx->cfg.map_table[m]])
+      return fail(ctx, P2M_ERR_STATE, "table slot " + std::to_string(ctx->cfg.map_table[m]) +
+                                          " used by map " + std::to_string(m) + " is not loaded");
+  return P2M_OK;
+}
+
+/* everything after the per-halo set-up: ring items, spans, paint, recheck, flat sky */
+p2m_status paint_halos(p2m_ctx *ctx, PaintParams &P, cudaStream_t s) {
+  PaintBuffers B = make_buffers(ctx, nullptr);
+  TB(PH_RINGSCAN);
+  if (P.nside > 0) p2m_launch_ring_scan(P, B, s);
+  TE(PH_RINGSCAN);
+  CK(cudaMemcpyAsync(ctx->h_ctr, ctx->d_ctr, sizeof(DevCounters), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  long long n_halo = (long long)ctx->h_ctr->n_halo;
+  long long n_items = P.nside > 0 ? (long long)ctx->h_ctr->n_items : 0;
+  long long n_fs = (long long)ctx->h_ctr->n_fs_rows;
+  if (ctx->h_ctr->err & P2M_DEVERR_RADIUS)
+    return fail(ctx, P2M_ERR_BADARG, "a halo's disc radius exceeds pi (query_disc aborts)");
+  {
+    long long c1 = ctx->cap_items, c2 = ctx->cap_items;
+    CK(grow(&ctx->d_items, &ctx->cap_items, std::max(n_items, 1LL)));
+    CK(grow(&ctx->d_counts, &c1, ctx->cap_items, ctx->cap_items));
+    CK(grow(&ctx->d_pix_off, &c2, ctx->cap_items, ctx->cap_items));
+  }
+  CK(grow(&ctx->d_fs_items, &ctx->cap_fs, std::max(n_fs, 1LL)));
+  B = make_buffers(ctx, nullptr);
+  if (n_halo > 0) {
+    TB(PH_EMIT);
+    p2m_launch_emit(P, B, n_halo, s, ctx->nsm);
+    TE(PH_EMIT);
+    if (P.nside > 0 && n_items > 0) {
+      TB(PH_RINGS);
+      p2m_launch_rings(P, B, n_items, s, ctx->nsm);
+      TE(PH_RINGS);
+      TB(PH_COUNTSCAN);
+      p2m_launch_count_scan(P, B, s);
+      TE(PH_COUNTSCAN);
+      CK(cudaMemcpyAsync(ctx->h_ctr, ctx->d_ctr, sizeof(DevCounters), cudaMemcpyDeviceToHost, s));
+      CK(cudaStreamSynchronize(s));
+      long long n_pix = (long long)ctx->h_ctr->n_pix;
+      if (P.precision == P2M_PREC_MIXED) {
+        CK(grow(&ctx->d_fb, &ctx->cap_fb, n_pix / 4 + (1LL << 20)));
+        B = make_buffers(ctx, nullptr);
+      }
+      TB(PH_PAINT);
+      p2m_launch_paint(P, B, s, ctx->nsm);
+      TE(PH_PAINT);
+      if (P.precision == P2M_PREC_MIXED) {
+        TB(PH_RECHECK);
+        p2m_launch_recheck(P, B, s, ctx->nsm);
+        TE(PH_RECHECK);
+      }
+    }
+    if (P.npix_fs > 0 && n_fs > 0) {
+      TB(PH_FS);
+      p2m_launch_paint_fs(P, B, s, ctx->nsm);
+      TE(PH_FS);
+    }
+  }
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(ctx->h_ctr, ctx->d_ctr, sizeof(DevCounters), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  const DevCounters &h = *ctx->h_ctr;
+  if (h.err & P2M_DEVERR_FB_OVERFLOW)
+    return fail(ctx, P2M_ERR_CAPACITY, "recheck buffer overflow (maps are incomplete)");
+  if (h.err & P2M_DEVERR_FS_OVERFLOW)
+    return fail(ctx, P2M_ERR_CAPACITY, "flat-sky row buffer overflow (maps are incomplete)");
+  ctx->stats.n_shell += (long long)h.n_shell;
+  ctx->stats.n_painted += (long long)h.n_surv;
+  ctx->stats.n_enumerated += (long long)h.n_halo;
+  ctx->stats.hp_candidates += (long long)h.n_pix;
+  ctx->stats.hp_updates += (long long)h.hp_updates;
+  ctx->stats.fs_updates += (long long)h.fs_updates;
+  ctx->stats.n_recheck += (long long)h.n_recheck;
+  ctx->last_sets = (long long)h.n_sets;
+  return P2M_OK;
+}
+
+p2m_status begin_call(p2m_ctx *ctx, long long n_halos_max, cudaStream_t s) {
+  CK(grow(&ctx->d_surv, &ctx->cap_records, std::max(n_halos_max, 1LL)));
+  long long hcap = ctx->cap_halos;
+  CK(grow(&ctx->d_halos, &hcap, std::max(n_halos_max, 1LL)));
+  ctx->cap_halos = hcap;
+  for (int k = 0; k < P2M_NPHASE; k++) ctx->tev_used[k] = false;
+  CK(cudaMemsetAsync(ctx->d_ctr, 0, sizeof(DevCounters), s));
+  if (ctx->cfg.nside > 0) {
+    size_t nr = sizeof(unsigned int) * (size_t)(4 * ctx->cfg.nside);
+    CK(cudaMemsetAsync(ctx->d_ring_hist, 0, nr, s));
+    CK(cudaMemsetAsync(ctx->d_ring_cursor, 0, nr, s));
+  }
+  return P2M_OK;
+}
+
+p2m_status flush_prepared(p2m_ctx *ctx) {
+  if (ctx->prep.empty()) return P2M_OK;
+  p2m_status st = check_tables(ctx);
+  if (st) return st;
+  cudaStream_t s = ctx->stream;
+  long long n = (long long)ctx->prep.size() / 9;
+  CK(grow(&ctx->d_prep, &ctx->cap_prep, (long long)ctx->prep.size()));
+  CK(cudaMemcpyAsync(ctx->d_prep, ctx->prep.data(), sizeof(float) * ctx->prep.size(),
+                     cudaMemcpyHostToDevice, s));
+  st = begin_call(ctx, n, s);
+  if (st) return st;
+  PaintParams P = make_params(ctx, 7);
+  PaintBuffers B = make_buffers(ctx, nullptr);
+  TB(PH_SETUP);
+  p2m_launch_prepared(P, B, ctx->d_prep, n, s, ctx->nsm);
+  TE(PH_SETUP);
+  ctx->prep.clear();
+  return paint_halos(ctx, P, s);
+}
+
+p2m_status paint_device(p2m_ctx *ctx, const float *d_rec, long long nrec, int nfloat,
+                        cudaStream_t s) {
+  if (nfloat != 7 && nfloat != 10) return fail(ctx, P2M_ERR_BADARG, "nfloat must be 7 or 10");
+  if (nrec < 0) return fail(ctx, P2M_ERR_BADARG, "negative record count");
+  if (nrec > (1LL << 31) - 1) return fail(ctx, P2M_ERR_BADARG, "more than 2^31-1 records per call");
+  p2m_status st = check_tables(ctx);
+  if (st) return st;
+  st = flush_prepared(ctx);
+  if (st) return st;
+  if (nrec == 0) return P2M_OK;
+  join_in(ctx, s);
+  st = begin_call(ctx, nrec, s);
+  if (st) return st;
+  PaintParams P = make_params(ctx, nfloat);
+  PaintBuffers B = make_buffers(ctx, d_rec);
+  TB(PH_CUT);
+  p2m_launch_cut(P, B, nrec, s, ctx->nsm);
+  TE(PH_CUT);
+  TB(PH_SETUP);
+  p2m_launch_setup(P, B, nrec, s, ctx->nsm);
+  TE(PH_SETUP);
+  st = paint_halos(ctx, P, s);
+  join_out(ctx, s);
+  if (st) return st;
+  ctx->stats.n_records += nrec;
+  return P2M_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+p2m_status p2m_create(const p2m_config *cfg, p2m_ctx **out) {
+  p2m_ctx *ctx = nullptr;
+  if (!cfg || !out) return P2M_ERR_BADARG;
+  *out = nullptr;
+  if (cfg->nside != 0 && (!is_pow2(cfg->nside) || cfg->nside > 8192)) return P2M_ERR_BADARG;
+  if (cfg->npix_fs < 0 || cfg->npix_fs > 65536) return P2M_ERR_BADARG;
+  if (cfg->nside == 0 && cfg->npix_fs == 0) return P2M_ERR_BADARG;
+  if (cfg->model < 1 || cfg->model > 3) return P2M_ERR_BADARG;
+  if (cfg->nmaps < 1 || cfg->nmaps > P2M_MAXMAPS) return P2M_ERR_BADARG;
+  if (cfg->precision != P2M_PREC_FP64 && cfg->precision != P2M_PREC_MIXED) return P2M_ERR_BADARG;
+  for (int m = 0; m < cfg->nmaps; m++) {
+    if (cfg->map_table[m] < 0 || cfg->map_table[m] >= P2M_MAXTABLES) return P2M_ERR_BADARG;
+    if (cfg->map_profile[m] != 1 && cfg->map_profile[m] != 2) return P2M_ERR_BADARG;
+  }
+  ctx = new (std::nothrow) p2m_ctx();
+  if (!ctx) return P2M_ERR_NOMEM;
+  ctx->cfg = *cfg;
+  memset(&ctx->stats, 0, sizeof(ctx->stats));
+  *out = ctx;
+  CK(cudaSetDevice(cfg->device));
+  CK(cudaDeviceGetAttribute(&ctx->nsm, cudaDevAttrMultiProcessorCount, cfg->device));
+  CK(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+  CK(cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming));
+  CK(cudaEventCreateWithFlags(&ctx->ev_back, cudaEventDisableTiming));
+  /* cosmology tables, built once on the host with the reference's float sequence */
+  ctx->rofz_host.assign(P2M_NZTAB, 0.0f);
+  ctx->zofr_host.assign(P2M_NZTAB, 0.0f);
+  p2m_cosmo_build(&ctx->cosmo, ctx->rofz_host.data(), ctx->zofr_host.data());
+  CK(cudaMalloc((void **)&ctx->d_rofz, sizeof(float) * P2M_NZTAB));
+  CK(cudaMalloc((void **)&ctx->d_zofr, sizeof(float) * P2M_NZTAB));
+  CK(cudaMemcpy(ctx->d_rofz, ctx->rofz_host.data(), sizeof(float) * P2M_NZTAB, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(ctx->d_zofr, ctx->zofr_host.data(), sizeof(float) * P2M_NZTAB, cudaMemcpyHostToDevice));
+  if (cfg->nside > 0) {
+    int nr = 4 * cfg->nside;
+    std::vector<double2> rt((size_t)nr);
+    rt[0] = make_double2(1.0, 0.0);
+    for (int r = 1; r < nr; r++) {
+      double z, s;
+      p2m_ring_z_sth(cfg->nside, r, &z, &s);
+      rt[(size_t)r] = make_double2(z, s);
+    }
+    CK(cudaMalloc((void **)&ctx->d_ringtab, sizeof(double2) * (size_t)nr));
+    CK(cudaMemcpy(ctx->d_ringtab, rt.data(), sizeof(double2) * (size_t)nr, cudaMemcpyHostToDevice));
+    CK(cudaMalloc((void **)&ctx->d_ring_hist, sizeof(unsigned int) * (size_t)nr));
+    CK(cudaMalloc((void **)&ctx->d_ring_cursor, sizeof(unsigned int) * (size_t)nr));
+    CK(cudaMalloc((void **)&ctx->d_ring_start, sizeof(long long) * (size_t)nr));
+    ctx->hp_npix = 12LL * cfg->nside * cfg->nside;
+    CK(cudaMalloc(&ctx->d_hp_acc, 8 * (size_t)cfg->nmaps * (size_t)ctx->hp_npix));
+  }
+  if (cfg->npix_fs > 0) {
+    ctx->fs_npix = (long long)cfg->npix_fs * cfg->npix_fs;
+    CK(cudaMalloc(&ctx->d_fs_acc, 8 * (size_t)cfg->nmaps * (size_t)ctx->fs_npix));
+  }
+  CK(cudaMalloc((void **)&ctx->d_scan_tmp, sizeof(long long) * 1024));
+  CK(cudaMalloc((void **)&ctx->d_ctr, sizeof(DevCounters)));
+  CK(cudaMallocHost((void **)&ctx->h_ctr, sizeof(DevCounters)));
+  CK(cudaMalloc((void **)&ctx->d_sums, sizeof(double) * 2 * P2M_MAXMAPS));
+  if (cfg->flags & P2M_FLAG_RECORD_SETS) {
+    ctx->cap_set = 1LL << 24;
+    CK(cudaMalloc((void **)&ctx->d_set_rec, sizeof(long long) * (size_t)ctx->cap_set));
+    CK(cudaMalloc((void **)&ctx->d_set_pix, sizeof(long long) * (size_t)ctx->cap_set));
+  }
+  long long nrec = std::max<long long>(cfg->max_records, 1024);
+  CK(grow(&ctx->d_surv, &ctx->cap_records, nrec));
+  CK(grow(&ctx->d_halos, &ctx->cap_halos, nrec));
+  p2m_status st = p2m_reset_maps(ctx);
+  if (st) return st;
+  CK(cudaStreamSynchronize(ctx->stream));
+  return P2M_OK;
+}
+
+void p2m_destroy(p2m_ctx *ctx) {
+  if (!ctx) return;
+  cudaSetDevice(ctx->cfg.device);
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  void *ptrs[] = {ctx->d_rofz, ctx->d_zofr, ctx->d_ringtab, ctx->d_hp_acc, ctx->d_fs_acc,
+                  ctx->d_out, ctx->d_records, ctx->d_surv, ctx->d_halos, ctx->d_ring_hist,
+                  ctx->d_ring_cursor, ctx->d_ring_start, ctx->d_items, ctx->d_counts,
+                  ctx->d_pix_off, ctx->d_fb, ctx->d_fs_items, ctx->d_set_rec, ctx->d_set_pix,
+                  ctx->d_scan_tmp, ctx->d_ctr, ctx->d_sums, ctx->d_prep};
+  for (void *p : ptrs)
+    if (p) cudaFree(p);
+  for (int t = 0; t < P2M_MAXTABLES; t++)
+    if (ctx->d_tab[t]) cudaFree(ctx->d_tab[t]);
+  if (ctx->h_ctr) cudaFreeHost(ctx->h_ctr);
+  if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
+  if (ctx->ev_back) cudaEventDestroy(ctx->ev_back);
+  for (int k = 0; k < P2M_NPHASE; k++)
+    for (int e = 0; e < 2; e++)
+      if (ctx->tev[k][e]) cudaEventDestroy(ctx->tev[k][e]);
+  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+}
+
+const char *p2m_last_error(const p2m_ctx *ctx) {
+  if (!ctx) return "null context";
+  return ctx->err.c_str();
+}
+
+p2m_status p2m_load_table(p2m_ctx *ctx, int32_t slot, const void *image, int64_t nbytes) {
+  if (!ctx) return P2M_ERR_BADARG;
+  if (slot < 0 || slot >= P2M_MAXTABLES) return fail(ctx, P2M_ERR_BADARG, "table slot out of range");
+  if (!image || nbytes < 36) return fail(ctx, P2M_ERR_IO, "table image shorter than its header");
+  p2m_tabhdr t;
+  memset(&t, 0, sizeof(t));
+  const char *b = (const char *)image;
+  memcpy(&t.nchit, b + 0, 4);
+  memcpy(&t.nmht, b + 4, 4);
+  memcpy(&t.nrt, b + 8, 4);
+  memcpy(&t.chimint, b + 12, 4);
+  memcpy(&t.chimaxt, b + 16, 4);
+  memcpy(&t.mhmint, b + 20, 4);
+  memcpy(&t.mhmaxt, b + 24, 4);
+  memcpy(&t.rmint, b + 28, 4);
+  memcpy(&t.rmaxt, b + 32, 4);
+  if (t.nchit < 2 || t.nmht < 2 || t.nrt < 2 || t.nchit > 100000 || t.nmht > 100000 || t.nrt > 100000)
+    return fail(ctx, P2M_ERR_IO, "table header sizes out of range");
+  if (!(t.chimint > 0 && t.chimaxt > t.chimint && t.mhmint > 0 && t.mhmaxt > t.mhmint &&
+        t.rmint > 0 && t.rmaxt > t.rmint))
+    return fail(ctx, P2M_ERR_IO, "table header bounds invalid");
+  p2m_tabhdr_derive(&t);
+  if (t.nelem > (1LL << 30)) return fail(ctx, P2M_ERR_IO, "table too large");
+  if (nbytes < 36 + 4 * t.nelem) return fail(ctx, P2M_ERR_IO, "table image shorter than its header says");
+  if (ctx->th_set) {
+    bool same = t.nchit == ctx->th.nchit && t.nmht == ctx->th.nmht && t.nrt == ctx->th.nrt &&
+                t.chimint == ctx->th.chimint && t.chimaxt == ctx->th.chimaxt &&
+                t.mhmint == ctx->th.mhmint && t.mhmaxt == ctx->th.mhmaxt &&
+                t.rmint == ctx->th.rmint && t.rmaxt == ctx->th.rmaxt;
+    int loaded = 0;
+    for (int k = 0; k < P2M_MAXTABLES; k++) loaded += (ctx->d_tab[k] != nullptr && k != slot);
+    if (!same && loaded) return fail(ctx, P2M_ERR_BADARG, "all tables of a context must share one header");
+  }
+  CK(cudaSetDevice(ctx->cfg.device));
+  if (ctx->d_tab[slot]) cudaFree(ctx->d_tab[slot]);
+  ctx->d_tab[slot] = nullptr;
+  CK(cudaMalloc((void **)&ctx->d_tab[slot], sizeof(float) * (size_t)t.nelem));
+  CK(cudaMemcpy(ctx->d_tab[slot], b + 36, sizeof(float) * (size_t)t.nelem, cudaMemcpyHostToDevice));
+  ctx->th = t;
+  ctx->th_set = true;
+  return P2M_OK;
+}
+
+p2m_status p2m_reset_maps(p2m_ctx *ctx) {
+  if (!ctx) return P2M_ERR_BADARG;
+  CK(cudaSetDevice(ctx->cfg.device));
+  ctx->prep.clear();
+  if (ctx->d_hp_acc)
+    CK(cudaMemsetAsync(ctx->d_hp_acc, 0, 8 * (size_t)ctx->cfg.nmaps * (size_t)ctx->hp_npix, ctx->stream));
+  if (ctx->d_fs_acc)
+    CK(cudaMemsetAsync(ctx->d_fs_acc, 0, 8 * (size_t)ctx->cfg.nmaps * (size_t)ctx->fs_npix, ctx->stream));
+  memset(&ctx->stats, 0, sizeof(ctx->stats));
+  return P2M_OK;
+}
+
+p2m_status p2m_paint_records(p2m_ctx *ctx, const float *records, int64_t nrec, int32_t nfloat) {
+  if (!ctx) return P2M_ERR_BADARG;
+  if (nrec > 0 && !records) return fail(ctx, P2M_ERR_BADARG, "null records");
+  CK(cudaSetDevice(ctx->cfg.device));
+  if (nfloat != 7 && nfloat != 10) return fail(ctx, P2M_ERR_BADARG, "nfloat must be 7 or 10");
+  long long chunk = std::max<long long>(ctx->cfg.max_records, 1024);
+  for (long long off = 0; off < nrec; off += chunk) {
+    long long n = std::min(chunk, nrec - off);
+    long long need = n * nfloat;
+    CK(grow(&ctx->d_records, &ctx->cap_rec_floats, need));
+    CK(cudaMemcpyAsync(ctx->d_records, records + off * nfloat, sizeof(float) * (size_t)need,
+                       cudaMemcpyHostToDevice, ctx->stream));
+    p2m_status st = paint_device(ctx, ctx->d_records, n, nfloat, ctx->stream);
+    if (st) return st;
+  }
+  return P2M_OK;
+}
+
+p2m_status p2m_paint_records_device(p2m_ctx *ctx, const float *d_records, int64_t nrec,
+                                    int32_t nfloat, void *stream) {
+  if (!ctx) return P2M_ERR_BADARG;
+  if (nrec > 0 && !d_records) return fail(ctx, P2M_ERR_BADARG, "null records");
+  CK(cudaSetDevice(ctx->cfg.device));
+  cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
+  return paint_device(ctx, d_records, nrec, nfloat, s);
+}
+
+p2m_status p2m_project_halo(p2m_ctx *ctx, float *x, float *y, float *z, const float *r,
+                            const float *chi, const float *m, const float *redshift,
+                            const float *v, const int32_t *profile) {
+  if (!ctx || !x || !y || !z || !r || !chi || !m || !redshift || !v || !profile)
+    return P2M_ERR_BADARG;
+  if (*profile != 1 && *profile != 2) return fail(ctx, P2M_ERR_BADARG, "profile must be 1 or 2");
+  float q[9] = {*x, *y, *z, *r, *chi, *m, *redshift, *v, (float)*profile};
+  ctx->prep.insert(ctx->prep.end(), q, q + 9);
+  /* haloproject.f90:97-99 divides the caller's x, y, z by chi */
+  *x = FDIV(*x, *chi);
+  *y = FDIV(*y, *chi);
+  *z = FDIV(*z, *chi);
+  return P2M_OK;
+}
+
+p2m_status p2m_flush(p2m_ctx *ctx) {
+  if (!ctx) return P2M_ERR_BADARG;
+  CK(cudaSetDevice(ctx->cfg.device));
+  return flush_prepared(ctx);
+}
+
+static p2m_status finalize_map(p2m_ctx *ctx, bool hp, int32_t map, float *d_out, cudaStream_t s) {
+  if (map < 0 || map >= ctx->cfg.nmaps) return fail(ctx, P2M_ERR_BADARG, "map index out of range");
+  if (hp && ctx->cfg.nside <= 0) return fail(ctx, P2M_ERR_BADARG, "no HEALPix map configured");
+  if (!hp && ctx->cfg.npix_fs <= 0) return fail(ctx, P2M_ERR_BADARG, "no flat-sky map configured");
+  p2m_status st = flush_prepared(ctx);
+  if (st) return st;
+  PaintParams P = make_params(ctx, 7);
+  double *sum = ctx->d_sums + (hp ? 0 : P2M_MAXMAPS) + map;
+  join_in(ctx, s);
+  CK(cudaMemsetAsync(sum, 0, sizeof(double), s));
+  TB(PH_FINAL);
+  p2m_launch_finalize(P, hp ? ctx->d_hp_acc : ctx->d_fs_acc, hp ? ctx->hp_npix : ctx->fs_npix, map,
+                      d_out, sum, s, ctx->nsm);
+  TE(PH_FINAL);
+  join_out(ctx, s);
+  CK(cudaGetLastError());
+  return P2M_OK;
+}
+
+p2m_status p2m_get_healpix_device(p2m_ctx *ctx, int32_t map, float *d_out, void *stream) {
+  if (!ctx || !d_out) return P2M_ERR_BADARG;
+  CK(cudaSetDevice(ctx->cfg.device));
+  cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
+  return finalize_map(ctx, true, map, d_out, s);
+}
+
+static p2m_status get_host(p2m_ctx *ctx, bool hp, int32_t map, float *out) {
+  if (!ctx || !out) return P2M_ERR_BADARG;
+  CK(cudaSetDevice(ctx->cfg.device));
+  long long n = hp ? ctx->hp_npix : ctx->fs_npix;
+  CK(grow(&ctx->d_out, &ctx->out_cap, std::max(n, 1LL)));
+  p2m_status st = finalize_map(ctx, hp, map, ctx->d_out, ctx->stream);
+  if (st) return st;
+  CK(cudaMemcpyAsync(out, ctx->d_out, sizeof(float) * (size_t)n, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return P2M_OK;
+}
+
+p2m_status p2m_get_healpix(p2m_ctx *ctx, int32_t map, float *out) { return get_host(ctx, true, map, out); }
+p2m_status p2m_get_flatsky(p2m_ctx *ctx, int32_t map, float *out) { return get_host(ctx, false, map, out); }
+
+p2m_status p2m_get_stats(p2m_ctx *ctx, p2m_stats *out) {
+  if (!ctx || !out) return P2M_ERR_BADARG;
+  CK(cudaSetDevice(ctx->cfg.device));
+  p2m_status st = flush_prepared(ctx);
+  if (st) return st;
+  *out = ctx->stats;
+  double sums[2 * P2M_MAXMAPS];
+  CK(cudaStreamSynchronize(ctx->stream));
+  CK(cudaMemcpy(sums, ctx->d_sums, sizeof(sums), cudaMemcpyDeviceToHost));
+  for (int m = 0; m < P2M_MAXMAPS; m++) {
+    out->hp_sum[m] = sums[m];
+    out->fs_sum[m] = sums[P2M_MAXMAPS + m];
+  }
+  return P2M_OK;
+}
+
+p2m_status p2m_get_timings(p2m_ctx *ctx, double *ms, int32_t n) {
+  if (!ctx || !ms) return P2M_ERR_BADARG;
+  if (!(ctx->cfg.flags & P2M_FLAG_TIMING))
+    return fail(ctx, P2M_ERR_STATE, "context was created without P2M_FLAG_TIMING");
+  CK(cudaSetDevice(ctx->cfg.device));
+  for (int k = 0; k < n; k++) {
+    ms[k] = 0.0;
+    if (k < P2M_NPHASE && ctx->tev_used[k]) {
+      float t = 0.0f;
+      CK(cudaEventSynchronize(ctx->tev[k][1]));
+      CK(cudaEventElapsedTime(&t, ctx->tev[k][0], ctx->tev[k][1]));
+      ms[k] = (double)t;
+    }
+  }
+  return P2M_OK;
+}
+
+p2m_status p2m_synchronize(p2m_ctx *ctx) {
+  if (!ctx) return P2M_ERR_BADARG;
+  CK(cudaSetDevice(ctx->cfg.device));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return P2M_OK;
+}
+
+p2m_status p2m_get_pixel_sets(p2m_ctx *ctx, int64_t *rec, int64_t *pix, int64_t cap, int64_t *n) {
+  if (!ctx || !n) return P2M_ERR_BADARG;
+  if (!(ctx->cfg.flags & P2M_FLAG_RECORD_SETS))
+    return fail(ctx, P2M_ERR_STATE, "context was created without P2M_FLAG_RECORD_SETS");
+  CK(cudaSetDevice(ctx->cfg.device));
+  *n = ctx->last_sets;
+  long long k = std::min<long long>(std::min<long long>(cap, ctx->last_sets), ctx->cap_set);
+  if (ctx->last_sets > ctx->cap_set)
+    return fail(ctx, P2M_ERR_CAPACITY, "pixel-set buffer overflow");
+  if (k > 0 && rec && pix) {
+    CK(cudaMemcpy(rec, ctx->d_set_rec, sizeof(long long) * (size_t)k, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(pix, ctx->d_set_pix, sizeof(long long) * (size_t)k, cudaMemcpyDeviceToHost));
+  }
+  return P2M_OK;
+}
+
+p2m_status p2m_make_maptable(int32_t device, int32_t model, float nu, float alpha_cmb,
+                             int32_t nchit, int32_t nmht, int32_t nrt, void *image,
+                             int64_t *nbytes) {
+  p2m_ctx *ctx = nullptr; /* for CK: errors carry no context message */
+  if (!nbytes) return P2M_ERR_BADARG;
+  if (nchit <= 0) nchit = 100;
+  if (nmht <= 0) nmht = 100;
+  if (nrt <= 0) nrt = 200;
+  if (model < 1 || model > 3 || nchit < 2 || nmht < 2 || nrt < 2) return P2M_ERR_BADARG;
+  p2m_tabhdr th;
+  memset(&th, 0, sizeof(th));
+  th.nchit = nchit;
+  th.nmht = nmht;
+  th.nrt = nrt;
+  th.chimint = 1e2f; /* maptable.f90:69-85 */
+  th.chimaxt = 7e3f;
+  th.mhmint = 1e13f;
+  th.mhmaxt = 1e16f;
+  th.rmint = 1e-2f;
+  th.rmaxt = 10.0f;
+  p2m_tabhdr_derive(&th);
+  *nbytes = 36 + 4 * th.nelem;
+  if (!image) return P2M_OK;
+  CK(cudaSetDevice(device));
+  p2m_cosmo cosmo;
+  std::vector<float> rofz(P2M_NZTAB), zofr(P2M_NZTAB);
+  p2m_cosmo_build(&cosmo, rofz.data(), zofr.data());
+  /* maptable.f90:56-64 with cosmology.f90:231-251 constants (pi is the float literal;
+     mp, mue, 1.932 and 8. are single-precision literals) */
+  const double PI_D = P2M_COSMO_PI;
+  const double sigmat = 6.65246e-25, me = 9.109383e-28, mp = (double)1.67e-24f, c = 2.99792458e10;
+  const double msun = 1.9891e33, Mpc2km = 3.08567758e19, Mpc = 3.08567758e24, kpc = 3.08567758e21;
+  const double H100 = 1e2 / Mpc2km;
+  const double ypermass = ((((((3.0 * sigmat) * (H100 * H100)) / 8.0) / PI_D) / me) / (c * c) * msun) /
+                          (double)1.932f;
+  const double taupersigma =
+      (((sigmat / (double)1.136f) / mp) * msun / ((kpc * kpc) * kpc)) * Mpc * 1e10;
+  static const float bbps_delta[3] = {200.0f, 500.0f, 200.0f};
+  float Delta = bbps_delta[model - 1];
+  float m2rfac = (float)pow(((double)(3.0f / 4.0f) / PI_D) / (double)Delta, (double)(1.0f / 3.0f));
+  TableConsts K;
+  K.y0 = (float)((double)FMUL(FMUL(cosmo.fb, Delta), FMUL(cosmo.h, cosmo.h)) * ypermass);
+  K.tau0 = (float)((taupersigma * (double)FMUL(cosmo.h, cosmo.h)) * (double)m2rfac);
+  K.x0const = FMUL(0.017612f, nu);
+  K.nu = nu;
+  K.alpha = alpha_cmb;
+  K.model = model;
+  PaintParams P;
+  memset(&P, 0, sizeof(P));
+  P.cosmo = cosmo;
+  float *d_rofz = nullptr, *d_zofr = nullptr, *d_tab = nullptr;
+  CK(cudaMalloc((void **)&d_rofz, sizeof(float) * P2M_NZTAB));
+  CK(cudaMalloc((void **)&d_zofr, sizeof(float) * P2M_NZTAB));
+  CK(cudaMalloc((void **)&d_tab, sizeof(float) * (size_t)th.nelem));
+  CK(cudaMemcpy(d_rofz, rofz.data(), sizeof(float) * P2M_NZTAB, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(d_zofr, zofr.data(), sizeof(float) * P2M_NZTAB, cudaMemcpyHostToDevice));
+  P.rofz = d_rofz;
+  P.zofr = d_zofr;
+  p2m_launch_maptable(P, K, th, d_tab, 0);
+  CK(cudaGetLastError());
+  char *b = (char *)image;
+  memcpy(b + 0, &th.nchit, 4);
+  memcpy(b + 4, &th.nmht, 4);
+  memcpy(b + 8, &th.nrt, 4);
+  memcpy(b + 12, &th.chimint, 4);
+  memcpy(b + 16, &th.chimaxt, 4);
+  memcpy(b + 20, &th.mhmint, 4);
+  memcpy(b + 24, &th.mhmaxt, 4);
+  memcpy(b + 28, &th.rmint, 4);
+  memcpy(b + 32, &th.rmaxt, 4);
+  CK(cudaMemcpy(b + 36, d_tab, sizeof(float) * (size_t)th.nelem, cudaMemcpyDeviceToHost));
+  cudaFree(d_rofz);
+  cudaFree(d_zofr);
+  cudaFree(d_tab);
+  return P2M_OK;
+}
+
+}  // extern "C"
