@@ -259,6 +259,8 @@ p2m_status paint_halos(p2m_ctx *ctx, PaintParams &P, cudaStream_t s) {
   const DevCounters &h = *ctx->h_ctr;
   if (h.err & P2M_DEVERR_FB_OVERFLOW)
     return fail(ctx, P2M_ERR_CAPACITY, "recheck buffer overflow (maps are incomplete)");
+  if (h.err & P2M_DEVERR_ITEMS)
+    return fail(ctx, P2M_ERR_STATE, "candidate walk exceeded its round bound (maps are incomplete)");
   if (h.err & P2M_DEVERR_FS_OVERFLOW)
     return fail(ctx, P2M_ERR_CAPACITY, "flat-sky row buffer overflow (maps are incomplete)");
   ctx->stats.n_shell += (long long)h.n_shell;

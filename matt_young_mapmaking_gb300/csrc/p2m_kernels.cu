@@ -630,7 +630,12 @@ __global__ void __launch_bounds__(256) k_paint(PaintParams P, PaintBuffers B) {
     for (long long base = p0; base < p1; base += 32) {
       long long p = base + lane;
       bool todo = p < p1;
-      while (__any_sync(FULL, todo)) {
+      /* every round serves at least the lowest pending lane: <= 32 rounds */
+      for (int round = 0; __any_sync(FULL, todo); round++) {
+        if (round >= 64) {
+          atomicOr(&B.ctr->err, (unsigned)P2M_DEVERR_ITEMS);
+          break;
+        }
         /* slide the 32-item window so that it starts at the item holding the lowest
            pending pixel */
         long long pmin = todo ? p : (1LL << 62);
