@@ -208,6 +208,8 @@ def run_ours(args):
 
     def step(pt):
         pt.reset()
+        for m in range(len(MAPS)):  # the sweep writes the maps in place
+            pt.bind_healpix_device(m, outs[m].data_ptr())
         pt.paint_records_device(d_rec.data_ptr(), N, 10, stream.cuda_stream)
         for m in range(len(MAPS)):
             pt.healpix_device(m, outs[m].data_ptr(), stream.cuda_stream)
@@ -247,6 +249,8 @@ def run_ours(args):
     # end to end through the C ABI with host buffers
     def e2e_step():
         pt.reset()
+        for m in range(len(MAPS)):
+            pt.bind_healpix_device(m, 0)
         pt.paint_records(h_rec.numpy())
         for m in range(len(MAPS)):
             pt.healpix_into(m, h_outs[m].data_ptr())
@@ -272,14 +276,15 @@ def run_ours(args):
         pass
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
     peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
-    s_acc = 8
+    # algorithmic HBM bytes per launch: the catalogue is read once by the cut; the mixed
+    # sweep accumulates in L2 and writes each output pixel once; the plain path reads and
+    # writes an 8-byte accumulator per update and reads it once more at read-out
     alg = {
-        "paint": upd * 2 * s_acc,                       # read-modify-write of the accumulator
-        "readout": len(MAPS) * npix * (s_acc + 4),      # accumulator read + float write
-        "cut": N * 40,                                  # one pass over the records
+        "cut": N * 40,
+        "paint": (len(MAPS) * npix * 4 if args.precision == "mixed" else upd * 16),
+        "readout": len(MAPS) * npix * (8 + 4),
     }
-    dom = max(("paint", "readout", "cut"), key=lambda k: phases.get(k, 0.0) * (
-        len(MAPS) if k == "readout" else 1))
+    dom = max(alg, key=lambda k: phases.get(k, 0.0))
     dom_ms = phases[dom]
     achieved = alg[dom] / (dom_ms * 1e-3) / 1e9 if dom_ms > 0 else None
     roof = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak,
@@ -307,7 +312,9 @@ def run_ours(args):
            "e2e": {"value": total_halos / (e2e_ms * 1e-3), "unit": "halos/s",
                    "ms_per_step": e2e_ms, "h2d_bytes_per_step": int(rec.nbytes),
                    "d2h_bytes_per_step": int(len(MAPS) * npix * 4)}}
-    nlaunch = 2 + 1 + 1 + 1 + 1 + 3 + 1 + (1 if args.precision == "mixed" else 0) + len(MAPS)
+    # cut, set-up, 3-kernel item scan, items | band scan, band scatter, 3-kernel candidate
+    # scan, unit queue + sweep (mixed) or paint + read-out (plain)
+    nlaunch = 2 + 3 + 1 + 1 + 1 + 3 + 2
     out["gpu_launches"] = nlaunch * args.steps
 
     if not args.no_plain and args.precision == "mixed":

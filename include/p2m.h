@@ -55,7 +55,9 @@ enum { P2M_LAYOUT_7 = 7, P2M_LAYOUT_10 = 10 };
 enum {
   P2M_FLAG_RECORD_SETS = 1, /* keep (record index, pixel) of every HEALPix deposit */
   P2M_FLAG_ALL_HALOS = 2,   /* enumerate halos whose table value is identically zero */
-  P2M_FLAG_TIMING = 4       /* record per-phase device times (p2m_get_timings) */
+  P2M_FLAG_TIMING = 4,      /* record per-phase device times (p2m_get_timings) */
+  P2M_FLAG_VALIDATE = 8     /* mixed precision: also run the exact path for every candidate
+                               and count disagreements (p2m_stats.val_*); slow */
 };
 
 #define P2M_MAXMAPS 8
@@ -87,6 +89,9 @@ typedef struct p2m_stats {
   int64_t hp_updates;  /* (halo, pixel) pairs inside the disc */
   int64_t fs_updates;  /* flat-sky (halo, pixel) pairs inside the disc */
   int64_t n_recheck;   /* pixels decided by the exact FP64 recheck (mixed precision) */
+  int64_t val_checked, val_bad_set, val_bad_index; /* P2M_FLAG_VALIDATE: candidates compared,
+                          disc decisions and table indices that disagree with the exact path */
+  float val_max_du;    /* largest |r-index coordinate fast - exact| seen (table cells) */
   double hp_sum[P2M_MAXMAPS]; /* sum over the HEALPix map of each map (total Y, kSZ) */
   double fs_sum[P2M_MAXMAPS];
 } p2m_stats;
@@ -129,6 +134,11 @@ p2m_status p2m_get_healpix(p2m_ctx *ctx, int32_t map, float *out);
 p2m_status p2m_get_flatsky(p2m_ctx *ctx, int32_t map, float *out);
 /* ... or device memory, ordered on `stream` (NULL = the context's stream). */
 p2m_status p2m_get_healpix_device(p2m_ctx *ctx, int32_t map, float *d_out, void *stream);
+/* Make a caller-owned device buffer of 12*nside^2 floats the storage of HEALPix map `map`
+   (the reference's hpmap allocation, pks2map.f90:113): read-outs then write it in place
+   and p2m_get_healpix_device with the same pointer copies nothing.  Call right after
+   p2m_create or p2m_reset_maps; NULL restores the context's own buffer. */
+p2m_status p2m_bind_healpix_device(p2m_ctx *ctx, int32_t map, float *d_out);
 
 /* Counters and map sums of everything painted since the last reset. */
 p2m_status p2m_get_stats(p2m_ctx *ctx, p2m_stats *out);

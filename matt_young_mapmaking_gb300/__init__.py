@@ -5,14 +5,15 @@ onto HEALPix (RING) and flat-sky maps by hand-written sm_103a CUDA kernels behin
 ABI of include/p2m.h.  This package holds the Python binding of that ABI, the file
 formats and the build step.
 """
-from .capi import (FLAG_ALL_HALOS, FLAG_RECORD_SETS, FLAG_TIMING, MAXMAPS, PHASES, PREC_FP64,
-                   PREC_MIXED,
+from .capi import (FLAG_ALL_HALOS, FLAG_RECORD_SETS, FLAG_TIMING, FLAG_VALIDATE, MAXMAPS, PHASES,
+                   PREC_FP64, PREC_MIXED,
                    P2MConfig, P2MError, Painter, exported_symbols, generate_catalogue,
                    load_library, make_maptable)
 from .formats import (detect_layout, read_pksc, read_table, table_array, table_header,
                       write_pksc, write_table)
 
-__all__ = ["FLAG_ALL_HALOS", "FLAG_RECORD_SETS", "FLAG_TIMING", "PHASES", "MAXMAPS", "PREC_FP64", "PREC_MIXED",
+__all__ = ["FLAG_ALL_HALOS", "FLAG_RECORD_SETS", "FLAG_TIMING", "FLAG_VALIDATE", "PHASES",
+           "MAXMAPS", "PREC_FP64", "PREC_MIXED",
            "P2MConfig", "P2MError", "Painter", "exported_symbols", "generate_catalogue",
            "load_library", "make_maptable", "detect_layout", "read_pksc", "read_table",
            "table_array", "table_header", "write_pksc", "write_table"]

@@ -17,7 +17,7 @@ LIB_PATH = os.path.join(_HERE, "libp2m_gb300.so")
 
 MAXMAPS = 8
 PREC_FP64, PREC_MIXED = 0, 1
-FLAG_RECORD_SETS, FLAG_ALL_HALOS, FLAG_TIMING = 1, 2, 4
+FLAG_RECORD_SETS, FLAG_ALL_HALOS, FLAG_TIMING, FLAG_VALIDATE = 1, 2, 4, 8
 STATUS = {0: "OK", 1: "BADARG", 2: "CUDA", 3: "CAPACITY", 4: "TIMEOUT", 5: "IO", 6: "STATE",
           7: "NOMEM"}
 
@@ -57,6 +57,10 @@ class P2MStats(ctypes.Structure):
         ("hp_updates", ctypes.c_int64),
         ("fs_updates", ctypes.c_int64),
         ("n_recheck", ctypes.c_int64),
+        ("val_checked", ctypes.c_int64),
+        ("val_bad_set", ctypes.c_int64),
+        ("val_bad_index", ctypes.c_int64),
+        ("val_max_du", ctypes.c_float),
         ("hp_sum", ctypes.c_double * MAXMAPS),
         ("fs_sum", ctypes.c_double * MAXMAPS),
     ]
@@ -91,6 +95,7 @@ def load_library():
         "p2m_get_healpix": (I32, [VP, I32, VP]),
         "p2m_get_flatsky": (I32, [VP, I32, VP]),
         "p2m_get_healpix_device": (I32, [VP, I32, VP, VP]),
+        "p2m_bind_healpix_device": (I32, [VP, I32, VP]),
         "p2m_get_stats": (I32, [VP, ctypes.POINTER(P2MStats)]),
         "p2m_synchronize": (I32, [VP]),
         "p2m_get_pixel_sets": (I32, [VP, VP, VP, I64, ctypes.POINTER(ctypes.c_int64)]),
@@ -113,14 +118,14 @@ def exported_symbols():
     """Names the C ABI exports (include/p2m.h and include/p2m_tools.h)."""
     return ["p2m_create", "p2m_destroy", "p2m_last_error", "p2m_load_table", "p2m_reset_maps",
             "p2m_paint_records", "p2m_paint_records_device", "p2m_project_halo", "p2m_flush",
-            "p2m_get_healpix", "p2m_get_flatsky", "p2m_get_healpix_device", "p2m_get_stats",
+            "p2m_get_healpix", "p2m_get_flatsky", "p2m_get_healpix_device",
+            "p2m_bind_healpix_device", "p2m_get_stats",
             "p2m_synchronize", "p2m_get_pixel_sets", "p2m_make_maptable",
             "p2m_generate_catalogue", "p2m_philox4x32", "p2m_fmath_eval_device",
             "p2m_get_timings"]
 
 
-PHASES = ["cut", "setup", "ring_scan", "emit", "rings", "count_scan", "paint", "recheck",
-          "flatsky", "readout"]
+PHASES = ["cut", "setup", "item_scan", "items", "flatsky", "group", "paint", "readout"]
 
 
 def _ptr(a):
@@ -230,6 +235,10 @@ class Painter:
     def healpix_into(self, m, host_ptr):
         """Read map m into host memory at host_ptr (12*nside^2 floats, e.g. pinned)."""
         self._check(self._lib.p2m_get_healpix(self._h, m, ctypes.c_void_p(host_ptr)))
+
+    def bind_healpix_device(self, m, dptr):
+        """Make device buffer dptr (12*nside^2 floats) the storage of map m."""
+        self._check(self._lib.p2m_bind_healpix_device(self._h, m, ctypes.c_void_p(dptr)))
 
     def healpix_device(self, m, dptr, stream=None):
         self._check(self._lib.p2m_get_healpix_device(self._h, m, ctypes.c_void_p(dptr),

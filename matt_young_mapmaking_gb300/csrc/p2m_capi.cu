@@ -1,13 +1,15 @@
 /*
  * p2m_capi.cu -- the C ABI of include/p2m.h: context, device buffers, and the order of
- * kernel launches for one paint call.  The only host round trips of a paint call are
- * two counter reads used to size the item and recheck buffers before they are filled.
+ * kernel launches.  A paint call ingests records (one host round trip, to size the item
+ * buffer); the HEALPix maps are produced by one sweep over everything ingested since the
+ * last read, started by the first read of a map.
  */
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <cmath>
-#include <cstdio>
+#include <cstddef>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 #include <string>
@@ -17,8 +19,10 @@
 #include "../../include/p2m_tools.h"
 #include "p2m_internal.h"
 
-enum { PH_CUT, PH_SETUP, PH_RINGSCAN, PH_EMIT, PH_RINGS, PH_COUNTSCAN, PH_PAINT, PH_RECHECK,
-       PH_FS, PH_FINAL, P2M_NPHASE };
+enum { PH_CUT, PH_SETUP, PH_SCAN, PH_ITEMS, PH_FS, PH_GROUP, PH_PAINT, PH_READOUT, P2M_NPHASE };
+
+/* L2 budget of one window (two windows alternate) */
+#define P2M_WINDOW_BYTES (40LL << 20)
 
 struct p2m_ctx {
   p2m_config cfg;
@@ -26,46 +30,66 @@ struct p2m_ctx {
   cudaStream_t stream = nullptr;
   std::string err;
   p2m_cosmo cosmo;
+  std::vector<float> rofz_host, zofr_host;
   float *d_rofz = nullptr, *d_zofr = nullptr;
   double2 *d_ringtab = nullptr;
   p2m_tabhdr th;
   bool th_set = false;
   float *d_tab[P2M_MAXTABLES] = {};
-  void *d_hp_acc = nullptr, *d_fs_acc = nullptr;
+  float band_u = 2e-4f;
+  /* ring bands and windows */
+  int nbands = 0;
+  long long wpix = 0;
+  int *d_band_of_ring = nullptr;
+  long long *d_band_pix0 = nullptr;
+  float2 *d_win = nullptr;
+  /* outputs */
   long long hp_npix = 0, fs_npix = 0;
-  float *d_out = nullptr;
-  long long out_cap = 0;
-  /* work buffers */
-  float *d_records = nullptr;
-  long long cap_records = 0;
-  int *d_surv = nullptr;
+  float *d_out_own[P2M_MAXMAPS] = {};
+  float *d_out[P2M_MAXMAPS] = {};
+  double *d_acc64 = nullptr; /* plain FP64 path */
+  void *d_fs_acc = nullptr;
+  float *d_fs_out = nullptr;
+  /* ingest state (accumulated until the next sweep) */
   HaloRec *d_halos = nullptr;
-  long long cap_halos = 0;
-  unsigned int *d_ring_hist = nullptr, *d_ring_cursor = nullptr;
-  long long *d_ring_start = nullptr;
-  RingItem *d_items = nullptr;
-  unsigned int *d_counts = nullptr;
-  long long *d_pix_off = nullptr;
-  long long cap_items = 0;
-  unsigned long long *d_fb = nullptr;
-  long long cap_fb = 0;
+  long long cap_halos = 0, n_halos = 0;
+  RingItem *d_items_raw = nullptr;
+  long long cap_items_raw = 0, n_items = 0;
+  unsigned int *d_band_hist = nullptr;
+  long long rec_count = 0;
+  bool dirty = false, swept = false;
+  /* per-call buffers */
+  float *d_records = nullptr;
+  long long cap_rec_floats = 0;
+  int *d_surv = nullptr;
+  long long cap_surv = 0;
+  unsigned int *d_nring = nullptr;
+  long long cap_nring = 0;
+  long long *d_ioff = nullptr;
+  long long cap_ioff = 0;
   FsItem *d_fs_items = nullptr;
   long long cap_fs = 0;
+  long long *d_scan_tmp = nullptr;
+  /* sweep buffers */
+  RingItem *d_items = nullptr;
+  long long cap_items = 0;
+  unsigned int *d_counts = nullptr;
+  long long cap_counts = 0;
+  long long *d_pix_off = nullptr;
+  long long cap_pix_off = 0;
+  long long *d_band_item0 = nullptr, *d_band_cand0 = nullptr;
+  unsigned int *d_band_cursor = nullptr, *d_paint_done = nullptr, *d_drain_done = nullptr;
+  int *d_seg_start = nullptr, *d_seg_code = nullptr, *d_unit_target = nullptr;
+  unsigned long long *d_nitems = nullptr;
+  double *d_sums = nullptr; /* [0, MAXMAPS): HEALPix, [MAXMAPS, 2 MAXMAPS): flat sky */
   long long *d_set_rec = nullptr, *d_set_pix = nullptr;
   long long cap_set = 0;
-  long long *d_scan_tmp = nullptr;
   DevCounters *d_ctr = nullptr, *h_ctr = nullptr;
-  double *d_sums = nullptr;
   float *d_prep = nullptr;
   long long cap_prep = 0;
   std::vector<float> prep;
-  std::vector<float> rofz_host, zofr_host;
-  long long cap_rec_floats = 0;
-  p2m_stats stats;
-  long long last_sets = 0;
-  /* ordering between the context stream and a caller's stream */
+  long long n_records = 0;
   cudaEvent_t ev_join = nullptr, ev_back = nullptr;
-  /* per-phase device timing of the last paint call (P2M_FLAG_TIMING) */
   cudaEvent_t tev[P2M_NPHASE][2] = {};
   bool tev_used[P2M_NPHASE] = {};
 };
@@ -84,21 +108,36 @@ p2m_status fail(p2m_ctx *c, p2m_status s, const std::string &msg) {
       return fail(ctx, P2M_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
   } while (0)
 
+#define ST(call)                    \
+  do {                              \
+    p2m_status st_ = (call);        \
+    if (st_ != P2M_OK) return st_;  \
+  } while (0)
+
+/* grows a device buffer to at least `need` elements; keeps the first `keep` elements */
 template <typename T>
-cudaError_t grow(T **p, long long *cap, long long need, long long floor_n = 1024) {
+cudaError_t grow(T **p, long long *cap, long long need, long long keep = 0, cudaStream_t s = 0) {
   if (need <= *cap && *p) return cudaSuccess;
-  long long n = std::max(need + need / 4, floor_n);
+  long long n = std::max(need + need / 4, (long long)1024);
+  T *q = nullptr;
+  cudaError_t e = cudaMalloc((void **)&q, sizeof(T) * (size_t)n);
+  if (e != cudaSuccess) return e;
+  if (*p && keep > 0) {
+    e = cudaMemcpyAsync(q, *p, sizeof(T) * (size_t)keep, cudaMemcpyDeviceToDevice, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+      cudaFree(q);
+      return e;
+    }
+  }
   if (*p) cudaFree(*p);
-  *p = nullptr;
-  *cap = 0;
-  cudaError_t e = cudaMalloc((void **)p, sizeof(T) * (size_t)n);
-  if (e == cudaSuccess) *cap = n;
-  return e;
+  *p = q;
+  *cap = n;
+  return cudaSuccess;
 }
 
 bool is_pow2(int n) { return n > 0 && (n & (n - 1)) == 0; }
 
-/* phase timing marks (no-ops unless P2M_FLAG_TIMING) */
 void tmark(p2m_ctx *ctx, int ph, int end, cudaStream_t s) {
   if (!(ctx->cfg.flags & P2M_FLAG_TIMING)) return;
   if (!ctx->tev[ph][end]) cudaEventCreate(&ctx->tev[ph][end]);
@@ -108,8 +147,8 @@ void tmark(p2m_ctx *ctx, int ph, int end, cudaStream_t s) {
 #define TB(ph) tmark(ctx, ph, 0, s)
 #define TE(ph) tmark(ctx, ph, 1, s)
 
-/* work queued on the context stream before this call runs first on s; work queued on
-   the context stream after this call waits for s */
+/* work queued on the context stream before a call on stream s runs first; work queued
+   on the context stream after it waits for s */
 void join_in(p2m_ctx *ctx, cudaStream_t s) {
   if (s == ctx->stream) return;
   cudaEventRecord(ctx->ev_join, ctx->stream);
@@ -120,6 +159,9 @@ void join_out(p2m_ctx *ctx, cudaStream_t s) {
   cudaEventRecord(ctx->ev_back, s);
   cudaStreamWaitEvent(ctx->stream, ctx->ev_back, 0);
 }
+
+/* per-call counters precede the cumulative ones in DevCounters */
+const size_t CALL_CTR_BYTES = offsetof(DevCounters, hp_updates);
 
 PaintParams make_params(const p2m_ctx *ctx, int nfloat) {
   PaintParams P;
@@ -155,6 +197,8 @@ PaintParams make_params(const p2m_ctx *ctx, int nfloat) {
   P.rofz = ctx->d_rofz;
   P.zofr = ctx->d_zofr;
   P.ringtab = ctx->d_ringtab;
+  P.band_of_ring = ctx->d_band_of_ring;
+  P.band_u = ctx->band_u;
   if (ctx->th_set) {
     float fr;
     int ir;
@@ -165,29 +209,26 @@ PaintParams make_params(const p2m_ctx *ctx, int nfloat) {
   return P;
 }
 
-PaintBuffers make_buffers(const p2m_ctx *ctx, const float *records) {
-  PaintBuffers B;
+IngestBuffers ingest_buffers(const p2m_ctx *ctx, const float *records) {
+  IngestBuffers B;
   memset(&B, 0, sizeof(B));
   B.records = records;
+  B.rec_base = ctx->rec_count;
   B.surv = ctx->d_surv;
-  B.halos = ctx->d_halos;
-  B.ring_hist = ctx->d_ring_hist;
-  B.ring_cursor = ctx->d_ring_cursor;
-  B.ring_start = ctx->d_ring_start;
-  B.items = ctx->d_items;
-  B.counts = ctx->d_counts;
-  B.pix_off = ctx->d_pix_off;
-  B.fb = ctx->d_fb;
-  B.fb_cap = ctx->cap_fb;
+  B.halos = ctx->d_halos + ctx->n_halos;
+  B.halo_base = ctx->n_halos;
+  B.nring = ctx->d_nring;
+  B.ioff = ctx->d_ioff;
+  B.items = ctx->d_items_raw + ctx->n_items;
+  B.band_hist = ctx->d_band_hist;
   B.fs_items = ctx->d_fs_items;
   B.fs_cap = ctx->cap_fs;
-  B.hp_acc = ctx->d_hp_acc;
   B.fs_acc = ctx->d_fs_acc;
+  B.scan_tmp = ctx->d_scan_tmp;
+  B.ctr = ctx->d_ctr;
   B.set_rec = ctx->d_set_rec;
   B.set_pix = ctx->d_set_pix;
   B.set_cap = ctx->cap_set;
-  B.scan_tmp = ctx->d_scan_tmp;
-  B.ctr = ctx->d_ctr;
   return B;
 }
 
@@ -199,141 +240,265 @@ p2m_status check_tables(p2m_ctx *ctx) {
   return P2M_OK;
 }
 
-/* everything after the per-halo set-up: ring items, spans, paint, recheck, flat sky */
-p2m_status paint_halos(p2m_ctx *ctx, PaintParams &P, cudaStream_t s) {
-  PaintBuffers B = make_buffers(ctx, nullptr);
-  TB(PH_RINGSCAN);
-  if (P.nside > 0) p2m_launch_ring_scan(P, B, s);
-  TE(PH_RINGSCAN);
-  CK(cudaMemcpyAsync(ctx->h_ctr, ctx->d_ctr, sizeof(DevCounters), cudaMemcpyDeviceToHost, s));
-  CK(cudaStreamSynchronize(s));
-  long long n_halo = (long long)ctx->h_ctr->n_halo;
-  long long n_items = P.nside > 0 ? (long long)ctx->h_ctr->n_items : 0;
-  long long n_fs = (long long)ctx->h_ctr->n_fs_rows;
-  if (ctx->h_ctr->err & P2M_DEVERR_RADIUS)
-    return fail(ctx, P2M_ERR_BADARG, "a halo's disc radius exceeds pi (query_disc aborts)");
-  {
-    long long c1 = ctx->cap_items, c2 = ctx->cap_items;
-    CK(grow(&ctx->d_items, &ctx->cap_items, std::max(n_items, 1LL)));
-    CK(grow(&ctx->d_counts, &c1, ctx->cap_items, ctx->cap_items));
-    CK(grow(&ctx->d_pix_off, &c2, ctx->cap_items, ctx->cap_items));
-  }
-  CK(grow(&ctx->d_fs_items, &ctx->cap_fs, std::max(n_fs, 1LL)));
-  B = make_buffers(ctx, nullptr);
-  if (n_halo > 0) {
-    TB(PH_EMIT);
-    p2m_launch_emit(P, B, n_halo, s, ctx->nsm);
-    TE(PH_EMIT);
-    if (P.nside > 0 && n_items > 0) {
-      TB(PH_RINGS);
-      p2m_launch_rings(P, B, n_items, s, ctx->nsm);
-      TE(PH_RINGS);
-      TB(PH_COUNTSCAN);
-      p2m_launch_count_scan(P, B, s);
-      TE(PH_COUNTSCAN);
-      CK(cudaMemcpyAsync(ctx->h_ctr, ctx->d_ctr, sizeof(DevCounters), cudaMemcpyDeviceToHost, s));
-      CK(cudaStreamSynchronize(s));
-      long long n_pix = (long long)ctx->h_ctr->n_pix;
-      if (P.precision == P2M_PREC_MIXED) {
-        CK(grow(&ctx->d_fb, &ctx->cap_fb, n_pix / 4 + (1LL << 20)));
-        B = make_buffers(ctx, nullptr);
-      }
-      TB(PH_PAINT);
-      p2m_launch_paint(P, B, s, ctx->nsm);
-      TE(PH_PAINT);
-      if (P.precision == P2M_PREC_MIXED) {
-        TB(PH_RECHECK);
-        p2m_launch_recheck(P, B, s, ctx->nsm);
-        TE(PH_RECHECK);
-      }
-    }
-    if (P.npix_fs > 0 && n_fs > 0) {
-      TB(PH_FS);
-      p2m_launch_paint_fs(P, B, s, ctx->nsm);
-      TE(PH_FS);
-    }
-  }
-  CK(cudaGetLastError());
+p2m_status read_counters(p2m_ctx *ctx, cudaStream_t s) {
   CK(cudaMemcpyAsync(ctx->h_ctr, ctx->d_ctr, sizeof(DevCounters), cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
   const DevCounters &h = *ctx->h_ctr;
-  if (h.err & P2M_DEVERR_FB_OVERFLOW)
-    return fail(ctx, P2M_ERR_CAPACITY, "recheck buffer overflow (maps are incomplete)");
+  if (h.err & P2M_DEVERR_RADIUS)
+    return fail(ctx, P2M_ERR_BADARG, "a halo's disc radius exceeds pi (query_disc aborts)");
   if (h.err & P2M_DEVERR_ITEMS)
     return fail(ctx, P2M_ERR_STATE, "candidate walk exceeded its round bound (maps are incomplete)");
   if (h.err & P2M_DEVERR_FS_OVERFLOW)
     return fail(ctx, P2M_ERR_CAPACITY, "flat-sky row buffer overflow (maps are incomplete)");
-  ctx->stats.n_shell += (long long)h.n_shell;
-  ctx->stats.n_painted += (long long)h.n_surv;
-  ctx->stats.n_enumerated += (long long)h.n_halo;
-  ctx->stats.hp_candidates += (long long)h.n_pix;
-  ctx->stats.hp_updates += (long long)h.hp_updates;
-  ctx->stats.fs_updates += (long long)h.fs_updates;
-  ctx->stats.n_recheck += (long long)h.n_recheck;
-  ctx->last_sets = (long long)h.n_sets;
+  if (h.err & P2M_DEVERR_TIMEOUT)
+    return fail(ctx, P2M_ERR_TIMEOUT, "a sweep unit waited past its limit (maps are incomplete)");
   return P2M_OK;
 }
 
-p2m_status begin_call(p2m_ctx *ctx, long long n_halos_max, cudaStream_t s) {
-  CK(grow(&ctx->d_surv, &ctx->cap_records, std::max(n_halos_max, 1LL)));
-  long long hcap = ctx->cap_halos;
-  CK(grow(&ctx->d_halos, &hcap, std::max(n_halos_max, 1LL)));
-  ctx->cap_halos = hcap;
-  for (int k = 0; k < P2M_NPHASE; k++) ctx->tev_used[k] = false;
-  CK(cudaMemsetAsync(ctx->d_ctr, 0, sizeof(DevCounters), s));
-  if (ctx->cfg.nside > 0) {
-    size_t nr = sizeof(unsigned int) * (size_t)(4 * ctx->cfg.nside);
-    CK(cudaMemsetAsync(ctx->d_ring_hist, 0, nr, s));
-    CK(cudaMemsetAsync(ctx->d_ring_cursor, 0, nr, s));
+/* Everything after the per-halo set-up of one ingest call: item offsets, items, flat sky.
+   The set-up kernel has been queued on s; n_max bounds the halo count. */
+p2m_status ingest_tail(p2m_ctx *ctx, const PaintParams &P, long long n_max, cudaStream_t s) {
+  IngestBuffers B = ingest_buffers(ctx, nullptr);
+  TB(PH_SCAN);
+  p2m_launch_scan_u32(ctx->d_nring, &ctx->d_ctr->n_surv, ctx->d_ioff, &ctx->d_ctr->n_items,
+                      ctx->d_scan_tmp, s);
+  TE(PH_SCAN);
+  ST(read_counters(ctx, s));
+  long long n_halo = (long long)ctx->h_ctr->n_surv;
+  long long n_items = P.nside > 0 ? (long long)ctx->h_ctr->n_items : 0;
+  long long n_fs = (long long)ctx->h_ctr->n_fs_rows;
+  (void)n_max;
+  CK(grow(&ctx->d_items_raw, &ctx->cap_items_raw, ctx->n_items + std::max(n_items, 1LL),
+          ctx->n_items, s));
+  CK(grow(&ctx->d_fs_items, &ctx->cap_fs, std::max(n_fs, 1LL)));
+  B = ingest_buffers(ctx, nullptr);
+  if (n_halo > 0) {
+    if (P.nside > 0 && n_items > 0) {
+      TB(PH_ITEMS);
+      p2m_launch_items(P, B, n_halo, s, ctx->nsm);
+      TE(PH_ITEMS);
+    }
+    if (P.npix_fs > 0 && n_fs > 0) {
+      TB(PH_FS);
+      p2m_launch_fs(P, B, n_halo, s, ctx->nsm);
+      TE(PH_FS);
+    }
   }
+  CK(cudaGetLastError());
+  ctx->n_halos += n_halo;
+  ctx->n_items += n_items;
+  if (n_halo > 0) ctx->dirty = true;
+  return P2M_OK;
+}
+
+p2m_status begin_call(p2m_ctx *ctx, long long n, cudaStream_t s) {
+  CK(grow(&ctx->d_surv, &ctx->cap_surv, std::max(n, 1LL)));
+  CK(grow(&ctx->d_nring, &ctx->cap_nring, std::max(n, 1LL)));
+  CK(grow(&ctx->d_ioff, &ctx->cap_ioff, std::max(n, 1LL)));
+  CK(grow(&ctx->d_halos, &ctx->cap_halos, ctx->n_halos + std::max(n, 1LL), ctx->n_halos, s));
+  for (int k = 0; k < P2M_NPHASE; k++) ctx->tev_used[k] = false;
+  CK(cudaMemsetAsync(ctx->d_ctr, 0, CALL_CTR_BYTES, s));
   return P2M_OK;
 }
 
 p2m_status flush_prepared(p2m_ctx *ctx) {
   if (ctx->prep.empty()) return P2M_OK;
-  p2m_status st = check_tables(ctx);
-  if (st) return st;
+  ST(check_tables(ctx));
   cudaStream_t s = ctx->stream;
   long long n = (long long)ctx->prep.size() / 9;
   CK(grow(&ctx->d_prep, &ctx->cap_prep, (long long)ctx->prep.size()));
   CK(cudaMemcpyAsync(ctx->d_prep, ctx->prep.data(), sizeof(float) * ctx->prep.size(),
                      cudaMemcpyHostToDevice, s));
-  st = begin_call(ctx, n, s);
-  if (st) return st;
+  ST(begin_call(ctx, n, s));
   PaintParams P = make_params(ctx, 7);
-  PaintBuffers B = make_buffers(ctx, nullptr);
+  IngestBuffers B = ingest_buffers(ctx, nullptr);
+  /* every queued halo is enumerated: n_surv = n */
+  unsigned long long nn = (unsigned long long)n;
+  CK(cudaMemcpyAsync(&ctx->d_ctr->n_surv, &nn, sizeof(nn), cudaMemcpyHostToDevice, s));
   TB(PH_SETUP);
-  p2m_launch_prepared(P, B, ctx->d_prep, n, s, ctx->nsm);
+  p2m_launch_setup_prepared(P, B, ctx->d_prep, n, s, ctx->nsm);
   TE(PH_SETUP);
+  CK(cudaStreamSynchronize(s)); /* nn and prep are host memory */
   ctx->prep.clear();
-  return paint_halos(ctx, P, s);
+  ST(ingest_tail(ctx, P, n, s));
+  ctx->rec_count += n;
+  return P2M_OK;
 }
 
-p2m_status paint_device(p2m_ctx *ctx, const float *d_rec, long long nrec, int nfloat,
-                        cudaStream_t s) {
+p2m_status ingest_device(p2m_ctx *ctx, const float *d_rec, long long nrec, int nfloat,
+                         cudaStream_t s) {
   if (nfloat != 7 && nfloat != 10) return fail(ctx, P2M_ERR_BADARG, "nfloat must be 7 or 10");
   if (nrec < 0) return fail(ctx, P2M_ERR_BADARG, "negative record count");
   if (nrec > (1LL << 31) - 1) return fail(ctx, P2M_ERR_BADARG, "more than 2^31-1 records per call");
-  p2m_status st = check_tables(ctx);
-  if (st) return st;
-  st = flush_prepared(ctx);
-  if (st) return st;
+  ST(check_tables(ctx));
+  ST(flush_prepared(ctx));
   if (nrec == 0) return P2M_OK;
   join_in(ctx, s);
-  st = begin_call(ctx, nrec, s);
-  if (st) return st;
+  ST(begin_call(ctx, nrec, s));
   PaintParams P = make_params(ctx, nfloat);
-  PaintBuffers B = make_buffers(ctx, d_rec);
+  IngestBuffers B = ingest_buffers(ctx, d_rec);
   TB(PH_CUT);
   p2m_launch_cut(P, B, nrec, s, ctx->nsm);
   TE(PH_CUT);
   TB(PH_SETUP);
   p2m_launch_setup(P, B, nrec, s, ctx->nsm);
   TE(PH_SETUP);
-  st = paint_halos(ctx, P, s);
+  p2m_status st = ingest_tail(ctx, P, nrec, s);
   join_out(ctx, s);
   if (st) return st;
-  ctx->stats.n_records += nrec;
+  ctx->rec_count += nrec;
+  ctx->n_records += nrec;
+  return P2M_OK;
+}
+
+SweepBuffers sweep_buffers(const p2m_ctx *ctx) {
+  SweepBuffers W;
+  memset(&W, 0, sizeof(W));
+  W.halos = ctx->d_halos;
+  W.items = ctx->d_items;
+  W.pix_off = ctx->d_pix_off;
+  W.n_items = ctx->n_items;
+  W.nbands = ctx->nbands;
+  W.band_item0 = ctx->d_band_item0;
+  W.band_cand0 = ctx->d_band_cand0;
+  W.band_pix0 = ctx->d_band_pix0;
+  W.seg_start = ctx->d_seg_start;
+  W.seg_code = ctx->d_seg_code;
+  W.unit_target = ctx->d_unit_target;
+  W.paint_done = ctx->d_paint_done;
+  W.drain_done = ctx->d_drain_done;
+  W.win = ctx->d_win;
+  W.wpix = ctx->wpix;
+  for (int m = 0; m < P2M_MAXMAPS; m++) W.out[m] = ctx->d_out[m];
+  W.accumulate = ctx->swept ? 1 : 0;
+  W.acc = ctx->d_acc64;
+  W.sums = ctx->d_sums;
+  W.ctr = ctx->d_ctr;
+  W.set_rec = ctx->d_set_rec;
+  W.set_pix = ctx->d_set_pix;
+  W.set_cap = ctx->cap_set;
+  return W;
+}
+
+/* produces the HEALPix output maps from everything ingested since the last sweep */
+p2m_status sweep(p2m_ctx *ctx, cudaStream_t s) {
+  ST(flush_prepared(ctx));
+  if (ctx->cfg.nside <= 0) {
+    ctx->dirty = false;
+    return P2M_OK;
+  }
+  if (!ctx->dirty) {
+    if (!ctx->swept) {
+      for (int m = 0; m < ctx->cfg.nmaps; m++)
+        CK(cudaMemsetAsync(ctx->d_out[m], 0, sizeof(float) * (size_t)ctx->hp_npix, s));
+      ctx->swept = true;
+    }
+    return P2M_OK;
+  }
+  join_in(ctx, s);
+  const long long n = ctx->n_items;
+  const int nb = ctx->nbands;
+  CK(grow(&ctx->d_items, &ctx->cap_items, std::max(n, 1LL)));
+  CK(grow(&ctx->d_counts, &ctx->cap_counts, std::max(n, 1LL)));
+  CK(grow(&ctx->d_pix_off, &ctx->cap_pix_off, std::max(n, 1LL)));
+  CK(cudaMemsetAsync(ctx->d_ctr, 0, CALL_CTR_BYTES, s));
+  unsigned long long nn = (unsigned long long)n;
+  CK(cudaMemcpyAsync(ctx->d_nitems, &nn, sizeof(nn), cudaMemcpyHostToDevice, s));
+  PaintParams P = make_params(ctx, 7);
+  TB(PH_GROUP);
+  p2m_launch_scan_single(ctx->d_band_hist, ctx->d_band_item0, nb, nullptr, s);
+  CK(cudaMemcpyAsync(ctx->d_band_item0 + nb, &n, sizeof(long long), cudaMemcpyHostToDevice, s));
+  CK(cudaMemsetAsync(ctx->d_band_cursor, 0, sizeof(unsigned) * (size_t)nb, s));
+  CK(cudaMemsetAsync(ctx->d_paint_done, 0, sizeof(unsigned) * (size_t)nb, s));
+  CK(cudaMemsetAsync(ctx->d_drain_done, 0, sizeof(unsigned) * (size_t)nb, s));
+  p2m_launch_band_scatter(P, ctx->d_items_raw, n, ctx->d_band_item0, ctx->d_band_cursor,
+                          ctx->d_items, ctx->d_counts, s, ctx->nsm);
+  p2m_launch_scan_u32(ctx->d_counts, ctx->d_nitems, ctx->d_pix_off, &ctx->d_ctr->n_pix,
+                      ctx->d_scan_tmp, s);
+  SweepBuffers W = sweep_buffers(ctx);
+  if (!ctx->swept) CK(cudaMemsetAsync(ctx->d_sums, 0, sizeof(double) * P2M_MAXMAPS, s));
+  if (ctx->cfg.precision == P2M_PREC_MIXED)
+    p2m_launch_units(W, ctx->d_band_item0, ctx->d_band_cand0, ctx->d_seg_start, ctx->d_seg_code,
+                     ctx->d_unit_target, ctx->d_band_pix0, &ctx->d_ctr->n_pix, s);
+  TE(PH_GROUP);
+  TB(PH_PAINT);
+  if (ctx->cfg.precision == P2M_PREC_MIXED) {
+    p2m_launch_sweep(P, W, s, ctx->nsm);
+    TE(PH_PAINT);
+  } else {
+    p2m_launch_paint_full(P, W, s, ctx->nsm);
+    TE(PH_PAINT);
+    TB(PH_READOUT);
+    p2m_launch_finalize_full(P, ctx->d_acc64, ctx->hp_npix, ctx->d_out, ctx->swept ? 1 : 0,
+                             ctx->d_sums, s, ctx->nsm);
+    TE(PH_READOUT);
+    CK(cudaMemsetAsync(ctx->d_acc64, 0, sizeof(double) * (size_t)ctx->cfg.nmaps * (size_t)ctx->hp_npix, s));
+  }
+  CK(cudaGetLastError());
+  p2m_status st = read_counters(ctx, s);
+  join_out(ctx, s);
+  if (st == P2M_ERR_TIMEOUT || st == P2M_ERR_STATE) {
+    /* windows may hold partial sums: clear them so the context stays usable */
+    cudaMemsetAsync(ctx->d_win, 0, sizeof(float2) * (size_t)(P2M_NBUF * ctx->wpix * ctx->cfg.nmaps), ctx->stream);
+  }
+  if (st) return st;
+  CK(cudaMemsetAsync(ctx->d_band_hist, 0, sizeof(unsigned) * (size_t)nb, s));
+  ctx->n_items = 0;
+  ctx->n_halos = 0;
+  ctx->dirty = false;
+  ctx->swept = true;
+  return P2M_OK;
+}
+
+/* ring bands whose pixels fit one window */
+p2m_status build_bands(p2m_ctx *ctx) {
+  const int N = ctx->cfg.nside, nr = 4 * N;
+  long long w = P2M_WINDOW_BYTES / (8LL * ctx->cfg.nmaps);
+  w = std::max(w, 4LL * N); /* at least the widest ring */
+  std::vector<int> bor((size_t)nr, 0);
+  std::vector<long long> pix0;
+  long long start = 0, cur = 0;
+  int b = 0;
+  pix0.push_back(0);
+  for (int r = 1; r < nr; r++) {
+    int npr, ks;
+    long long npn;
+    p2m_ring_info(N, r, &npr, &ks, &npn);
+    if (cur + npr > w && cur > 0) {
+      b++;
+      start += cur;
+      pix0.push_back(start);
+      cur = 0;
+    }
+    bor[(size_t)r] = b;
+    cur += npr;
+  }
+  pix0.push_back(start + cur);
+  ctx->nbands = b + 1;
+  if (ctx->nbands > 2047) return fail(ctx, P2M_ERR_BADARG, "too many ring bands");
+  long long wmax = 0;
+  for (int k = 0; k < ctx->nbands; k++) wmax = std::max(wmax, pix0[(size_t)k + 1] - pix0[(size_t)k]);
+  ctx->wpix = wmax;
+  CK(cudaMalloc((void **)&ctx->d_band_of_ring, sizeof(int) * (size_t)nr));
+  CK(cudaMemcpy(ctx->d_band_of_ring, bor.data(), sizeof(int) * (size_t)nr, cudaMemcpyHostToDevice));
+  CK(cudaMalloc((void **)&ctx->d_band_pix0, sizeof(long long) * pix0.size()));
+  CK(cudaMemcpy(ctx->d_band_pix0, pix0.data(), sizeof(long long) * pix0.size(), cudaMemcpyHostToDevice));
+  size_t nb = (size_t)ctx->nbands;
+  CK(cudaMalloc((void **)&ctx->d_band_hist, sizeof(unsigned) * nb));
+  CK(cudaMemset(ctx->d_band_hist, 0, sizeof(unsigned) * nb));
+  CK(cudaMalloc((void **)&ctx->d_band_cursor, sizeof(unsigned) * nb));
+  CK(cudaMalloc((void **)&ctx->d_paint_done, sizeof(unsigned) * nb));
+  CK(cudaMalloc((void **)&ctx->d_drain_done, sizeof(unsigned) * nb));
+  CK(cudaMalloc((void **)&ctx->d_band_item0, sizeof(long long) * (nb + 1)));
+  CK(cudaMalloc((void **)&ctx->d_band_cand0, sizeof(long long) * (nb + 1)));
+  CK(cudaMalloc((void **)&ctx->d_seg_start, sizeof(int) * (2 * nb + 1)));
+  CK(cudaMalloc((void **)&ctx->d_seg_code, sizeof(int) * 2 * nb));
+  CK(cudaMalloc((void **)&ctx->d_unit_target, sizeof(int) * 2 * nb));
+  if (ctx->cfg.precision == P2M_PREC_MIXED) {
+    size_t wb = sizeof(float2) * (size_t)(P2M_NBUF * ctx->wpix * ctx->cfg.nmaps);
+    CK(cudaMalloc((void **)&ctx->d_win, wb));
+    CK(cudaMemset(ctx->d_win, 0, wb));
+  }
   return P2M_OK;
 }
 
@@ -342,7 +507,6 @@ p2m_status paint_device(p2m_ctx *ctx, const float *d_rec, long long nrec, int nf
 extern "C" {
 
 p2m_status p2m_create(const p2m_config *cfg, p2m_ctx **out) {
-  p2m_ctx *ctx = nullptr;
   if (!cfg || !out) return P2M_ERR_BADARG;
   *out = nullptr;
   if (cfg->nside != 0 && (!is_pow2(cfg->nside) || cfg->nside > 8192)) return P2M_ERR_BADARG;
@@ -355,11 +519,11 @@ p2m_status p2m_create(const p2m_config *cfg, p2m_ctx **out) {
     if (cfg->map_table[m] < 0 || cfg->map_table[m] >= P2M_MAXTABLES) return P2M_ERR_BADARG;
     if (cfg->map_profile[m] != 1 && cfg->map_profile[m] != 2) return P2M_ERR_BADARG;
   }
-  ctx = new (std::nothrow) p2m_ctx();
+  p2m_ctx *ctx = new (std::nothrow) p2m_ctx();
   if (!ctx) return P2M_ERR_NOMEM;
   ctx->cfg = *cfg;
-  memset(&ctx->stats, 0, sizeof(ctx->stats));
   *out = ctx;
+  if (const char *e = getenv("P2M_BAND_U")) ctx->band_u = (float)atof(e);
   CK(cudaSetDevice(cfg->device));
   CK(cudaDeviceGetAttribute(&ctx->nsm, cudaDevAttrMultiProcessorCount, cfg->device));
   CK(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
@@ -378,25 +542,34 @@ p2m_status p2m_create(const p2m_config *cfg, p2m_ctx **out) {
     std::vector<double2> rt((size_t)nr);
     rt[0] = make_double2(1.0, 0.0);
     for (int r = 1; r < nr; r++) {
-      double z, s;
-      p2m_ring_z_sth(cfg->nside, r, &z, &s);
-      rt[(size_t)r] = make_double2(z, s);
+      double z, sn;
+      p2m_ring_z_sth(cfg->nside, r, &z, &sn);
+      rt[(size_t)r] = make_double2(z, sn);
     }
     CK(cudaMalloc((void **)&ctx->d_ringtab, sizeof(double2) * (size_t)nr));
     CK(cudaMemcpy(ctx->d_ringtab, rt.data(), sizeof(double2) * (size_t)nr, cudaMemcpyHostToDevice));
-    CK(cudaMalloc((void **)&ctx->d_ring_hist, sizeof(unsigned int) * (size_t)nr));
-    CK(cudaMalloc((void **)&ctx->d_ring_cursor, sizeof(unsigned int) * (size_t)nr));
-    CK(cudaMalloc((void **)&ctx->d_ring_start, sizeof(long long) * (size_t)nr));
     ctx->hp_npix = 12LL * cfg->nside * cfg->nside;
-    CK(cudaMalloc(&ctx->d_hp_acc, 8 * (size_t)cfg->nmaps * (size_t)ctx->hp_npix));
+    for (int m = 0; m < cfg->nmaps; m++) {
+      CK(cudaMalloc((void **)&ctx->d_out_own[m], sizeof(float) * (size_t)ctx->hp_npix));
+      ctx->d_out[m] = ctx->d_out_own[m];
+    }
+    if (cfg->precision == P2M_PREC_FP64) {
+      size_t ab = sizeof(double) * (size_t)cfg->nmaps * (size_t)ctx->hp_npix;
+      CK(cudaMalloc((void **)&ctx->d_acc64, ab));
+      CK(cudaMemset(ctx->d_acc64, 0, ab));
+    }
+    p2m_status st = build_bands(ctx);
+    if (st) return st;
   }
   if (cfg->npix_fs > 0) {
     ctx->fs_npix = (long long)cfg->npix_fs * cfg->npix_fs;
     CK(cudaMalloc(&ctx->d_fs_acc, 8 * (size_t)cfg->nmaps * (size_t)ctx->fs_npix));
+    CK(cudaMalloc((void **)&ctx->d_fs_out, sizeof(float) * (size_t)ctx->fs_npix));
   }
   CK(cudaMalloc((void **)&ctx->d_scan_tmp, sizeof(long long) * 1024));
   CK(cudaMalloc((void **)&ctx->d_ctr, sizeof(DevCounters)));
   CK(cudaMallocHost((void **)&ctx->h_ctr, sizeof(DevCounters)));
+  CK(cudaMalloc((void **)&ctx->d_nitems, sizeof(unsigned long long)));
   CK(cudaMalloc((void **)&ctx->d_sums, sizeof(double) * 2 * P2M_MAXMAPS));
   if (cfg->flags & P2M_FLAG_RECORD_SETS) {
     ctx->cap_set = 1LL << 24;
@@ -404,10 +577,11 @@ p2m_status p2m_create(const p2m_config *cfg, p2m_ctx **out) {
     CK(cudaMalloc((void **)&ctx->d_set_pix, sizeof(long long) * (size_t)ctx->cap_set));
   }
   long long nrec = std::max<long long>(cfg->max_records, 1024);
-  CK(grow(&ctx->d_surv, &ctx->cap_records, nrec));
-  CK(grow(&ctx->d_halos, &ctx->cap_halos, nrec));
-  p2m_status st = p2m_reset_maps(ctx);
-  if (st) return st;
+  CK(grow(&ctx->d_surv, &ctx->cap_surv, nrec));
+  CK(grow(&ctx->d_nring, &ctx->cap_nring, nrec));
+  CK(grow(&ctx->d_ioff, &ctx->cap_ioff, nrec));
+  CK(grow(&ctx->d_halos, &ctx->cap_halos, nrec / 4 + 1024));
+  ST(p2m_reset_maps(ctx));
   CK(cudaStreamSynchronize(ctx->stream));
   return P2M_OK;
 }
@@ -416,13 +590,18 @@ void p2m_destroy(p2m_ctx *ctx) {
   if (!ctx) return;
   cudaSetDevice(ctx->cfg.device);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
-  void *ptrs[] = {ctx->d_rofz, ctx->d_zofr, ctx->d_ringtab, ctx->d_hp_acc, ctx->d_fs_acc,
-                  ctx->d_out, ctx->d_records, ctx->d_surv, ctx->d_halos, ctx->d_ring_hist,
-                  ctx->d_ring_cursor, ctx->d_ring_start, ctx->d_items, ctx->d_counts,
-                  ctx->d_pix_off, ctx->d_fb, ctx->d_fs_items, ctx->d_set_rec, ctx->d_set_pix,
-                  ctx->d_scan_tmp, ctx->d_ctr, ctx->d_sums, ctx->d_prep};
+  void *ptrs[] = {ctx->d_rofz, ctx->d_zofr, ctx->d_ringtab, ctx->d_band_of_ring, ctx->d_band_pix0,
+                  ctx->d_win, ctx->d_acc64, ctx->d_fs_acc, ctx->d_fs_out, ctx->d_halos,
+                  ctx->d_items_raw, ctx->d_band_hist, ctx->d_records, ctx->d_surv, ctx->d_nring,
+                  ctx->d_ioff, ctx->d_fs_items, ctx->d_scan_tmp, ctx->d_items, ctx->d_counts,
+                  ctx->d_pix_off, ctx->d_band_item0, ctx->d_band_cand0, ctx->d_band_cursor,
+                  ctx->d_paint_done, ctx->d_drain_done, ctx->d_seg_start, ctx->d_seg_code,
+                  ctx->d_unit_target, ctx->d_nitems, ctx->d_sums, ctx->d_set_rec, ctx->d_set_pix,
+                  ctx->d_ctr, ctx->d_prep};
   for (void *p : ptrs)
     if (p) cudaFree(p);
+  for (int m = 0; m < P2M_MAXMAPS; m++)
+    if (ctx->d_out_own[m]) cudaFree(ctx->d_out_own[m]);
   for (int t = 0; t < P2M_MAXTABLES; t++)
     if (ctx->d_tab[t]) cudaFree(ctx->d_tab[t]);
   if (ctx->h_ctr) cudaFreeHost(ctx->h_ctr);
@@ -473,7 +652,10 @@ p2m_status p2m_load_table(p2m_ctx *ctx, int32_t slot, const void *image, int64_t
     for (int k = 0; k < P2M_MAXTABLES; k++) loaded += (ctx->d_tab[k] != nullptr && k != slot);
     if (!same && loaded) return fail(ctx, P2M_ERR_BADARG, "all tables of a context must share one header");
   }
+  if (ctx->dirty || !ctx->prep.empty())
+    return fail(ctx, P2M_ERR_STATE, "tables cannot change while painted halos await a read-out");
   CK(cudaSetDevice(ctx->cfg.device));
+  CK(cudaStreamSynchronize(ctx->stream));
   if (ctx->d_tab[slot]) cudaFree(ctx->d_tab[slot]);
   ctx->d_tab[slot] = nullptr;
   CK(cudaMalloc((void **)&ctx->d_tab[slot], sizeof(float) * (size_t)t.nelem));
@@ -486,12 +668,19 @@ p2m_status p2m_load_table(p2m_ctx *ctx, int32_t slot, const void *image, int64_t
 p2m_status p2m_reset_maps(p2m_ctx *ctx) {
   if (!ctx) return P2M_ERR_BADARG;
   CK(cudaSetDevice(ctx->cfg.device));
+  cudaStream_t s = ctx->stream;
   ctx->prep.clear();
-  if (ctx->d_hp_acc)
-    CK(cudaMemsetAsync(ctx->d_hp_acc, 0, 8 * (size_t)ctx->cfg.nmaps * (size_t)ctx->hp_npix, ctx->stream));
+  ctx->n_halos = 0;
+  ctx->n_items = 0;
+  ctx->rec_count = 0;
+  ctx->n_records = 0;
+  ctx->dirty = false;
+  ctx->swept = false;
+  if (ctx->d_band_hist) CK(cudaMemsetAsync(ctx->d_band_hist, 0, sizeof(unsigned) * (size_t)ctx->nbands, s));
   if (ctx->d_fs_acc)
-    CK(cudaMemsetAsync(ctx->d_fs_acc, 0, 8 * (size_t)ctx->cfg.nmaps * (size_t)ctx->fs_npix, ctx->stream));
-  memset(&ctx->stats, 0, sizeof(ctx->stats));
+    CK(cudaMemsetAsync(ctx->d_fs_acc, 0, 8 * (size_t)ctx->cfg.nmaps * (size_t)ctx->fs_npix, s));
+  CK(cudaMemsetAsync(ctx->d_ctr, 0, sizeof(DevCounters), s));
+  CK(cudaMemsetAsync(ctx->d_sums, 0, sizeof(double) * 2 * P2M_MAXMAPS, s));
   return P2M_OK;
 }
 
@@ -507,8 +696,7 @@ p2m_status p2m_paint_records(p2m_ctx *ctx, const float *records, int64_t nrec, i
     CK(grow(&ctx->d_records, &ctx->cap_rec_floats, need));
     CK(cudaMemcpyAsync(ctx->d_records, records + off * nfloat, sizeof(float) * (size_t)need,
                        cudaMemcpyHostToDevice, ctx->stream));
-    p2m_status st = paint_device(ctx, ctx->d_records, n, nfloat, ctx->stream);
-    if (st) return st;
+    ST(ingest_device(ctx, ctx->d_records, n, nfloat, ctx->stream));
   }
   return P2M_OK;
 }
@@ -519,7 +707,7 @@ p2m_status p2m_paint_records_device(p2m_ctx *ctx, const float *d_records, int64_
   if (nrec > 0 && !d_records) return fail(ctx, P2M_ERR_BADARG, "null records");
   CK(cudaSetDevice(ctx->cfg.device));
   cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
-  return paint_device(ctx, d_records, nrec, nfloat, s);
+  return ingest_device(ctx, d_records, nrec, nfloat, s);
 }
 
 p2m_status p2m_project_halo(p2m_ctx *ctx, float *x, float *y, float *z, const float *r,
@@ -540,79 +728,92 @@ p2m_status p2m_project_halo(p2m_ctx *ctx, float *x, float *y, float *z, const fl
 p2m_status p2m_flush(p2m_ctx *ctx) {
   if (!ctx) return P2M_ERR_BADARG;
   CK(cudaSetDevice(ctx->cfg.device));
-  return flush_prepared(ctx);
+  return sweep(ctx, ctx->stream);
 }
 
-static p2m_status finalize_map(p2m_ctx *ctx, bool hp, int32_t map, float *d_out, cudaStream_t s) {
-  if (map < 0 || map >= ctx->cfg.nmaps) return fail(ctx, P2M_ERR_BADARG, "map index out of range");
-  if (hp && ctx->cfg.nside <= 0) return fail(ctx, P2M_ERR_BADARG, "no HEALPix map configured");
-  if (!hp && ctx->cfg.npix_fs <= 0) return fail(ctx, P2M_ERR_BADARG, "no flat-sky map configured");
-  p2m_status st = flush_prepared(ctx);
-  if (st) return st;
-  PaintParams P = make_params(ctx, 7);
-  double *sum = ctx->d_sums + (hp ? 0 : P2M_MAXMAPS) + map;
-  join_in(ctx, s);
-  CK(cudaMemsetAsync(sum, 0, sizeof(double), s));
-  TB(PH_FINAL);
-  p2m_launch_finalize(P, hp ? ctx->d_hp_acc : ctx->d_fs_acc, hp ? ctx->hp_npix : ctx->fs_npix, map,
-                      d_out, sum, s, ctx->nsm);
-  TE(PH_FINAL);
-  join_out(ctx, s);
-  CK(cudaGetLastError());
+p2m_status p2m_bind_healpix_device(p2m_ctx *ctx, int32_t map, float *d_out) {
+  if (!ctx) return P2M_ERR_BADARG;
+  if (map < 0 || map >= ctx->cfg.nmaps || ctx->cfg.nside <= 0)
+    return fail(ctx, P2M_ERR_BADARG, "map index out of range");
+  if (ctx->dirty || ctx->swept)
+    return fail(ctx, P2M_ERR_STATE, "bind output buffers right after p2m_reset_maps");
+  ctx->d_out[map] = d_out ? d_out : ctx->d_out_own[map];
   return P2M_OK;
 }
 
 p2m_status p2m_get_healpix_device(p2m_ctx *ctx, int32_t map, float *d_out, void *stream) {
   if (!ctx || !d_out) return P2M_ERR_BADARG;
+  if (map < 0 || map >= ctx->cfg.nmaps || ctx->cfg.nside <= 0)
+    return fail(ctx, P2M_ERR_BADARG, "map index out of range");
   CK(cudaSetDevice(ctx->cfg.device));
   cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
-  return finalize_map(ctx, true, map, d_out, s);
-}
-
-static p2m_status get_host(p2m_ctx *ctx, bool hp, int32_t map, float *out) {
-  if (!ctx || !out) return P2M_ERR_BADARG;
-  CK(cudaSetDevice(ctx->cfg.device));
-  long long n = hp ? ctx->hp_npix : ctx->fs_npix;
-  CK(grow(&ctx->d_out, &ctx->out_cap, std::max(n, 1LL)));
-  p2m_status st = finalize_map(ctx, hp, map, ctx->d_out, ctx->stream);
-  if (st) return st;
-  CK(cudaMemcpyAsync(out, ctx->d_out, sizeof(float) * (size_t)n, cudaMemcpyDeviceToHost, ctx->stream));
-  CK(cudaStreamSynchronize(ctx->stream));
-  return P2M_OK;
-}
-
-p2m_status p2m_get_healpix(p2m_ctx *ctx, int32_t map, float *out) { return get_host(ctx, true, map, out); }
-p2m_status p2m_get_flatsky(p2m_ctx *ctx, int32_t map, float *out) { return get_host(ctx, false, map, out); }
-
-p2m_status p2m_get_stats(p2m_ctx *ctx, p2m_stats *out) {
-  if (!ctx || !out) return P2M_ERR_BADARG;
-  CK(cudaSetDevice(ctx->cfg.device));
-  p2m_status st = flush_prepared(ctx);
-  if (st) return st;
-  *out = ctx->stats;
-  double sums[2 * P2M_MAXMAPS];
-  CK(cudaStreamSynchronize(ctx->stream));
-  CK(cudaMemcpy(sums, ctx->d_sums, sizeof(sums), cudaMemcpyDeviceToHost));
-  for (int m = 0; m < P2M_MAXMAPS; m++) {
-    out->hp_sum[m] = sums[m];
-    out->fs_sum[m] = sums[P2M_MAXMAPS + m];
+  ST(sweep(ctx, s));
+  if (d_out != ctx->d_out[map]) {
+    join_in(ctx, s);
+    CK(cudaMemcpyAsync(d_out, ctx->d_out[map], sizeof(float) * (size_t)ctx->hp_npix,
+                       cudaMemcpyDeviceToDevice, s));
+    join_out(ctx, s);
   }
   return P2M_OK;
 }
 
-p2m_status p2m_get_timings(p2m_ctx *ctx, double *ms, int32_t n) {
-  if (!ctx || !ms) return P2M_ERR_BADARG;
-  if (!(ctx->cfg.flags & P2M_FLAG_TIMING))
-    return fail(ctx, P2M_ERR_STATE, "context was created without P2M_FLAG_TIMING");
+p2m_status p2m_get_healpix(p2m_ctx *ctx, int32_t map, float *out) {
+  if (!ctx || !out) return P2M_ERR_BADARG;
+  if (map < 0 || map >= ctx->cfg.nmaps || ctx->cfg.nside <= 0)
+    return fail(ctx, P2M_ERR_BADARG, "map index out of range");
   CK(cudaSetDevice(ctx->cfg.device));
-  for (int k = 0; k < n; k++) {
-    ms[k] = 0.0;
-    if (k < P2M_NPHASE && ctx->tev_used[k]) {
-      float t = 0.0f;
-      CK(cudaEventSynchronize(ctx->tev[k][1]));
-      CK(cudaEventElapsedTime(&t, ctx->tev[k][0], ctx->tev[k][1]));
-      ms[k] = (double)t;
-    }
+  ST(sweep(ctx, ctx->stream));
+  CK(cudaMemcpyAsync(out, ctx->d_out[map], sizeof(float) * (size_t)ctx->hp_npix,
+                     cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return P2M_OK;
+}
+
+p2m_status p2m_get_flatsky(p2m_ctx *ctx, int32_t map, float *out) {
+  if (!ctx || !out) return P2M_ERR_BADARG;
+  if (map < 0 || map >= ctx->cfg.nmaps || ctx->cfg.npix_fs <= 0)
+    return fail(ctx, P2M_ERR_BADARG, "no flat-sky map / map index out of range");
+  CK(cudaSetDevice(ctx->cfg.device));
+  ST(flush_prepared(ctx));
+  cudaStream_t s = ctx->stream;
+  PaintParams P = make_params(ctx, 7);
+  double *sum = ctx->d_sums + P2M_MAXMAPS + map;
+  CK(cudaMemsetAsync(sum, 0, sizeof(double), s));
+  p2m_launch_finalize_fs(P, ctx->d_fs_acc, ctx->fs_npix, ctx->d_fs_out, map, sum, s, ctx->nsm);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(out, ctx->d_fs_out, sizeof(float) * (size_t)ctx->fs_npix,
+                     cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  return P2M_OK;
+}
+
+p2m_status p2m_get_stats(p2m_ctx *ctx, p2m_stats *out) {
+  if (!ctx || !out) return P2M_ERR_BADARG;
+  CK(cudaSetDevice(ctx->cfg.device));
+  ST(sweep(ctx, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  DevCounters h;
+  CK(cudaMemcpy(&h, ctx->d_ctr, sizeof(h), cudaMemcpyDeviceToHost));
+  double sums[2 * P2M_MAXMAPS];
+  CK(cudaMemcpy(sums, ctx->d_sums, sizeof(sums), cudaMemcpyDeviceToHost));
+  memset(out, 0, sizeof(*out));
+  out->n_records = ctx->n_records;
+  out->n_shell = (long long)h.n_shell;
+  out->n_painted = (long long)h.n_massive;
+  out->n_enumerated = (long long)h.n_enum;
+  out->hp_candidates = (long long)h.n_cand;
+  out->hp_updates = (long long)h.hp_updates;
+  out->fs_updates = (long long)h.fs_updates;
+  out->n_recheck = (long long)h.n_recheck;
+  out->val_checked = (long long)h.val_checked;
+  out->val_bad_set = (long long)h.val_bad_set;
+  out->val_bad_index = (long long)h.val_bad_index;
+  float du;
+  memcpy(&du, &h.val_max_du, 4);
+  out->val_max_du = du;
+  for (int m = 0; m < P2M_MAXMAPS; m++) {
+    out->hp_sum[m] = sums[m];
+    out->fs_sum[m] = sums[P2M_MAXMAPS + m];
   }
   return P2M_OK;
 }
@@ -629,10 +830,14 @@ p2m_status p2m_get_pixel_sets(p2m_ctx *ctx, int64_t *rec, int64_t *pix, int64_t 
   if (!(ctx->cfg.flags & P2M_FLAG_RECORD_SETS))
     return fail(ctx, P2M_ERR_STATE, "context was created without P2M_FLAG_RECORD_SETS");
   CK(cudaSetDevice(ctx->cfg.device));
-  *n = ctx->last_sets;
-  long long k = std::min<long long>(std::min<long long>(cap, ctx->last_sets), ctx->cap_set);
-  if (ctx->last_sets > ctx->cap_set)
-    return fail(ctx, P2M_ERR_CAPACITY, "pixel-set buffer overflow");
+  ST(sweep(ctx, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  DevCounters h;
+  CK(cudaMemcpy(&h, ctx->d_ctr, sizeof(h), cudaMemcpyDeviceToHost));
+  long long total = (long long)h.n_sets;
+  *n = total;
+  if (total > ctx->cap_set) return fail(ctx, P2M_ERR_CAPACITY, "pixel-set buffer overflow");
+  long long k = std::min<long long>(cap, total);
   if (k > 0 && rec && pix) {
     CK(cudaMemcpy(rec, ctx->d_set_rec, sizeof(long long) * (size_t)k, cudaMemcpyDeviceToHost));
     CK(cudaMemcpy(pix, ctx->d_set_pix, sizeof(long long) * (size_t)k, cudaMemcpyDeviceToHost));
@@ -640,10 +845,27 @@ p2m_status p2m_get_pixel_sets(p2m_ctx *ctx, int64_t *rec, int64_t *pix, int64_t 
   return P2M_OK;
 }
 
+int32_t p2m_get_timings(p2m_ctx *ctx, double *ms, int32_t n) {
+  if (!ctx || !ms) return P2M_ERR_BADARG;
+  if (!(ctx->cfg.flags & P2M_FLAG_TIMING))
+    return fail(ctx, P2M_ERR_STATE, "context was created without P2M_FLAG_TIMING");
+  CK(cudaSetDevice(ctx->cfg.device));
+  for (int k = 0; k < n; k++) {
+    ms[k] = 0.0;
+    if (k < P2M_NPHASE && ctx->tev_used[k]) {
+      float t = 0.0f;
+      CK(cudaEventSynchronize(ctx->tev[k][1]));
+      CK(cudaEventElapsedTime(&t, ctx->tev[k][0], ctx->tev[k][1]));
+      ms[k] = (double)t;
+    }
+  }
+  return P2M_OK;
+}
+
 p2m_status p2m_make_maptable(int32_t device, int32_t model, float nu, float alpha_cmb,
                              int32_t nchit, int32_t nmht, int32_t nrt, void *image,
                              int64_t *nbytes) {
-  p2m_ctx *ctx = nullptr; /* for CK: errors carry no context message */
+  p2m_ctx *ctx = nullptr; /* CK needs a name; errors carry no context message */
   if (!nbytes) return P2M_ERR_BADARG;
   if (nchit <= 0) nchit = 100;
   if (nmht <= 0) nmht = 100;

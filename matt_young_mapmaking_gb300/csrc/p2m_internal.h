@@ -1,21 +1,24 @@
 /*
  * p2m_internal.h -- device data layout and kernel launchers of the halo painter.
  *
- * Pipeline for one batch of catalogue records (all on one stream, no host round trip
- * inside the paint except the two capacity checks in p2m_capi.cu):
- *   k_cut      records -> indices of halos inside the shell with mass >= mmin
- *   k_setup    per halo: the loop quantities of pks2map.f90:284-298, disc radius,
- *              centre, interpolation constants, candidate ring range, flat-sky box;
- *              histogram of (halo, ring) items per ring
- *   scan       ring histogram -> ring offsets
- *   k_emit     (halo, ring) items placed in ring order; flat-sky (halo, row) items
- *   k_rings    per item: candidate pixel span of the ring (FP32 superset of the disc)
- *              and the ring constants of the disc test
- *   scan       candidate counts -> candidate offsets
- *   k_paint    per candidate pixel: disc test, profile value, deposit
- *   k_recheck  (mixed precision) exact FP64 decision for pixels near a boundary
- *   k_paint_fs flat-sky rows
- *   k_finalize accumulators -> float maps and map sums
+ * A paint call ingests catalogue records; the maps are produced by a sweep when they
+ * are read.  Ingest (one stream, one host round trip to size the item buffer):
+ *   k_cut      records -> halos inside the radial cut with mass >= mmin whose table
+ *              value is not identically zero (block-aggregated compaction)
+ *   k_setup    per halo: the loop quantities of pks2map.f90:284-298, disc radius and
+ *              centre, interpolation constants, candidate ring range, flat-sky box
+ *   scan       rings per halo -> item offsets
+ *   k_items    per (halo, ring) item: FP32 superset of the ring's pixel span and the
+ *              ring constants of the disc test; histogram of items per ring band
+ *   k_paint_fs flat-sky rows (exact float sequence of the reference)
+ * Sweep (mixed precision):
+ *   scan + k_band_scatter   items grouped by ring band (a band's pixels fit in L2)
+ *   scan       candidate counts -> candidate offsets; k_units: the unit queue
+ *   k_sweep    persistent: claims units in order; a paint unit deposits one slice of a
+ *              band's candidates into that band's L2-resident window (two-float
+ *              atomics), a drain unit converts one slice of a painted window to the
+ *              float output maps and clears it.  Two windows alternate between bands.
+ * Sweep (plain FP64): k_paint_full into a full-sky FP64 accumulator, k_finalize_full.
  */
 #ifndef P2M_INTERNAL_H
 #define P2M_INTERNAL_H
@@ -25,18 +28,31 @@
 
 #include "p2m_scalar.h"
 
+#define P2M_NBUF 2            /* windows alternating between bands */
+#define P2M_PAINT_UNIT 4096   /* candidates per paint unit (one block) */
+#define P2M_DRAIN_UNIT 32768  /* map pixels per drain unit (one block) */
+#define P2M_SWEEP_THREADS 256
+
 struct DevCounters {
-  unsigned long long n_records, n_shell, n_surv, n_halo, n_items, n_pix;
-  unsigned long long n_fb, n_fs_items, hp_updates, fs_updates, n_sets, n_recheck;
-  unsigned long long n_candidates, n_fs_rows;
-  unsigned int err;
-  unsigned int pad;
+  /* per call (cleared before every ingest call and every sweep) */
+  unsigned long long n_surv, n_items, n_pix, n_fs_items, n_fs_rows;
+  unsigned int err, next_unit, abort, pad0;
+  /* cumulative since the last reset */
+  unsigned long long hp_updates, fs_updates, n_sets, n_recheck, n_shell, n_massive, n_enum,
+      n_cand;
+  unsigned long long val_checked, val_bad_set, val_bad_index;
+  unsigned int val_max_du; /* float bits of the largest |u_fast - u_exact| */
+  unsigned int pad1;
 };
 
-enum { P2M_DEVERR_FB_OVERFLOW = 1, P2M_DEVERR_FS_OVERFLOW = 2, P2M_DEVERR_RADIUS = 4,
-       P2M_DEVERR_ITEMS = 8 };
+enum {
+  P2M_DEVERR_FS_OVERFLOW = 2,
+  P2M_DEVERR_RADIUS = 4,
+  P2M_DEVERR_ITEMS = 8,
+  P2M_DEVERR_TIMEOUT = 16
+};
 
-/* one halo inside the cut, as the painter needs it */
+/* one enumerated halo */
 struct HaloRec {
   double z0, sth0, phi0f; /* unit disc centre: z, sin(theta), phi / 2pi */
   float hv[3];            /* hpvec1 of haloproject.f90:51-53 (float values) */
@@ -45,10 +61,10 @@ struct HaloRec {
   float chi_t, fc, fm;    /* per-halo part of interpolate_table */
   int ichi, imh, zero;
   float w1, w2;           /* deposit weights of profile-1 and profile-2 maps */
-  int rec;                /* record index */
+  long long rec;          /* record index (over all paint calls since the reset) */
   int ir_lo, ir_hi;       /* candidate rings */
   int cbase[4];           /* table offsets of corners (imh,ichi),(imh+1,ichi),(imh,ichi+1),
-                             (imh+1,ichi+1) at ir=1, profile 1; -1: use clamped offsets */
+                             (imh+1,ichi+1) at ir=1, profile 1; -1: clamped offsets */
   float theta_h, phi_h;   /* flat-sky centre (float values), haloproject.f90:105-106 */
   int jmin, jmax, kmin, kmax; /* flat-sky box; jmin > jmax: none */
 };
@@ -75,50 +91,86 @@ struct PaintParams {
   p2m_tabhdr th;
   int ir_c;     /* r-index and fraction for r < rmint (r = rmint + 1e-5) */
   float fr_c;
+  float band_u;  /* half-width of the r-index recheck band (cell units) */
   const float *tables[P2M_MAXTABLES];
   const float *rofz, *zofr;
   const double2 *ringtab; /* (z, sin theta) of rings 1..4N-1 at index ring */
+  const int *band_of_ring;
 };
 
-struct PaintBuffers {
+/* buffers of one ingest call */
+struct IngestBuffers {
   const float *records;
-  int *surv;
-  HaloRec *halos;
-  unsigned int *ring_hist, *ring_cursor;
-  long long *ring_start;
-  RingItem *items;
-  unsigned int *counts;
-  long long *pix_off;
-  unsigned long long *fb; /* (item << 32 | k) */
-  long long fb_cap;
+  long long rec_base;   /* record index of records[0] */
+  int *surv;            /* record indices of enumerated halos (call-local) */
+  HaloRec *halos;       /* halos[0..n_surv) of this call */
+  long long halo_base;  /* global index of halos[0] */
+  unsigned int *nring;  /* rings per halo */
+  long long *ioff;      /* item offset per halo (call-local) */
+  RingItem *items;      /* items of this call */
+  unsigned int *band_hist;
   FsItem *fs_items;
   long long fs_cap;
-  void *hp_acc; /* nmaps per pixel: double, or float2 (hi, lo) */
   void *fs_acc;
+  long long *scan_tmp;
+  DevCounters *ctr;
   long long *set_rec, *set_pix;
   long long set_cap;
-  long long *scan_tmp; /* block sums */
+};
+
+/* buffers of one sweep */
+struct SweepBuffers {
+  const HaloRec *halos;
+  const RingItem *items;   /* grouped by band */
+  const long long *pix_off;
+  long long n_items;
+  int nbands;
+  const long long *band_item0; /* [nbands+1] */
+  const long long *band_cand0; /* [nbands+1] */
+  const long long *band_pix0;  /* [nbands+1] first map pixel of each band */
+  const int *seg_start;        /* [2*nbands+1] unit prefix of the segment sequence */
+  const int *seg_code;         /* [2*nbands] band | (is_drain << 30) */
+  const int *unit_target;      /* [2*nbands] units of P_b at b, of D_b at nbands + b */
+  unsigned int *paint_done, *drain_done; /* [nbands] */
+  float2 *win;                 /* P2M_NBUF windows of wpix * nmaps (hi, lo) */
+  long long wpix;
+  float *out[P2M_MAXMAPS];     /* float output maps */
+  int accumulate;              /* add to the output maps instead of overwriting */
+  void *acc;                   /* plain path: full-sky FP64 accumulator */
+  double *sums;                /* [nmaps] sum over each output map */
   DevCounters *ctr;
+  long long *set_rec, *set_pix;
+  long long set_cap;
 };
 
 /* launchers (p2m_kernels.cu) */
-void p2m_launch_cut(const PaintParams &P, const PaintBuffers &B, long long n, cudaStream_t s,
+void p2m_launch_cut(const PaintParams &P, const IngestBuffers &B, long long n, cudaStream_t s,
                     int nsm);
-void p2m_launch_setup(const PaintParams &P, const PaintBuffers &B, long long n_max,
+void p2m_launch_setup(const PaintParams &P, const IngestBuffers &B, long long n_max,
                       cudaStream_t s, int nsm);
-void p2m_launch_ring_scan(const PaintParams &P, const PaintBuffers &B, cudaStream_t s);
-void p2m_launch_emit(const PaintParams &P, const PaintBuffers &B, long long n_max,
-                     cudaStream_t s, int nsm);
-void p2m_launch_rings(const PaintParams &P, const PaintBuffers &B, long long n_max,
+void p2m_launch_setup_prepared(const PaintParams &P, const IngestBuffers &B, const float *prep,
+                               long long n, cudaStream_t s, int nsm);
+void p2m_launch_scan_u32(const unsigned int *in, const unsigned long long *n_ptr, long long *out,
+                         unsigned long long *total, long long *tmp, cudaStream_t s);
+void p2m_launch_items(const PaintParams &P, const IngestBuffers &B, long long n_max,
                       cudaStream_t s, int nsm);
-void p2m_launch_count_scan(const PaintParams &P, const PaintBuffers &B, cudaStream_t s);
-void p2m_launch_paint(const PaintParams &P, const PaintBuffers &B, cudaStream_t s, int nsm);
-void p2m_launch_recheck(const PaintParams &P, const PaintBuffers &B, cudaStream_t s, int nsm);
-void p2m_launch_paint_fs(const PaintParams &P, const PaintBuffers &B, cudaStream_t s, int nsm);
-void p2m_launch_finalize(const PaintParams &P, const void *acc, long long npix, int map,
-                         float *out, double *sum, cudaStream_t s, int nsm);
-void p2m_launch_prepared(const PaintParams &P, const PaintBuffers &B, const float *d_prep,
-                         long long n, cudaStream_t s, int nsm);
+void p2m_launch_fs(const PaintParams &P, const IngestBuffers &B, long long n_max, cudaStream_t s,
+                   int nsm);
+void p2m_launch_band_scatter(const PaintParams &P, const RingItem *in, long long n,
+                             const long long *band_start, unsigned int *band_cursor,
+                             RingItem *out, unsigned int *counts, cudaStream_t s, int nsm);
+void p2m_launch_scan_single(const unsigned int *in, long long *out, long long n,
+                            unsigned long long *total, cudaStream_t s);
+void p2m_launch_units(const SweepBuffers &W, long long *band_item0, long long *band_cand0,
+                      int *seg_start, int *seg_code, int *unit_target, const long long *band_pix0,
+                      unsigned long long *n_pix, cudaStream_t s);
+void p2m_launch_sweep(const PaintParams &P, const SweepBuffers &W, cudaStream_t s, int nsm);
+void p2m_launch_paint_full(const PaintParams &P, const SweepBuffers &W, cudaStream_t s, int nsm);
+void p2m_launch_finalize_full(const PaintParams &P, const void *acc, long long npix,
+                              float *const *out, int accumulate, double *sums, cudaStream_t s,
+                              int nsm);
+void p2m_launch_finalize_fs(const PaintParams &P, const void *acc, long long npix, float *out,
+                            int map, double *sum, cudaStream_t s, int nsm);
 struct TableConsts {
   float y0, tau0, x0const, nu, alpha;
   int model;

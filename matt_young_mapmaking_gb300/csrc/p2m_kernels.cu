@@ -1,37 +1,39 @@
 /*
- * p2m_kernels.cu -- sm_103a kernels of the halo painter (see p2m_internal.h for the
- * pipeline).  Work is balanced at the level of candidate pixels: per-ring candidate
- * spans are prefix-summed and each warp walks a fixed-size range of the candidate
- * space, locating items with a 32-wide search in registers.  Items are ordered by
- * ring, so concurrently running warps deposit into a narrow band of the RING-ordered
- * map that stays resident in L2.
+ * p2m_kernels.cu -- sm_103a kernels of the halo painter (pipeline in p2m_internal.h).
+ *
+ * Load balance is at the level of candidate pixels: per-ring candidate spans are
+ * prefix-summed and each warp walks a contiguous range of the candidate space, finding
+ * each lane's item with a 32-wide search over offsets held in registers.  Deposits of
+ * the mixed-precision path go to an L2-resident window of one ring band; the HBM
+ * traffic of the maps is then one float write per map pixel.
  */
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "../../include/p2m_tools.h"
 #include "p2m_internal.h"
 
 #define FULL 0xffffffffu
 
 /* ------------------------------------------------------------------ helpers ----- */
 
-/* warp-aggregated append: all 32 lanes must call; returns slot or -1 */
-__device__ __forceinline__ long long warp_append(unsigned long long *ctr, bool pred) {
-  unsigned m = __ballot_sync(FULL, pred);
-  int lane = threadIdx.x & 31;
-  unsigned long long base = 0;
-  if (m) {
-    int leader = __ffs(m) - 1;
-    if (lane == leader) base = atomicAdd(ctr, (unsigned long long)__popc(m));
-    base = __shfl_sync(FULL, base, leader);
-  }
-  if (!pred) return -1;
-  return (long long)(base + __popc(m & ((1u << lane) - 1u)));
-}
-
 __device__ __forceinline__ void warp_count(unsigned long long *ctr, unsigned long long v) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(FULL, v, o);
   if ((threadIdx.x & 31) == 0 && v) atomicAdd(ctr, v);
+}
+
+/* block-wide sum of v added to *ctr by one thread (blockDim.x <= 1024, all threads call) */
+__device__ void block_count(unsigned long long *ctr, unsigned long long v) {
+  __shared__ unsigned long long red[32];
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(FULL, v, o);
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned long long t = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += red[w];
+    if (t) atomicAdd(ctr, t);
+  }
 }
 
 __device__ __forceinline__ bool p2m_isfinite(float x) { return fabsf(x) <= 3.4028234e38f; }
@@ -54,44 +56,82 @@ __device__ __forceinline__ p2m_hinterp halo_hinterp(const HaloRec &H) {
   return hi;
 }
 
-/* --------------------------------------------------------------------- k_cut ----- */
+__device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
 
-/* radial cut (pks2map.f90:144-160) and mass cut (:264, :296) */
-__global__ void __launch_bounds__(256) k_cut(PaintParams P, PaintBuffers B, long long n) {
-  long long stride = (long long)gridDim.x * blockDim.x;
-  int lane = threadIdx.x & 31;
-  unsigned long long nshell = 0;
-  for (long long base = (long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < n;
-       base += stride) {
-    long long i = base + lane;
-    bool shell = false, keep = false;
-    if (i < n) {
+/* ---------------------------------------------------------------- ingest: cut ----- */
+
+#define CUT_PER_THREAD 8
+
+/* radial cut (pks2map.f90:144-160), mass cut (:264, :296), and the table's chi bound
+   (maptable.f90:184,188: chi = rofz(zofr(chi)) > chimaxt paints zeros) */
+__global__ void __launch_bounds__(256) k_cut(PaintParams P, IngestBuffers B, long long n) {
+  __shared__ int wsum[8];
+  __shared__ long long base_s;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  unsigned long long nshell = 0, nmass = 0, nkeep = 0;
+  const long long tile = (long long)blockDim.x * CUT_PER_THREAD;
+  for (long long t0 = (long long)blockIdx.x * tile; t0 < n; t0 += (long long)gridDim.x * tile) {
+    unsigned keepbits = 0;
+#pragma unroll
+    for (int k = 0; k < CUT_PER_THREAD; k++) {
+      long long i = t0 + (long long)k * blockDim.x + threadIdx.x;
+      if (i >= n) continue;
       const float *r = B.records + i * P.nfloat;
       float p0 = __ldg(r + 0), p1 = __ldg(r + 1), p2 = __ldg(r + 2), rth = __ldg(r + 6);
-      if (p2m_isfinite(p0) && p2m_isfinite(p1) && p2m_isfinite(p2) && p2m_isfinite(rth)) {
-        float xh = FSUB(p2, P.chihview), yh = p1, zh = p0;
-        float chih = FSQRT(FADD(FADD(FMUL(xh, xh), FMUL(yh, yh)), FMUL(zh, zh)));
-        shell = !(chih > P.cut_high || chih < P.cut_low);
-        float mass = FMUL(P.mass_fac, FMUL(FMUL(rth, rth), rth));
-        keep = shell && !(mass < 1e13f);
+      if (!(p2m_isfinite(p0) && p2m_isfinite(p1) && p2m_isfinite(p2) && p2m_isfinite(rth))) continue;
+      float xh = FSUB(p2, P.chihview), yh = p1, zh = p0;
+      float chih = FSQRT(FADD(FADD(FMUL(xh, xh), FMUL(yh, yh)), FMUL(zh, zh)));
+      bool shell = !(chih > P.cut_high || chih < P.cut_low);
+      float mass = FMUL(P.mass_fac, FMUL(FMUL(rth, rth), rth));
+      bool massive = shell && !(mass < 1e13f);
+      bool keep = massive;
+      if (massive && !(P.flags & 2)) {
+        float chi0 = FSQRT(FADD(FADD(FMUL(p2, p2), FMUL(p1, p1)), FMUL(p0, p0)));
+        float z = p2m_lookup(P.zofr, P.cosmo.dzofr, chi0);
+        keep = !(p2m_lookup(P.rofz, P.cosmo.drofz, z) > P.th.chimaxt);
       }
+      nshell += shell;
+      nmass += massive;
+      if (keep) keepbits |= 1u << k;
     }
-    nshell += shell;
-    long long slot = warp_append(&B.ctr->n_surv, keep);
-    if (keep) B.surv[slot] = (int)i;
+    int cnt = __popc(keepbits);
+    nkeep += cnt;
+    int x = cnt;
+    for (int o = 1; o < 32; o <<= 1) {
+      int y = __shfl_up_sync(FULL, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) wsum[wid] = x;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int tot = 0;
+      for (int w = 0; w < 8; w++) {
+        int v = wsum[w];
+        wsum[w] = tot;
+        tot += v;
+      }
+      base_s = tot ? (long long)atomicAdd(&B.ctr->n_surv, (unsigned long long)tot) : 0;
+    }
+    __syncthreads();
+    long long pos = base_s + wsum[wid] + (x - cnt);
+    for (int k = 0; k < CUT_PER_THREAD; k++)
+      if (keepbits & (1u << k)) B.surv[pos++] = (int)(t0 + (long long)k * blockDim.x + threadIdx.x);
+    __syncthreads();
   }
-  warp_count(&B.ctr->n_shell, nshell);
+  block_count(&B.ctr->n_shell, nshell);
+  block_count(&B.ctr->n_massive, nmass);
+  block_count(&B.ctr->n_enum, nkeep);
 }
 
-/* ------------------------------------------------------------------- k_setup ----- */
-
-__device__ __forceinline__ int hp_nrings(const HaloRec &H) {
-  return H.ir_hi >= H.ir_lo ? H.ir_hi - H.ir_lo + 1 : 0;
-}
+/* -------------------------------------------------------------- ingest: set-up ----- */
 
 /* geometry, thresholds and interpolation constants of one halo from its loop
-   quantities (pks2map.f90:284-298 outputs).  Returns false if nothing is painted. */
-__device__ bool halo_geometry(const PaintParams &P, float xh, float yh, float zh, float rh,
+   quantities (pks2map.f90:284-298 outputs) */
+__device__ void halo_geometry(const PaintParams &P, float xh, float yh, float zh, float rh,
                               float chih, float mh, float redshift, HaloRec &H,
                               unsigned int *err) {
   /* haloproject.f90:47 / :93 */
@@ -108,11 +148,9 @@ __device__ bool halo_geometry(const PaintParams &P, float xh, float yh, float zh
   H.ichi = hi.ichi;
   H.imh = hi.imh;
   H.zero = hi.zero;
-  if (hi.zero && !(P.flags & 2)) return false;
-  /* corner offsets for the fast blend (all corners in range for every ir < nrt) */
   {
     long long nrt2 = 2LL * P.th.nrt;
-    int dm[4] = {0, 1, 0, 1}, dc[4] = {0, 0, 1, 1};
+    const int dm[4] = {0, 1, 0, 1}, dc[4] = {0, 0, 1, 1};
     for (int c = 0; c < 4; c++) {
       long long b = 2LL * (long long)P.th.nrt *
                     ((long long)(hi.imh - 1 + dm[c]) + (long long)P.th.nmht * (hi.ichi - 1 + dc[c]));
@@ -124,6 +162,7 @@ __device__ bool halo_geometry(const PaintParams &P, float xh, float yh, float zh
   H.jmax = 0;
   H.kmin = 1;
   H.kmax = 0;
+  H.theta_h = H.phi_h = 0.0f;
   if (P.npix_fs > 0 && !(zf < 0.0f)) {
     float th = p2m_asinf(xf), ph = p2m_asinf(yf);
     double w = DMUL((double)1.1f, (double)T);
@@ -150,6 +189,8 @@ __device__ bool halo_geometry(const PaintParams &P, float xh, float yh, float zh
   /* HEALPix disc (haloproject.f90:51-55) */
   H.ir_lo = 1;
   H.ir_hi = 0;
+  H.z0 = H.sth0 = H.phi0f = 0.0;
+  H.C_in = H.C_out = H.C_span = 0.0f;
   if (P.nside > 0) {
     H.hv[0] = FDIV(zf, chih);
     H.hv[1] = FDIV(yf, chih);
@@ -178,105 +219,84 @@ __device__ bool halo_geometry(const PaintParams &P, float xh, float yh, float zh
       H.ir_hi = hi_;
     }
   }
-  return true;
+}
+
+__device__ __forceinline__ void store_halo(const PaintParams &P, const IngestBuffers &B, long long s,
+                                           const HaloRec &H, unsigned long long &fsrows) {
+  B.halos[s] = H;
+  B.nring[s] = H.ir_hi >= H.ir_lo ? (unsigned)(H.ir_hi - H.ir_lo + 1) : 0u;
+  if (H.jmin <= H.jmax && H.kmin <= H.kmax) fsrows += (unsigned long long)(H.kmax - H.kmin + 1);
 }
 
 /* per-halo set-up from a catalogue record (pks2map.f90:264, :284-298) */
-__global__ void __launch_bounds__(256) k_setup(PaintParams P, PaintBuffers B) {
+__global__ void __launch_bounds__(256) k_setup(PaintParams P, IngestBuffers B) {
   long long n = (long long)B.ctr->n_surv;
-  long long stride = (long long)gridDim.x * blockDim.x;
-  int lane = threadIdx.x & 31;
-  for (long long base = (long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < n;
-       base += stride) {
-    long long s = base + lane;
+  unsigned long long fsrows = 0;
+  for (long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x; s < n;
+       s += (long long)gridDim.x * blockDim.x) {
+    int i = B.surv[s];
+    const float *r = B.records + (long long)i * P.nfloat;
+    float p0 = r[0], p1 = r[1], p2 = r[2], rth = r[6];
+    float mass = FMUL(P.mass_fac, FMUL(FMUL(rth, rth), rth));
+    float xh = p2, yh = p1, zh = p0;
+    float chih = FSQRT(FADD(FADD(FMUL(xh, xh), FMUL(yh, yh)), FMUL(zh, zh)));
+    float redshift = p2m_lookup(P.zofr, P.cosmo.dzofr, chih);
+    xh = FSUB(xh, P.chihview);
+    chih = FSQRT(FADD(FADD(FMUL(xh, xh), FMUL(yh, yh)), FMUL(zh, zh)));
+    float mh = FMUL(FSQRT(FDIV(p2m_deltacrit(&P.cosmo, redshift), P.bbps_delta)), mass);
+    float rh = p2m_powf(FDIV(FDIV(FDIV(FDIV(FMUL(3.0f, mh), 4.0f), P.cosmo.mypi), 200.0f),
+                             p2m_rhocrit(&P.cosmo, redshift)),
+                        0.333333343f);
     HaloRec H;
-    bool keep = false;
-    if (s < n) {
-      int i = B.surv[s];
-      const float *r = B.records + (long long)i * P.nfloat;
-      float p0 = r[0], p1 = r[1], p2 = r[2], rth = r[6];
-      float mass = FMUL(P.mass_fac, FMUL(FMUL(rth, rth), rth));
-      float xh = p2, yh = p1, zh = p0;
-      float chih = FSQRT(FADD(FADD(FMUL(xh, xh), FMUL(yh, yh)), FMUL(zh, zh)));
-      float redshift = p2m_lookup(P.zofr, P.cosmo.dzofr, chih);
-      xh = FSUB(xh, P.chihview);
-      chih = FSQRT(FADD(FADD(FMUL(xh, xh), FMUL(yh, yh)), FMUL(zh, zh)));
-      float mh = FMUL(FSQRT(FDIV(p2m_deltacrit(&P.cosmo, redshift), P.bbps_delta)), mass);
-      float rh = p2m_powf(
-          FDIV(FDIV(FDIV(FDIV(FMUL(3.0f, mh), 4.0f), P.cosmo.mypi), 200.0f),
-               p2m_rhocrit(&P.cosmo, redshift)),
-          0.333333343f);
-      H.rec = i;
-      H.w1 = 1.0f;
-      H.w2 = 1.0f;
-      if (P.any_ksz) {
-        /* intended per-halo -v_los/c of pksc.f90:70-74 */
-        float v0 = r[3], v1 = r[4], v2 = r[5];
-        float dot = FADD(FADD(FMUL(p0, v0), FMUL(p1, v1)), FMUL(p2, v2));
-        float nrm = FSQRT(FADD(FADD(FMUL(p0, p0), FMUL(p1, p1)), FMUL(p2, p2)));
-        H.w2 = -FDIV(FDIV(dot, nrm), 3.e5f);
-      }
-      keep = halo_geometry(P, xh, yh, zh, rh, chih, mh, redshift, H, &B.ctr->err);
+    H.rec = B.rec_base + i;
+    H.w1 = 1.0f;
+    H.w2 = 1.0f;
+    if (P.any_ksz) {
+      /* intended per-halo -v_los/c of pksc.f90:70-74 */
+      float v0 = r[3], v1 = r[4], v2 = r[5];
+      float dot = FADD(FADD(FMUL(p0, v0), FMUL(p1, v1)), FMUL(p2, v2));
+      float nrm = FSQRT(FADD(FADD(FMUL(p0, p0), FMUL(p1, p1)), FMUL(p2, p2)));
+      H.w2 = -FDIV(FDIV(dot, nrm), 3.e5f);
     }
-    long long slot = warp_append(&B.ctr->n_halo, keep);
-    if (keep) B.halos[slot] = H;
-    warp_count(&B.ctr->n_fs_rows,
-               (keep && H.jmin <= H.jmax && H.kmin <= H.kmax) ? (unsigned long long)(H.kmax - H.kmin + 1) : 0ull);
-    /* ring histogram: small discs per lane, large discs by the whole warp */
-    int nr = keep ? hp_nrings(H) : 0;
-    bool small = nr <= 64;
-    if (keep && small)
-      for (int ring = H.ir_lo; ring <= H.ir_hi; ring++) atomicAdd(&B.ring_hist[ring], 1u);
-    unsigned big = __ballot_sync(FULL, keep && !small);
-    while (big) {
-      int b = __ffs(big) - 1;
-      big &= big - 1;
-      int lo = __shfl_sync(FULL, H.ir_lo, b), hi = __shfl_sync(FULL, H.ir_hi, b);
-      for (int ring = lo + lane; ring <= hi; ring += 32) atomicAdd(&B.ring_hist[ring], 1u);
-    }
+    halo_geometry(P, xh, yh, zh, rh, chih, mh, redshift, H, &B.ctr->err);
+    store_halo(P, B, s, H, fsrows);
   }
+  block_count(&B.ctr->n_fs_rows, fsrows);
 }
 
 /* per-halo set-up from already-computed loop quantities (p2m_project_halo): 9 floats
    x, y, z, r, chi, m, redshift, v, profile per halo */
-__global__ void __launch_bounds__(256) k_setup_prepared(PaintParams P, PaintBuffers B,
+__global__ void __launch_bounds__(256) k_setup_prepared(PaintParams P, IngestBuffers B,
                                                         const float *prep, long long n) {
-  long long stride = (long long)gridDim.x * blockDim.x;
-  int lane = threadIdx.x & 31;
-  for (long long base = (long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < n;
-       base += stride) {
-    long long s = base + lane;
+  unsigned long long fsrows = 0;
+  for (long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x; s < n;
+       s += (long long)gridDim.x * blockDim.x) {
+    const float *q = prep + s * 9;
+    int prof = (int)q[8];
     HaloRec H;
-    bool keep = false;
-    if (s < n) {
-      const float *q = prep + s * 9;
-      int prof = (int)q[8];
-      H.rec = (int)s;
-      H.w1 = prof == 1 ? q[7] : 0.0f;
-      H.w2 = prof == 2 ? q[7] : 0.0f;
-      keep = halo_geometry(P, q[0], q[1], q[2], q[3], q[4], q[5], q[6], H, &B.ctr->err);
+    H.rec = B.rec_base + s;
+    H.w1 = prof == 1 ? q[7] : 0.0f;
+    H.w2 = prof == 2 ? q[7] : 0.0f;
+    halo_geometry(P, q[0], q[1], q[2], q[3], q[4], q[5], q[6], H, &B.ctr->err);
+    if (H.zero && !(P.flags & 2)) { /* table value identically zero: nothing to enumerate */
+      H.ir_lo = 1;
+      H.ir_hi = 0;
+      H.jmin = 1;
+      H.jmax = 0;
     }
-    long long slot = warp_append(&B.ctr->n_halo, keep);
-    if (keep) B.halos[slot] = H;
-    warp_count(&B.ctr->n_fs_rows,
-               (keep && H.jmin <= H.jmax && H.kmin <= H.kmax) ? (unsigned long long)(H.kmax - H.kmin + 1) : 0ull);
-    int nr = keep ? hp_nrings(H) : 0;
-    bool small = nr <= 64;
-    if (keep && small)
-      for (int ring = H.ir_lo; ring <= H.ir_hi; ring++) atomicAdd(&B.ring_hist[ring], 1u);
-    unsigned big = __ballot_sync(FULL, keep && !small);
-    while (big) {
-      int b = __ffs(big) - 1;
-      big &= big - 1;
-      int lo = __shfl_sync(FULL, H.ir_lo, b), hi = __shfl_sync(FULL, H.ir_hi, b);
-      for (int ring = lo + lane; ring <= hi; ring += 32) atomicAdd(&B.ring_hist[ring], 1u);
-    }
+    store_halo(P, B, s, H, fsrows);
   }
+  block_count(&B.ctr->n_fs_rows, fsrows);
+  long long mine = 0;
+  for (long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x; s < n;
+       s += (long long)gridDim.x * blockDim.x)
+    mine++;
+  block_count(&B.ctr->n_enum, (unsigned long long)mine);
 }
 
-/* -------------------------------------------------------------------- scans ----- */
+/* --------------------------------------------------------------------- scans ----- */
 
-/* exclusive scan of n (<= any) uint32 in one block; out[i] int64; *total = sum */
+/* exclusive scan of n uint32 in one block; out[i] int64; *total = sum */
 __global__ void __launch_bounds__(1024) k_scan_single(const unsigned int *in, long long *out,
                                                       long long n, unsigned long long *total) {
   __shared__ long long warp_sums[32];
@@ -300,7 +320,7 @@ __global__ void __launch_bounds__(1024) k_scan_single(const unsigned int *in, lo
         long long y = __shfl_up_sync(FULL, ws, o);
         if (lane >= o) ws += y;
       }
-      warp_sums[lane] = ws; /* inclusive */
+      warp_sums[lane] = ws;
     }
     __syncthreads();
     long long wofs = wid > 0 ? warp_sums[wid - 1] : 0;
@@ -314,7 +334,6 @@ __global__ void __launch_bounds__(1024) k_scan_single(const unsigned int *in, lo
 
 #define SCAN_BLOCKS 1024
 
-/* block sums of counts over SCAN_BLOCKS equal ranges of [0, n) */
 __global__ void __launch_bounds__(256) k_scan_partial(const unsigned int *in,
                                                       const unsigned long long *n_ptr,
                                                       long long *bsum) {
@@ -334,9 +353,7 @@ __global__ void __launch_bounds__(256) k_scan_partial(const unsigned int *in,
   }
 }
 
-__global__ void __launch_bounds__(1024) k_scan_top(long long *bsum,
-                                                   unsigned long long *total) {
-  /* exclusive scan of SCAN_BLOCKS int64 in place */
+__global__ void __launch_bounds__(1024) k_scan_top(long long *bsum, unsigned long long *total) {
   __shared__ long long sh[SCAN_BLOCKS];
   int t = threadIdx.x;
   sh[t] = bsum[t];
@@ -381,132 +398,124 @@ __global__ void __launch_bounds__(256) k_scan_apply(const unsigned int *in,
   }
 }
 
-/* -------------------------------------------------------------------- k_emit ----- */
+/* --------------------------------------------------------------- ingest: items ----- */
 
-__device__ __forceinline__ void emit_item(const PaintBuffers &B, int h, int ring) {
-  unsigned int k = atomicAdd(&B.ring_cursor[ring], 1u);
-  long long pos = B.ring_start[ring] + k;
+/* candidate span of ring `ring` of halo H: every pixel centre with chord^2 <= C_span
+   (a disc 2e-5 wider than dtheta) lies in [lo, lo+count); FP32 with a margin */
+__device__ __forceinline__ RingItem make_item(const PaintParams &P, const HaloRec &H, int h,
+                                              int ring) {
   RingItem it;
+  double2 zs = P.ringtab[ring];
+  double dz = zs.x - H.z0, ds = zs.y - H.sth0;
+  float A = (float)(dz * dz + ds * ds);
+  float Bc = (float)(4.0 * zs.y * H.sth0);
+  int npr, kshift;
+  long long npn;
+  p2m_ring_info(P.nside, ring, &npr, &kshift, &npn);
+  double q = H.phi0f * (double)npr;
+  double sh = 0.5 * kshift;
+  float cspan = H.C_span;
+  int lo = 0, cnt = 0;
+  bool full = false, empty = false;
+  float hw = 0.0f;
+  if (!(Bc > 1e-30f)) {
+    if (A < cspan) full = true;
+    else empty = true;
+  } else {
+    float t = (cspan - A) / Bc;
+    if (t <= 0.0f) empty = true;
+    else if (t >= 1.0f) full = true;
+    else hw = asinf(sqrtf(t)) * ((float)npr * 0.318309886f);
+  }
+  if (!empty) {
+    double eps = 0.02 + 1e-5 * (double)hw;
+    if (!full) {
+      long long l = (long long)ceil(q - sh - (double)hw - eps);
+      long long hh = (long long)floor(q - sh + (double)hw + eps);
+      if (hh - l + 1 >= npr) full = true;
+      else if (hh >= l) {
+        lo = (int)l;
+        cnt = (int)(hh - l + 1);
+      }
+    }
+    if (full) {
+      lo = (int)ceil(q - sh - 0.5 * (double)npr);
+      cnt = npr;
+    }
+  }
   it.halo = h;
   it.ring = ring;
-  it.lo = 0;
-  it.count = 0;
-  it.A = it.B = it.x0 = it.hdphi = 0.0f;
-  B.items[pos] = it;
+  it.lo = lo;
+  it.count = cnt;
+  it.A = A;
+  it.B = Bc;
+  it.x0 = (float)(((double)lo + sh) - q);
+  it.hdphi = 3.14159265358979f / (float)npr;
+  return it;
 }
 
-/* places every (halo, ring) item at its ring's slot range; appends flat-sky rows */
-__global__ void __launch_bounds__(256) k_emit(PaintParams P, PaintBuffers B) {
-  long long n = (long long)B.ctr->n_halo;
-  long long stride = (long long)gridDim.x * blockDim.x;
-  int lane = threadIdx.x & 31;
-  for (long long base = (long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < n;
-       base += stride) {
-    long long h = base + lane;
-    bool valid = h < n;
-    int lo = 1, hi = 0;
-    int jmin = 1, jmax = 0, kmin = 1, kmax = 0;
-    if (valid) {
-      const HaloRec &H = B.halos[h];
-      lo = H.ir_lo;
-      hi = H.ir_hi;
-      jmin = H.jmin;
-      jmax = H.jmax;
-      kmin = H.kmin;
-      kmax = H.kmax;
-    }
-    int nr = hi >= lo ? hi - lo + 1 : 0;
-    bool small = nr <= 64;
-    if (valid && small)
-      for (int ring = lo; ring <= hi; ring++) emit_item(B, (int)h, ring);
-    unsigned big = __ballot_sync(FULL, valid && !small);
-    while (big) {
-      int b = __ffs(big) - 1;
-      big &= big - 1;
-      int blo = __shfl_sync(FULL, lo, b), bhi = __shfl_sync(FULL, hi, b);
-      int hb = (int)__shfl_sync(FULL, (long long)h, b);
-      for (int ring = blo + lane; ring <= bhi; ring += 32) emit_item(B, hb, ring);
-    }
-    /* flat-sky rows */
-    if (valid && jmin <= jmax && kmin <= kmax) {
-      int nrow = kmax - kmin + 1;
-      unsigned long long fb = atomicAdd(&B.ctr->n_fs_items, (unsigned long long)nrow);
-      if ((long long)(fb + nrow) > B.fs_cap) {
-        atomicOr(&B.ctr->err, (unsigned)P2M_DEVERR_FS_OVERFLOW);
-      } else {
-        for (int t = 0; t < nrow; t++) {
-          FsItem f;
-          f.halo = (int)h;
-          f.k = kmin + t;
-          f.jmin = jmin;
-          f.count = jmax - jmin + 1;
-          B.fs_items[fb + t] = f;
-        }
+/* one warp expands 32 consecutive halos into their (halo, ring) items */
+__global__ void __launch_bounds__(256) k_items(PaintParams P, IngestBuffers B) {
+  const long long n = (long long)B.ctr->n_surv;
+  const int lane = threadIdx.x & 31;
+  const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+  for (long long h0 = warp * 32; h0 < n; h0 += nwarps * 32) {
+    long long h = h0 + lane;
+    long long off = h < n ? B.ioff[h] : (1LL << 62);
+    long long off0 = __shfl_sync(FULL, off, 0);
+    long long hl = min(h0 + 31, n - 1);
+    long long end = B.ioff[hl] + B.nring[hl];
+    int rel = (int)min(off - off0, (long long)0x7fffffff);
+    int total = (int)(end - off0);
+    for (int t = lane; t < total + ((32 - (total & 31)) & 31); t += 32) {
+      bool act = t < total;
+      int j = 0;
+#pragma unroll
+      for (int step = 16; step > 0; step >>= 1) {
+        int o = __shfl_sync(FULL, rel, j + step);
+        if (o <= t) j += step;
+      }
+      int relj = __shfl_sync(FULL, rel, j);
+      if (act) {
+        long long hh = h0 + j;
+        const HaloRec &H = B.halos[hh];
+        int ring = H.ir_lo + (t - relj);
+        RingItem it = make_item(P, H, (int)(B.halo_base + hh), ring);
+        B.items[off0 + t] = it;
+        int band = P.band_of_ring[ring];
+        unsigned grp = __match_any_sync(__activemask(), band);
+        if ((int)(__ffs(grp) - 1) == lane) atomicAdd(&B.band_hist[band], (unsigned)__popc(grp));
       }
     }
   }
 }
 
-/* ------------------------------------------------------------------- k_rings ----- */
+/* ------------------------------------------------------------------ flat sky ----- */
 
-/* candidate span of one (halo, ring): every pixel centre with chord^2 <= C_span
-   (a disc 2e-5 wider than dtheta) lies in [lo, lo+count); FP32 with a margin */
-__global__ void __launch_bounds__(256) k_rings(PaintParams P, PaintBuffers B) {
-  long long n = (long long)B.ctr->n_items;
-  long long stride = (long long)gridDim.x * blockDim.x;
-  for (long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x; g < n; g += stride) {
-    RingItem it = B.items[g];
-    const HaloRec &H = B.halos[it.halo];
-    double2 zs = P.ringtab[it.ring];
-    double dz = zs.x - H.z0, ds = zs.y - H.sth0;
-    float A = (float)(dz * dz + ds * ds);
-    float Bc = (float)(4.0 * zs.y * H.sth0);
-    int npr, kshift;
-    long long npn;
-    p2m_ring_info(P.nside, it.ring, &npr, &kshift, &npn);
-    double q = H.phi0f * (double)npr;
-    double sh = 0.5 * kshift;
-    float cspan = H.C_span;
-    int lo = 0, cnt = 0;
-    bool full = false, empty = false;
-    float hw = 0.0f;
-    if (!(Bc > 1e-30f)) {
-      if (A < cspan) full = true;
-      else empty = true;
-    } else {
-      float t = (cspan - A) / Bc;
-      if (t <= 0.0f) empty = true;
-      else if (t >= 1.0f) full = true;
-      else hw = asinf(sqrtf(t)) * ((float)npr * 0.318309886f);
+/* appends the (halo, row) items of every halo with a flat-sky box */
+__global__ void __launch_bounds__(256) k_fs_emit(PaintParams P, IngestBuffers B) {
+  long long n = (long long)B.ctr->n_surv;
+  for (long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x; s < n;
+       s += (long long)gridDim.x * blockDim.x) {
+    const HaloRec &H = B.halos[s];
+    if (H.jmin > H.jmax || H.kmin > H.kmax) continue;
+    int nrow = H.kmax - H.kmin + 1;
+    unsigned long long fb = atomicAdd(&B.ctr->n_fs_items, (unsigned long long)nrow);
+    if ((long long)(fb + nrow) > B.fs_cap) {
+      atomicOr(&B.ctr->err, (unsigned)P2M_DEVERR_FS_OVERFLOW);
+      continue;
     }
-    if (!empty) {
-      double eps = 0.02 + 1e-5 * (double)hw;
-      if (!full) {
-        long long l = (long long)ceil(q - sh - (double)hw - eps);
-        long long h = (long long)floor(q - sh + (double)hw + eps);
-        if (h - l + 1 >= npr) full = true;
-        else if (h >= l) {
-          lo = (int)l;
-          cnt = (int)(h - l + 1);
-        }
-      }
-      if (full) {
-        lo = (int)ceil(q - sh - 0.5 * (double)npr);
-        cnt = npr;
-      }
+    for (int t = 0; t < nrow; t++) {
+      FsItem f;
+      f.halo = (int)s;
+      f.k = H.kmin + t;
+      f.jmin = H.jmin;
+      f.count = H.jmax - H.jmin + 1;
+      B.fs_items[fb + t] = f;
     }
-    it.lo = lo;
-    it.count = cnt;
-    it.A = A;
-    it.B = Bc;
-    it.x0 = (float)(((double)lo + sh) - q);
-    it.hdphi = 3.14159265358979f / (float)npr;
-    B.items[g] = it;
-    B.counts[g] = (unsigned int)cnt;
   }
 }
-
-/* ------------------------------------------------------------------- deposit ----- */
 
 template <int PREC>
 __device__ __forceinline__ void deposit(void *acc, long long idx, float v) {
@@ -523,14 +532,15 @@ __device__ __forceinline__ void deposit(void *acc, long long idx, float v) {
   }
 }
 
-/* profile values of every map at one pixel (maptable.f90:204-212 with known ir, fr) */
+/* profile values of every map at one pixel (maptable.f90:204-212 with known ir, fr),
+   deposited at slot `slot` of acc (nmaps entries per slot) */
 template <int PREC>
-__device__ __forceinline__ void deposit_maps(const PaintParams &P, const HaloRec &H,
-                                             void *acc, long long pix, int ir, float fr) {
+__device__ __forceinline__ void deposit_maps(const PaintParams &P, const HaloRec &H, void *acc,
+                                             long long slot, int ir, float fr) {
   float ofr = FSUB(1.0f, fr), ofc = FSUB(1.0f, H.fc), ofm = FSUB(1.0f, H.fm);
   float fc = H.fc, fm = H.fm;
-  bool fast = H.cbase[0] >= 0 && H.cbase[1] >= 0 && H.cbase[2] >= 0 && H.cbase[3] >= 0;
-  p2m_hinterp hi = halo_hinterp(H);
+  bool fast = H.cbase[0] >= 0 && H.cbase[1] >= 0 && H.cbase[2] >= 0 && H.cbase[3] >= 0 &&
+              ir >= 1 && ir < P.th.nrt;
   for (int m = 0; m < P.nmaps; m++) {
     int prof = P.map_profile[m];
     float w = prof == 2 ? H.w2 : H.w1;
@@ -553,220 +563,17 @@ __device__ __forceinline__ void deposit_maps(const PaintParams &P, const HaloRec
       v = FADD(v, FMUL(FMUL(FMUL(t11a, ofr), fc), fm));
       v = FADD(v, FMUL(FMUL(FMUL(t11b, fr), fc), fm));
     } else {
+      p2m_hinterp hi = halo_hinterp(H);
       v = p2m_blend8(tab, &P.th, &hi, prof, ir, fr);
     }
-    deposit<PREC>(acc, pix * P.nmaps + m, FMUL(w, v));
+    deposit<PREC>(acc, slot * P.nmaps + m, FMUL(w, v));
   }
 }
-
-__device__ __forceinline__ void record_set(const PaintBuffers &B, const HaloRec &H, long long pix) {
-  unsigned long long k = atomicAdd(&B.ctr->n_sets, 1ull);
-  if ((long long)k < B.set_cap) {
-    B.set_rec[k] = H.rec;
-    B.set_pix[k] = pix;
-  }
-}
-
-/* exact decision and deposit for one candidate: the reference's FP64 pixel centre and
-   angular distance (haloproject.f90:60-73) and the float interpolation */
-template <int PREC>
-__device__ void paint_exact_pixel(const PaintParams &P, const PaintBuffers &B, const HaloRec &H,
-                                  long long pix, unsigned long long &nupd) {
-  double v2[3], v1[3] = {(double)H.hv[0], (double)H.hv[1], (double)H.hv[2]};
-  p2m_pix2vec_ring(P.nside, pix, v2);
-  float angle = (float)p2m_angdist(v1, v2);
-  if (!((double)angle < (double)H.T)) return;
-  nupd++;
-  if (P.flags & 1) record_set(B, H, pix);
-  if (H.zero) return;
-  float r = FMUL(H.chi_t, p2m_tanf(angle));
-  if (r > P.th.rmaxt) return;
-  int ir;
-  float fr;
-  p2m_rindex(&P.th, r, &ir, &fr);
-  deposit_maps<PREC>(P, H, B.hp_acc, pix, ir, fr);
-}
-
-/* ------------------------------------------------------------------- k_paint ----- */
-
-#define PAINT_CHUNK 1024
-
-/* largest g in [0, n) with off[g] <= p (off[0] = 0), found by the whole warp */
-__device__ __forceinline__ long long warp_upper(const long long *off, long long n, long long p) {
-  int lane = threadIdx.x & 31;
-  long long lo = 0, hi = n;
-  while (hi - lo > 32) {
-    long long span = hi - lo;
-    long long s = lo + (span * lane) / 32;
-    bool le = off[s] <= p;
-    unsigned m = __ballot_sync(FULL, le);
-    int t = 31 - __clz(m); /* lane 0 always true */
-    long long nlo = lo + (span * t) / 32;
-    long long nhi = t < 31 ? lo + (span * (t + 1)) / 32 : hi;
-    lo = nlo;
-    hi = nhi;
-  }
-  long long s = lo + lane;
-  bool le = s < hi && off[s] <= p;
-  unsigned m = __ballot_sync(FULL, le);
-  return lo + (31 - __clz(m));
-}
-
-template <int PREC>
-__global__ void __launch_bounds__(256) k_paint(PaintParams P, PaintBuffers B) {
-  const long long npix_c = (long long)B.ctr->n_pix;
-  const long long nitems = (long long)B.ctr->n_items;
-  if (npix_c == 0) return;
-  const int lane = threadIdx.x & 31;
-  const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
-  const long long nchunks = (npix_c + PAINT_CHUNK - 1) / PAINT_CHUNK;
-  unsigned long long nupd = 0, nfb = 0;
-  for (long long c = warp; c < nchunks; c += nwarps) {
-    long long p0 = c * PAINT_CHUNK, p1 = min(npix_c, p0 + PAINT_CHUNK);
-    long long g0 = warp_upper(B.pix_off, nitems, p0);
-    long long woff = (g0 + lane < nitems) ? B.pix_off[g0 + lane] : (1LL << 62);
-    long long wend = (g0 + 32 < nitems) ? B.pix_off[g0 + 32] : (1LL << 62);
-    for (long long base = p0; base < p1; base += 32) {
-      long long p = base + lane;
-      bool todo = p < p1;
-      /* every round serves at least the lowest pending lane: <= 32 rounds */
-      for (int round = 0; __any_sync(FULL, todo); round++) {
-        if (round >= 64) {
-          atomicOr(&B.ctr->err, (unsigned)P2M_DEVERR_ITEMS);
-          break;
-        }
-        /* slide the 32-item window so that it starts at the item holding the lowest
-           pending pixel */
-        long long pmin = todo ? p : (1LL << 62);
-        for (int o = 16; o > 0; o >>= 1) pmin = min(pmin, __shfl_xor_sync(FULL, pmin, o));
-        unsigned m = __ballot_sync(FULL, woff <= pmin);
-        int j0 = m ? 31 - __clz(m) : -1;
-        if (j0 != 0 || pmin >= wend) {
-          if (j0 < 0 || pmin >= wend) g0 = warp_upper(B.pix_off, nitems, pmin);
-          else g0 += j0;
-          woff = (g0 + lane < nitems) ? B.pix_off[g0 + lane] : (1LL << 62);
-          wend = (g0 + 32 < nitems) ? B.pix_off[g0 + 32] : (1LL << 62);
-        }
-        bool here = todo && p < wend;
-        /* item of p inside the window: binary search over lanes */
-        int j = 0;
-#pragma unroll
-        for (int step = 16; step > 0; step >>= 1) {
-          long long o = __shfl_sync(FULL, woff, j + step);
-          if (o <= p) j += step;
-        }
-        long long ooff = __shfl_sync(FULL, woff, j);
-        if (here) {
-          todo = false;
-          long long g = g0 + j;
-          const RingItem &it = B.items[g];
-          const HaloRec &H = B.halos[it.halo];
-          int k = (int)(p - ooff);
-          int npr, kshift;
-          long long npn;
-          p2m_ring_info(P.nside, it.ring, &npr, &kshift, &npn);
-          int iphi = it.lo + k;
-          if (iphi < 0) iphi += npr;
-          if (iphi >= npr) iphi -= npr;
-          long long pix = npn - npr + iphi;
-          if (PREC == 0) {
-            paint_exact_pixel<0>(P, B, H, pix, nupd);
-          } else {
-            float x = it.x0 + (float)k;
-            float s = sinf(x * it.hdphi);
-            float c2 = it.A + it.B * (s * s);
-            if (c2 < H.C_out) {
-              bool recheck = c2 > H.C_in;
-              int ir = 0;
-              float fr = 0.0f;
-              bool zero_val = false;
-              if (!recheck) {
-                float h2 = 0.25f * c2;
-                float cosd = 1.0f - 2.0f * h2;
-                if (cosd < 0.05f) {
-                  recheck = true;
-                } else {
-                  float sind = 2.0f * sqrtf(h2 * (1.0f - h2));
-                  float r = H.chi_t * __fdividef(sind, cosd);
-                  const float dr = 1e-5f;
-                  if (r > P.th.rmaxt * (1.0f + dr)) {
-                    zero_val = true;
-                  } else if (r >= P.th.rmaxt * (1.0f - dr)) {
-                    recheck = true;
-                  } else if (r < P.th.rmint * (1.0f - dr)) {
-                    ir = P.ir_c;
-                    fr = P.fr_c;
-                  } else if (r <= P.th.rmint * (1.0f + dr)) {
-                    recheck = true;
-                  } else {
-                    float lr = __logf(r);
-                    float u = (lr - P.th.lrmin) / P.th.drt;
-                    int iu = (int)u;
-                    float fu = u - (float)iu;
-                    if (fu < 2e-4f || fu > 1.0f - 2e-4f || iu < 0 || iu > P.th.nrt - 2) {
-                      recheck = true;
-                    } else {
-                      ir = iu + 1;
-                      fr = FSUB(lr, FADD(P.th.lrmin, FMUL((float)(ir - 1), P.th.drt)));
-                    }
-                  }
-                }
-              }
-              if (recheck) {
-                unsigned long long slot = atomicAdd(&B.ctr->n_fb, 1ull);
-                if ((long long)slot < B.fb_cap)
-                  B.fb[slot] = ((unsigned long long)g << 32) | (unsigned int)k;
-                else
-                  atomicOr(&B.ctr->err, (unsigned)P2M_DEVERR_FB_OVERFLOW);
-                nfb++;
-              } else {
-                nupd++;
-                if (P.flags & 1) record_set(B, H, pix);
-                if (!zero_val && !H.zero) deposit_maps<1>(P, H, B.hp_acc, pix, ir, fr);
-              }
-            }
-          }
-        }
-      }
-    }
-  }
-  warp_count(&B.ctr->hp_updates, nupd);
-  warp_count(&B.ctr->n_recheck, nfb);
-}
-
-/* exact FP64 decision for the pixels the mixed-precision test could not settle */
-__global__ void __launch_bounds__(256) k_recheck(PaintParams P, PaintBuffers B) {
-  long long n = (long long)min(B.ctr->n_fb, (unsigned long long)B.fb_cap);
-  long long stride = (long long)gridDim.x * blockDim.x;
-  unsigned long long nupd = 0;
-  for (long long base = (long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < n;
-       base += stride) {
-    long long e = base + (threadIdx.x & 31);
-    if (e < n) {
-      unsigned long long v = B.fb[e];
-      long long g = (long long)(v >> 32);
-      int k = (int)(v & 0xffffffffu);
-      const RingItem &it = B.items[g];
-      const HaloRec &H = B.halos[it.halo];
-      int npr, kshift;
-      long long npn;
-      p2m_ring_info(P.nside, it.ring, &npr, &kshift, &npn);
-      int iphi = it.lo + k;
-      if (iphi < 0) iphi += npr;
-      if (iphi >= npr) iphi -= npr;
-      paint_exact_pixel<1>(P, B, H, npn - npr + iphi, nupd);
-    }
-  }
-  warp_count(&B.ctr->hp_updates, nupd);
-}
-
-/* ----------------------------------------------------------------- flat sky ----- */
 
 /* haloproject.f90:136-152: one warp per (halo, row); every operation is the
    reference's float sequence, so the pixel set and values are exact */
 template <int PREC>
-__global__ void __launch_bounds__(256) k_paint_fs(PaintParams P, PaintBuffers B) {
+__global__ void __launch_bounds__(256) k_paint_fs(PaintParams P, IngestBuffers B) {
   long long n = (long long)min(B.ctr->n_fs_items, (unsigned long long)B.fs_cap);
   const int lane = threadIdx.x & 31;
   const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -799,33 +606,447 @@ __global__ void __launch_bounds__(256) k_paint_fs(PaintParams P, PaintBuffers B)
   warp_count(&B.ctr->fs_updates, nupd);
 }
 
-/* ----------------------------------------------------------------- finalize ----- */
+/* ------------------------------------------------------------ sweep: grouping ----- */
 
+__global__ void __launch_bounds__(256) k_band_scatter(PaintParams P, const RingItem *in, long long n,
+                                                      const long long *band_start,
+                                                      unsigned int *band_cursor, RingItem *out,
+                                                      unsigned int *counts) {
+  const int lane = threadIdx.x & 31;
+  for (long long base = (long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < n;
+       base += (long long)gridDim.x * blockDim.x) {
+    long long g = base + lane;
+    bool act = g < n;
+    RingItem it;
+    int band = -1 - lane; /* distinct keys for inactive lanes */
+    if (act) {
+      it = in[g];
+      band = P.band_of_ring[it.ring];
+    }
+    unsigned grp = __match_any_sync(FULL, band);
+    int leader = __ffs(grp) - 1;
+    unsigned k0 = 0;
+    if (act && lane == leader) k0 = atomicAdd(&band_cursor[band], (unsigned)__popc(grp));
+    k0 = __shfl_sync(FULL, k0, leader);
+    if (act) {
+      long long pos = band_start[band] + k0 + __popc(grp & ((1u << lane) - 1u));
+      out[pos] = it;
+      counts[pos] = (unsigned)it.count;
+    }
+  }
+}
+
+/* unit queue of the sweep: segments P0, P1, D0, P2, D1, ..., P_{B-1}, D_{B-2}, D_{B-1}
+   (P_b: paint units of band b, D_b: drain units of band b) */
+__global__ void k_units(SweepBuffers W, long long *band_item0, long long *band_cand0, int *seg_start,
+                        int *seg_code, int *unit_target, const long long *band_pix0,
+                        const unsigned long long *n_pix) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  int nb = W.nbands;
+  long long ni = W.n_items;
+  long long np = (long long)*n_pix;
+  for (int b = 0; b <= nb; b++) {
+    long long i0 = band_item0[b];
+    band_cand0[b] = (b == nb || i0 >= ni) ? np : W.pix_off[i0];
+  }
+  for (int b = 0; b < nb; b++) {
+    long long c = band_cand0[b + 1] - band_cand0[b];
+    unit_target[b] = (int)((c + P2M_PAINT_UNIT - 1) / P2M_PAINT_UNIT);
+    long long px = band_pix0[b + 1] - band_pix0[b];
+    unit_target[nb + b] = (int)((px + P2M_DRAIN_UNIT - 1) / P2M_DRAIN_UNIT);
+  }
+  int k = 0, acc = 0;
+  for (int b = 0; b < nb; b++) {
+    seg_start[k] = acc;
+    seg_code[k] = b;
+    acc += unit_target[b];
+    k++;
+    if (b >= 1) {
+      seg_start[k] = acc;
+      seg_code[k] = (b - 1) | (1 << 30);
+      acc += unit_target[nb + b - 1];
+      k++;
+    }
+  }
+  seg_start[k] = acc;
+  seg_code[k] = (nb - 1) | (1 << 30);
+  acc += unit_target[nb + nb - 1];
+  k++;
+  seg_start[k] = acc;
+}
+
+/* ---------------------------------------------------------- sweep: the painting ----- */
+
+/* largest g in [lo, hi) with off[g] <= p (off[lo] <= p), found by the whole warp */
+__device__ __forceinline__ long long warp_upper(const long long *off, long long lo, long long hi,
+                                                long long p) {
+  int lane = threadIdx.x & 31;
+  while (hi - lo > 32) {
+    long long span = hi - lo;
+    long long s = lo + (span * lane) / 32;
+    bool le = off[s] <= p;
+    unsigned m = __ballot_sync(FULL, le);
+    int t = m ? 31 - __clz(m) : 0;
+    long long nlo = lo + (span * t) / 32;
+    long long nhi = t < 31 ? lo + (span * (t + 1)) / 32 : hi;
+    lo = nlo;
+    hi = nhi;
+  }
+  long long s = lo + lane;
+  bool le = s < hi && off[s] <= p;
+  unsigned m = __ballot_sync(FULL, le);
+  return lo + (m ? 31 - __clz(m) : 0);
+}
+
+struct ExactRes {
+  bool inside, zero;
+  int ir;
+  float fr, u;
+};
+
+/* the reference's decision and interpolation inputs for one pixel: FP64 pixel centre
+   and angular distance (haloproject.f90:63-70), float interpolation (maptable.f90) */
+__device__ ExactRes exact_eval(const PaintParams &P, const HaloRec &H, long long pix) {
+  ExactRes e;
+  e.inside = false;
+  e.zero = false;
+  e.ir = 0;
+  e.fr = 0.0f;
+  e.u = 0.0f;
+  double v2[3], v1[3] = {(double)H.hv[0], (double)H.hv[1], (double)H.hv[2]};
+  p2m_pix2vec_ring(P.nside, pix, v2);
+  float angle = (float)p2m_angdist(v1, v2);
+  if (!((double)angle < (double)H.T)) return e;
+  e.inside = true;
+  if (H.zero) {
+    e.zero = true;
+    return e;
+  }
+  float r = FMUL(H.chi_t, p2m_tanf(angle));
+  if (r > P.th.rmaxt) {
+    e.zero = true;
+    return e;
+  }
+  p2m_rindex(&P.th, r, &e.ir, &e.fr);
+  float rr = r < P.th.rmint ? FADD(P.th.rmint, 1e-5f) : r;
+  e.u = FDIV(FSUB(p2m_logf(rr), P.th.lrmin), P.th.drt);
+  return e;
+}
+
+__device__ __forceinline__ void record_set(long long *set_rec, long long *set_pix, long long cap,
+                                           unsigned long long *ctr, long long rec, long long pix) {
+  unsigned long long k = atomicAdd(ctr, 1ull);
+  if ((long long)k < cap) {
+    set_rec[k] = rec;
+    set_pix[k] = pix;
+  }
+}
+
+/* Fast mixed-precision decision for one candidate.  Returns 0 outside, 1 inside with
+   (ir, fr) or zero value, 2 when the exact path must decide. */
+__device__ __forceinline__ int fast_decide(const PaintParams &P, const RingItem &it,
+                                           const HaloRec &H, int k, int &ir, float &fr,
+                                           bool &zero_val, float &u_out) {
+  float x = it.x0 + (float)k;
+  float s = sinf(x * it.hdphi);
+  float c2 = it.A + it.B * (s * s);
+  if (c2 >= H.C_out) return 0;
+  if (c2 > H.C_in) return 2;
+  zero_val = false;
+  float h2 = 0.25f * c2;
+  float cosd = 1.0f - 2.0f * h2;
+  if (cosd < 0.05f) return 2;
+  float sind = 2.0f * sqrtf(h2 * (1.0f - h2));
+  float r = H.chi_t * __fdividef(sind, cosd);
+  const float dr = 1e-5f;
+  if (r > P.th.rmaxt * (1.0f + dr)) {
+    zero_val = true;
+    return 1;
+  }
+  if (r >= P.th.rmaxt * (1.0f - dr)) return 2;
+  if (r < P.th.rmint * (1.0f - dr)) {
+    ir = P.ir_c;
+    fr = P.fr_c;
+    u_out = -1.0f;
+    return 1;
+  }
+  if (r <= P.th.rmint * (1.0f + dr)) return 2;
+  float lr = __logf(r);
+  float u = (lr - P.th.lrmin) / P.th.drt;
+  int iu = (int)u;
+  float fu = u - (float)iu;
+  if (fu < P.band_u || fu > 1.0f - P.band_u || iu < 0 || iu > P.th.nrt - 2) return 2;
+  ir = iu + 1;
+  fr = FSUB(lr, FADD(P.th.lrmin, FMUL((float)(ir - 1), P.th.drt)));
+  u_out = u;
+  return 1;
+}
+
+/* one candidate pixel of the mixed path: deposit into `acc` at slot pix - pix0 */
+__device__ __forceinline__ void mixed_pixel(const PaintParams &P, const SweepBuffers &W,
+                                            const RingItem &it, const HaloRec &H, int k,
+                                            long long pix, void *acc, long long pix0,
+                                            unsigned long long &nupd, unsigned long long &nrc) {
+  int ir = 0;
+  float fr = 0.0f, u = 0.0f;
+  bool zero_val = H.zero;
+  int d = fast_decide(P, it, H, k, ir, fr, zero_val, u);
+  if (P.flags & 8) { /* validation: compare every fast decision with the exact path */
+    ExactRes e = exact_eval(P, H, pix);
+    atomicAdd(&W.ctr->val_checked, 1ull);
+    if (d != 2) {
+      if ((d == 1) != e.inside) atomicAdd(&W.ctr->val_bad_set, 1ull);
+      else if (d == 1 && e.inside && !e.zero && !zero_val) {
+        if (e.ir != ir) atomicAdd(&W.ctr->val_bad_index, 1ull);
+        if (u >= 0.0f) atomicMax(&W.ctr->val_max_du, __float_as_uint(fabsf(u - e.u)));
+      }
+    }
+  }
+  if (d == 0) return;
+  if (d == 2) {
+    nrc++;
+    ExactRes e = exact_eval(P, H, pix);
+    if (!e.inside) return;
+    zero_val = e.zero;
+    ir = e.ir;
+    fr = e.fr;
+  }
+  nupd++;
+  if (P.flags & 1) record_set(W.set_rec, W.set_pix, W.set_cap, &W.ctr->n_sets, H.rec, pix);
+  if (!zero_val && !H.zero) deposit_maps<1>(P, H, acc, pix - pix0, ir, fr);
+}
+
+/* walk candidates [p0, p1) of items [ilo, ihi): one warp; PREC 0 deposits the exact
+   path into a full-sky FP64 accumulator, PREC 1 the mixed path into acc - pix0 */
 template <int PREC>
-__global__ void __launch_bounds__(256) k_finalize(const void *acc, long long npix, int nmaps,
-                                                  int map, float *out, double *sum) {
-  long long stride = (long long)gridDim.x * blockDim.x;
+__device__ void walk_candidates(const PaintParams &P, const SweepBuffers &W, long long p0,
+                                long long p1, long long ilo, long long ihi, void *acc,
+                                long long pix0, unsigned long long &nupd,
+                                unsigned long long &nrc) {
+  const int lane = threadIdx.x & 31;
+  const long long *off = W.pix_off;
+  long long g0 = warp_upper(off, ilo, ihi, p0);
+  long long woff = (g0 + lane < ihi) ? off[g0 + lane] : (1LL << 62);
+  long long wend = (g0 + 32 < ihi) ? off[g0 + 32] : (1LL << 62);
+  for (long long base = p0; base < p1; base += 32) {
+    long long p = base + lane;
+    bool todo = p < p1;
+    /* every round serves at least the lowest pending lane: <= 32 rounds */
+    for (int round = 0; __any_sync(FULL, todo); round++) {
+      if (round >= 64) {
+        atomicOr(&W.ctr->err, (unsigned)P2M_DEVERR_ITEMS);
+        return;
+      }
+      long long pmin = todo ? p : (1LL << 62);
+      for (int o = 16; o > 0; o >>= 1) pmin = min(pmin, __shfl_xor_sync(FULL, pmin, o));
+      unsigned m = __ballot_sync(FULL, woff <= pmin);
+      int j0 = m ? 31 - __clz(m) : -1;
+      if (j0 != 0 || pmin >= wend) {
+        if (j0 < 0 || pmin >= wend) g0 = warp_upper(off, ilo, ihi, pmin);
+        else g0 += j0;
+        woff = (g0 + lane < ihi) ? off[g0 + lane] : (1LL << 62);
+        wend = (g0 + 32 < ihi) ? off[g0 + 32] : (1LL << 62);
+      }
+      bool here = todo && p < wend;
+      int j = 0;
+#pragma unroll
+      for (int step = 16; step > 0; step >>= 1) {
+        long long o = __shfl_sync(FULL, woff, j + step);
+        if (o <= p) j += step;
+      }
+      long long ooff = __shfl_sync(FULL, woff, j);
+      if (here) {
+        todo = false;
+        const RingItem &it = W.items[g0 + j];
+        const HaloRec &H = W.halos[it.halo];
+        int k = (int)(p - ooff);
+        int npr, kshift;
+        long long npn;
+        p2m_ring_info(P.nside, it.ring, &npr, &kshift, &npn);
+        int iphi = it.lo + k;
+        if (iphi < 0) iphi += npr;
+        if (iphi >= npr) iphi -= npr;
+        long long pix = npn - npr + iphi;
+        if (PREC == 0) {
+          ExactRes e = exact_eval(P, H, pix);
+          if (e.inside) {
+            nupd++;
+            if (P.flags & 1) record_set(W.set_rec, W.set_pix, W.set_cap, &W.ctr->n_sets, H.rec, pix);
+            if (!e.zero) deposit_maps<0>(P, H, acc, pix, e.ir, e.fr);
+          }
+        } else {
+          RingItem itc = it;
+          mixed_pixel(P, W, itc, H, k, pix, acc, pix0, nupd, nrc);
+        }
+      }
+    }
+  }
+}
+
+/* bounded wait for *flag >= target (thread 0 only); false on abort or timeout */
+__device__ bool wait_geq(const unsigned *flag, unsigned target, DevCounters *ctr) {
+  for (long it = 0; it < (1L << 23); it++) {
+    if (ld_acquire(flag) >= target) return true;
+    if (ld_acquire(&ctr->abort)) return false;
+    __nanosleep(200);
+  }
+  atomicOr(&ctr->err, (unsigned)P2M_DEVERR_TIMEOUT);
+  atomicExch(&ctr->abort, 1u);
+  return false;
+}
+
+#define MAX_SEG 4096
+
+/* persistent sweep: claims units in queue order (see k_units) */
+__global__ void __launch_bounds__(P2M_SWEEP_THREADS) k_sweep(PaintParams P, SweepBuffers W) {
+  __shared__ int s_seg[MAX_SEG + 1];
+  __shared__ int s_u, s_ok;
+  __shared__ double s_sum[P2M_MAXMAPS];
+  const int nseg = 2 * W.nbands;
+  for (int k = threadIdx.x; k <= nseg; k += blockDim.x) s_seg[k] = W.seg_start[k];
+  if (threadIdx.x < P2M_MAXMAPS) s_sum[threadIdx.x] = 0.0;
+  __syncthreads();
+  const int total = s_seg[nseg];
+  const int wid = threadIdx.x >> 5;
+  const int nwarp = blockDim.x >> 5;
+  unsigned long long nupd = 0, nrc = 0, ncand = 0;
+  double msum[P2M_MAXMAPS];
+  for (int m = 0; m < P2M_MAXMAPS; m++) msum[m] = 0.0;
+  for (;;) {
+    if (threadIdx.x == 0) s_u = ld_acquire(&W.ctr->abort) ? total : (int)atomicAdd(&W.ctr->next_unit, 1u);
+    __syncthreads();
+    const int u = s_u;
+    if (u >= total) break;
+    int lo = 0, hi = nseg; /* largest seg with s_seg[seg] <= u */
+    while (hi - lo > 1) {
+      int mid = (lo + hi) >> 1;
+      if (s_seg[mid] <= u) lo = mid;
+      else hi = mid;
+    }
+    const int code = W.seg_code[lo];
+    const int band = code & 0x3fffffff;
+    const bool drain = (code >> 30) & 1;
+    const int k = u - s_seg[lo];
+    float2 *win = W.win + (long long)(band % P2M_NBUF) * W.wpix * P.nmaps;
+    const long long pix0 = W.band_pix0[band];
+    if (threadIdx.x == 0) {
+      bool ok = true;
+      if (!drain && band >= P2M_NBUF)
+        ok = wait_geq(&W.drain_done[band - P2M_NBUF], (unsigned)W.unit_target[W.nbands + band - P2M_NBUF], W.ctr);
+      if (drain) ok = wait_geq(&W.paint_done[band], (unsigned)W.unit_target[band], W.ctr);
+      __threadfence();
+      s_ok = ok;
+    }
+    __syncthreads();
+    if (!s_ok) break;
+    if (!drain) {
+      long long c0 = W.band_cand0[band] + (long long)k * P2M_PAINT_UNIT;
+      long long c1 = min(c0 + P2M_PAINT_UNIT, W.band_cand0[band + 1]);
+      const long long per = P2M_PAINT_UNIT / (P2M_SWEEP_THREADS / 32);
+      long long a = c0 + (long long)wid * per, b = min(a + per, c1);
+      if (a < b) {
+        walk_candidates<1>(P, W, a, b, W.band_item0[band], W.band_item0[band + 1], (void *)win, pix0,
+                           nupd, nrc);
+        if ((threadIdx.x & 31) == 0) ncand += (unsigned long long)(b - a);
+      }
+      __threadfence();
+      __syncthreads();
+      if (threadIdx.x == 0) atomicAdd(&W.paint_done[band], 1u);
+    } else {
+      long long q0 = pix0 + (long long)k * P2M_DRAIN_UNIT;
+      long long q1 = min(q0 + P2M_DRAIN_UNIT, W.band_pix0[band + 1]);
+      for (long long p = q0 + threadIdx.x; p < q1; p += blockDim.x) {
+        long long slot = (p - pix0) * P.nmaps;
+        for (int m = 0; m < P.nmaps; m++) {
+          float2 a = __ldcg(win + slot + m);
+          float v = __fadd_rn(a.x, a.y);
+          float *o = W.out[m] + p;
+          if (W.accumulate) v = __fadd_rn(*o, v);
+          __stcs(o, v);
+          __stcg(win + slot + m, make_float2(0.0f, 0.0f));
+          msum[m] += (double)v;
+        }
+      }
+      __threadfence();
+      __syncthreads();
+      if (threadIdx.x == 0) atomicAdd(&W.drain_done[band], 1u);
+    }
+    __syncthreads();
+  }
+  (void)nwarp;
+  __syncthreads();
+  for (int m = 0; m < P.nmaps; m++) {
+    double v = msum[m];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(FULL, v, o);
+    if ((threadIdx.x & 31) == 0 && v != 0.0) atomicAdd(&s_sum[m], v);
+  }
+  block_count(&W.ctr->hp_updates, nupd);
+  block_count(&W.ctr->n_recheck, nrc);
+  block_count(&W.ctr->n_cand, ncand);
+  __syncthreads();
+  if (threadIdx.x < P.nmaps && s_sum[threadIdx.x] != 0.0)
+    atomicAdd(W.sums + threadIdx.x, s_sum[threadIdx.x]);
+}
+
+/* plain FP64 path: every candidate through the exact path into a full-sky accumulator */
+__global__ void __launch_bounds__(256) k_paint_full(PaintParams P, SweepBuffers W) {
+  const long long npix_c = (long long)W.ctr->n_pix;
+  if (npix_c == 0) return;
+  const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+  const long long chunk = 1024;
+  unsigned long long nupd = 0, nrc = 0, ncand = 0;
+  for (long long c = warp; c * chunk < npix_c; c += nwarps) {
+    long long p0 = c * chunk, p1 = min(npix_c, p0 + chunk);
+    walk_candidates<0>(P, W, p0, p1, 0, W.n_items, W.acc, 0, nupd, nrc);
+    if ((threadIdx.x & 31) == 0) ncand += (unsigned long long)(p1 - p0);
+  }
+  warp_count(&W.ctr->hp_updates, nupd);
+  warp_count(&W.ctr->n_cand, ncand);
+}
+
+/* full-sky FP64 accumulator -> float maps (one pass over all maps) and map sums */
+__global__ void __launch_bounds__(256) k_finalize_full(const double *acc, long long npix, int nmaps,
+                                                       float *o0, float *o1, float *o2, float *o3,
+                                                       float *o4, float *o5, float *o6, float *o7,
+                                                       int accumulate, double *sums) {
+  float *outs[8] = {o0, o1, o2, o3, o4, o5, o6, o7};
+  double s[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < npix;
+       p += (long long)gridDim.x * blockDim.x) {
+    for (int m = 0; m < nmaps; m++) {
+      float v = (float)__ldcs(acc + p * nmaps + m);
+      if (accumulate) v = __fadd_rn(outs[m][p], v);
+      __stcs(outs[m] + p, v);
+      s[m] += (double)v;
+    }
+  }
+  for (int m = 0; m < nmaps; m++) {
+    double v = s[m];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(FULL, v, o);
+    if ((threadIdx.x & 31) == 0 && v != 0.0) atomicAdd(sums + m, v);
+  }
+}
+
+/* flat-sky accumulator -> float map */
+template <int PREC>
+__global__ void __launch_bounds__(256) k_finalize_fs(const void *acc, long long npix, int nmaps, int map,
+                                                     float *out, double *sum) {
   double s = 0.0;
-  for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < npix; p += stride) {
+  for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < npix;
+       p += (long long)gridDim.x * blockDim.x) {
     float v;
     if (PREC == 0) {
-      v = (float)__ldcs((const double *)acc + p * nmaps + map);
+      v = (float)((const double *)acc)[p * nmaps + map];
     } else {
-      float2 a = __ldcs((const float2 *)acc + p * nmaps + map);
+      float2 a = ((const float2 *)acc)[p * nmaps + map];
       v = __fadd_rn(a.x, a.y);
     }
-    __stcs(out + p, v);
+    out[p] = v;
     s += (double)v;
   }
-  __shared__ double red[8];
   for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(FULL, s, o);
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double t = 0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += red[w];
-    if (sum) atomicAdd(sum, t);
-  }
+  if ((threadIdx.x & 31) == 0 && s != 0.0 && sum) atomicAdd(sum, s);
 }
 
 /* -------------------------------------------------------------- table maker ----- */
@@ -960,52 +1181,74 @@ static inline int grid_for(long long n, int block, int nsm, int per_sm) {
   return (int)g;
 }
 
-void p2m_launch_cut(const PaintParams &P, const PaintBuffers &B, long long n, cudaStream_t s,
+void p2m_launch_cut(const PaintParams &P, const IngestBuffers &B, long long n, cudaStream_t s,
                     int nsm) {
-  k_cut<<<grid_for(n, 256, nsm, 8), 256, 0, s>>>(P, B, n);
+  k_cut<<<grid_for((n + CUT_PER_THREAD - 1) / CUT_PER_THREAD, 256, nsm, 8), 256, 0, s>>>(P, B, n);
 }
-void p2m_launch_setup(const PaintParams &P, const PaintBuffers &B, long long n_max,
+void p2m_launch_setup(const PaintParams &P, const IngestBuffers &B, long long n_max,
                       cudaStream_t s, int nsm) {
-  k_setup<<<grid_for(n_max, 256, nsm, 4), 256, 0, s>>>(P, B);
+  k_setup<<<grid_for(n_max, 256, nsm, 8), 256, 0, s>>>(P, B);
 }
-void p2m_launch_prepared(const PaintParams &P, const PaintBuffers &B, const float *d_prep,
-                         long long n, cudaStream_t s, int nsm) {
-  k_setup_prepared<<<grid_for(n, 256, nsm, 4), 256, 0, s>>>(P, B, d_prep, n);
+void p2m_launch_setup_prepared(const PaintParams &P, const IngestBuffers &B, const float *prep,
+                               long long n, cudaStream_t s, int nsm) {
+  k_setup_prepared<<<grid_for(n, 256, nsm, 8), 256, 0, s>>>(P, B, prep, n);
 }
-void p2m_launch_ring_scan(const PaintParams &P, const PaintBuffers &B, cudaStream_t s) {
-  long long n = 4LL * P.nside; /* rings 0..4N-1 (slot 0 unused) */
-  k_scan_single<<<1, 1024, 0, s>>>(B.ring_hist, B.ring_start, n, &B.ctr->n_items);
+void p2m_launch_scan_u32(const unsigned int *in, const unsigned long long *n_ptr, long long *out,
+                         unsigned long long *total, long long *tmp, cudaStream_t s) {
+  k_scan_partial<<<SCAN_BLOCKS, 256, 0, s>>>(in, n_ptr, tmp);
+  k_scan_top<<<1, SCAN_BLOCKS, 0, s>>>(tmp, total);
+  k_scan_apply<<<SCAN_BLOCKS, 256, 0, s>>>(in, n_ptr, tmp, out);
 }
-void p2m_launch_emit(const PaintParams &P, const PaintBuffers &B, long long n_max,
-                     cudaStream_t s, int nsm) {
-  k_emit<<<grid_for(n_max, 256, nsm, 4), 256, 0, s>>>(P, B);
-}
-void p2m_launch_rings(const PaintParams &P, const PaintBuffers &B, long long n_max,
+void p2m_launch_items(const PaintParams &P, const IngestBuffers &B, long long n_max,
                       cudaStream_t s, int nsm) {
-  k_rings<<<grid_for(n_max, 256, nsm, 8), 256, 0, s>>>(P, B);
+  k_items<<<grid_for(n_max, 256, nsm, 8), 256, 0, s>>>(P, B);
 }
-void p2m_launch_count_scan(const PaintParams &P, const PaintBuffers &B, cudaStream_t s) {
-  (void)P;
-  k_scan_partial<<<SCAN_BLOCKS, 256, 0, s>>>(B.counts, &B.ctr->n_items, B.scan_tmp);
-  k_scan_top<<<1, SCAN_BLOCKS, 0, s>>>(B.scan_tmp, &B.ctr->n_pix);
-  k_scan_apply<<<SCAN_BLOCKS, 256, 0, s>>>(B.counts, &B.ctr->n_items, B.scan_tmp, B.pix_off);
-}
-void p2m_launch_paint(const PaintParams &P, const PaintBuffers &B, cudaStream_t s, int nsm) {
-  if (P.precision == 0) k_paint<0><<<nsm * 8, 256, 0, s>>>(P, B);
-  else k_paint<1><<<nsm * 8, 256, 0, s>>>(P, B);
-}
-void p2m_launch_recheck(const PaintParams &P, const PaintBuffers &B, cudaStream_t s, int nsm) {
-  k_recheck<<<nsm * 2, 256, 0, s>>>(P, B);
-}
-void p2m_launch_paint_fs(const PaintParams &P, const PaintBuffers &B, cudaStream_t s, int nsm) {
+void p2m_launch_fs(const PaintParams &P, const IngestBuffers &B, long long n_max, cudaStream_t s,
+                   int nsm) {
+  k_fs_emit<<<grid_for(n_max, 256, nsm, 4), 256, 0, s>>>(P, B);
   if (P.precision == 0) k_paint_fs<0><<<nsm * 8, 256, 0, s>>>(P, B);
   else k_paint_fs<1><<<nsm * 8, 256, 0, s>>>(P, B);
 }
-void p2m_launch_finalize(const PaintParams &P, const void *acc, long long npix, int map,
-                         float *out, double *sum, cudaStream_t s, int nsm) {
+void p2m_launch_band_scatter(const PaintParams &P, const RingItem *in, long long n,
+                             const long long *band_start, unsigned int *band_cursor,
+                             RingItem *out, unsigned int *counts, cudaStream_t s, int nsm) {
+  k_band_scatter<<<grid_for(n, 256, nsm, 8), 256, 0, s>>>(P, in, n, band_start, band_cursor, out,
+                                                          counts);
+}
+void p2m_launch_scan_single(const unsigned int *in, long long *out, long long n,
+                            unsigned long long *total, cudaStream_t s) {
+  k_scan_single<<<1, 1024, 0, s>>>(in, out, n, total);
+}
+void p2m_launch_units(const SweepBuffers &W, long long *band_item0, long long *band_cand0,
+                      int *seg_start, int *seg_code, int *unit_target, const long long *band_pix0,
+                      unsigned long long *n_pix, cudaStream_t s) {
+  k_units<<<1, 32, 0, s>>>(W, band_item0, band_cand0, seg_start, seg_code, unit_target, band_pix0,
+                           n_pix);
+}
+void p2m_launch_sweep(const PaintParams &P, const SweepBuffers &W, cudaStream_t s, int nsm) {
+  /* one resident wave: every block claims units until the queue is empty */
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sweep, P2M_SWEEP_THREADS, 0) !=
+          cudaSuccess ||
+      per_sm < 1)
+    per_sm = 1;
+  k_sweep<<<nsm * per_sm, P2M_SWEEP_THREADS, 0, s>>>(P, W);
+}
+void p2m_launch_paint_full(const PaintParams &P, const SweepBuffers &W, cudaStream_t s, int nsm) {
+  k_paint_full<<<nsm * 8, 256, 0, s>>>(P, W);
+}
+void p2m_launch_finalize_full(const PaintParams &P, const void *acc, long long npix,
+                              float *const *out, int accumulate, double *sums, cudaStream_t s,
+                              int nsm) {
+  k_finalize_full<<<grid_for(npix, 256, nsm, 8), 256, 0, s>>>(
+      (const double *)acc, npix, P.nmaps, out[0], out[1], out[2], out[3], out[4], out[5], out[6],
+      out[7], accumulate, sums);
+}
+void p2m_launch_finalize_fs(const PaintParams &P, const void *acc, long long npix, float *out,
+                            int map, double *sum, cudaStream_t s, int nsm) {
   int g = grid_for(npix, 256, nsm, 8);
-  if (P.precision == 0) k_finalize<0><<<g, 256, 0, s>>>(acc, npix, P.nmaps, map, out, sum);
-  else k_finalize<1><<<g, 256, 0, s>>>(acc, npix, P.nmaps, map, out, sum);
+  if (P.precision == 0) k_finalize_fs<0><<<g, 256, 0, s>>>(acc, npix, P.nmaps, map, out, sum);
+  else k_finalize_fs<1><<<g, 256, 0, s>>>(acc, npix, P.nmaps, map, out, sum);
 }
 void p2m_launch_maptable(const PaintParams &P, const TableConsts &K, const p2m_tabhdr &th,
                          float *d_table, cudaStream_t s) {

@@ -217,3 +217,50 @@ def test_maptable_gpu_matches_oracle():
     scale = np.abs(r).max(axis=2, keepdims=True) + 1e-300
     assert (np.abs(g - r) / scale).max() <= 1e-6
     assert np.mean(g == r) > 0.99
+
+
+def test_fast_path_decisions_match_exact_path():
+    """Every disc decision and table index the mixed-precision fast path takes on its own
+    agrees with the exact FP64 path (the recheck bands are wide enough)."""
+    rec = catalogs.shell(12, 300_000, r=(100.0, 8000.0), m=(1e12, 3e15))
+    tab = catalogs.table(nu=0.0, nchit=40, nmht=40, nrt=200)
+    with p2m.Painter(nside=2048, precision="mixed", maps=((0, 1), (0, 2)), zmax=6.0,
+                     flags=p2m.FLAG_VALIDATE, max_records=len(rec)) as pt:
+        pt.load_table(0, tab)
+        pt.paint_records(rec)
+        pt.flush()
+        st = pt.stats()
+    assert st["val_checked"] == st["hp_candidates"] > 1_000_000
+    assert st["val_bad_set"] == 0
+    assert st["val_bad_index"] == 0
+    assert st["val_max_du"] < 0.2 * 2e-4  # observed error well inside the band half-width
+    assert st["n_recheck"] < 2e-3 * st["hp_candidates"]
+
+
+def test_readout_then_more_painting_accumulates():
+    rec = catalogs.shell(13, 40_000)
+    tab = catalogs.table()
+    whole, _, _, _ = run_gpu(rec, [tab], "mixed", 256, flags=0)
+    with p2m.Painter(nside=256, precision="mixed", max_records=len(rec)) as pt:
+        pt.load_table(0, tab)
+        pt.paint_records(rec[:15_000])
+        first = pt.healpix(0)
+        pt.paint_records(rec[15_000:])
+        both = pt.healpix(0)
+    assert np.abs(first).max() > 0
+    assert_maps_close(both, whole[0], rel=1e-6)
+
+
+def test_bound_device_output():
+    import torch
+    rec = catalogs.shell(14, 20_000)
+    tab = catalogs.table()
+    ref, _, _, _ = run_gpu(rec, [tab], "mixed", 128, flags=0)
+    out = torch.zeros(12 * 128 * 128, dtype=torch.float32, device="cuda")
+    with p2m.Painter(nside=128, precision="mixed", max_records=len(rec)) as pt:
+        pt.load_table(0, tab)
+        pt.bind_healpix_device(0, out.data_ptr())
+        pt.paint_records(rec)
+        pt.healpix_device(0, out.data_ptr())
+        pt.synchronize()
+    assert_maps_close(out.cpu().numpy(), ref[0], rel=1e-6)
