@@ -43,9 +43,11 @@ enum {
 enum {
   P2M_PREC_FP64 = 0,  /* plain drop-in: FP64 pixel geometry (pix2vec_ring + angdist) for
                          every candidate, FP64 accumulation */
-  P2M_PREC_MIXED = 1  /* FP32 disc test and profile interpolation with an exact FP64
+  P2M_PREC_MIXED = 1, /* FP32 disc test and profile interpolation with an exact FP64
                          recheck near every decision boundary; compensated two-float
-                         FP32 accumulation */
+                         FP32 accumulation in L2-resident band windows */
+  P2M_PREC_MIXED_F64 = 2 /* the same decisions; FP64 accumulation (atomic adds executed in
+                            L2, not on the SM's FP64 units) */
 };
 
 /* catalogue layouts (floats per record): 7 = x,y,z,vx,vy,vz,RTH after a 2-word header

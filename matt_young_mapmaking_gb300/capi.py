@@ -16,7 +16,7 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "libp2m_gb300.so")
 
 MAXMAPS = 8
-PREC_FP64, PREC_MIXED = 0, 1
+PREC_FP64, PREC_MIXED, PREC_MIXED_F64 = 0, 1, 2
 FLAG_RECORD_SETS, FLAG_ALL_HALOS, FLAG_TIMING, FLAG_VALIDATE = 1, 2, 4, 8
 STATUS = {0: "OK", 1: "BADARG", 2: "CUDA", 3: "CAPACITY", 4: "TIMEOUT", 5: "IO", 6: "STATE",
           7: "NOMEM"}
@@ -105,6 +105,7 @@ def load_library():
         "p2m_philox4x32": (None, [VP, VP, VP]),
         "p2m_fmath_eval_device": (I32, [I32, I32, VP, VP, VP, I64]),
         "p2m_get_timings": (I32, [VP, VP, I32]),
+        "p2m_get_diagnostics": (I32, [VP, VP, I32]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -122,7 +123,7 @@ def exported_symbols():
             "p2m_bind_healpix_device", "p2m_get_stats",
             "p2m_synchronize", "p2m_get_pixel_sets", "p2m_make_maptable",
             "p2m_generate_catalogue", "p2m_philox4x32", "p2m_fmath_eval_device",
-            "p2m_get_timings"]
+            "p2m_get_timings", "p2m_get_diagnostics"]
 
 
 PHASES = ["cut", "setup", "item_scan", "items", "flatsky", "group", "paint", "readout"]
@@ -147,7 +148,8 @@ class Painter:
         cfg.nside, cfg.npix_fs, cfg.fov_deg = nside, npix_fs, fov_deg
         cfg.zmin, cfg.zmax, cfg.chihview, cfg.model = zmin, zmax, chihview, model
         if isinstance(precision, str):
-            precision = {"fp64": PREC_FP64, "mixed": PREC_MIXED}[precision]
+            precision = {"fp64": PREC_FP64, "mixed": PREC_MIXED,
+                         "mixed64": PREC_MIXED_F64}[precision]
         cfg.precision = precision
         maps = list(maps)
         if not 1 <= len(maps) <= MAXMAPS:
@@ -265,6 +267,14 @@ class Painter:
         ms = np.zeros(len(PHASES))
         self._check(self._lib.p2m_get_timings(self._h, _ptr(ms), len(PHASES)))
         return dict(zip(PHASES, ms.tolist()))
+
+    def diagnostics(self):
+        """Sweep counters since the last reset (waits, unit cycles, bands, window size)."""
+        v = np.zeros(7, dtype=np.int64)
+        self._check(self._lib.p2m_get_diagnostics(self._h, _ptr(v), 7))
+        keys = ("wait_polls", "paint_cycles", "drain_cycles", "paint_units", "drain_units",
+                "bands", "window_pixels")
+        return dict(zip(keys, v.tolist()))
 
     def pixel_sets(self):
         n = ctypes.c_int64()

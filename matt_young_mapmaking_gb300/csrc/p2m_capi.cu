@@ -22,7 +22,7 @@
 enum { PH_CUT, PH_SETUP, PH_SCAN, PH_ITEMS, PH_FS, PH_GROUP, PH_PAINT, PH_READOUT, P2M_NPHASE };
 
 /* L2 budget of one window (two windows alternate) */
-#define P2M_WINDOW_BYTES (40LL << 20)
+#define P2M_WINDOW_BYTES (20LL << 20)
 
 struct p2m_ctx {
   p2m_config cfg;
@@ -47,7 +47,13 @@ struct p2m_ctx {
   long long hp_npix = 0, fs_npix = 0;
   float *d_out_own[P2M_MAXMAPS] = {};
   float *d_out[P2M_MAXMAPS] = {};
-  double *d_acc64 = nullptr; /* plain FP64 path */
+  double *d_acc64 = nullptr; /* full-sky FP64 accumulator (plain and FP64-accumulating paths) */
+  bool window_sweep = false; /* mixed precision: band windows instead of the full sky */
+  /* compensated path: the output maps accumulate the high words; low words and their
+     dirty-tile flags stay zero between sweeps */
+  float *d_lo = nullptr;
+  unsigned char *d_tiles = nullptr;
+  bool outs_zeroed = false;
   void *d_fs_acc = nullptr;
   float *d_fs_out = nullptr;
   /* ingest state (accumulated until the next sweep) */
@@ -80,6 +86,9 @@ struct p2m_ctx {
   long long *d_band_item0 = nullptr, *d_band_cand0 = nullptr;
   unsigned int *d_band_cursor = nullptr, *d_paint_done = nullptr, *d_drain_done = nullptr;
   int *d_seg_start = nullptr, *d_seg_code = nullptr, *d_unit_target = nullptr;
+  int *d_band_chunk0 = nullptr;
+  long long *d_chunk_g0 = nullptr;
+  long long cap_chunks = 0; /* sized from the previous sweep; larger sweeps search instead */
   unsigned long long *d_nitems = nullptr;
   double *d_sums = nullptr; /* [0, MAXMAPS): HEALPix, [MAXMAPS, 2 MAXMAPS): flat sky */
   long long *d_set_rec = nullptr, *d_set_pix = nullptr;
@@ -291,7 +300,20 @@ p2m_status ingest_tail(p2m_ctx *ctx, const PaintParams &P, long long n_max, cuda
   return P2M_OK;
 }
 
+bool compensated(const p2m_ctx *ctx) { return ctx->d_lo != nullptr; }
+
+/* the compensated path accumulates into the output maps: clear them before the first
+   paint after a reset (the buffers bound at that time) */
+p2m_status zero_outputs(p2m_ctx *ctx, cudaStream_t s) {
+  if (!compensated(ctx) || ctx->outs_zeroed) return P2M_OK;
+  for (int m = 0; m < ctx->cfg.nmaps; m++)
+    CK(cudaMemsetAsync(ctx->d_out[m], 0, sizeof(float) * (size_t)ctx->hp_npix, s));
+  ctx->outs_zeroed = true;
+  return P2M_OK;
+}
+
 p2m_status begin_call(p2m_ctx *ctx, long long n, cudaStream_t s) {
+  ST(zero_outputs(ctx, s));
   CK(grow(&ctx->d_surv, &ctx->cap_surv, std::max(n, 1LL)));
   CK(grow(&ctx->d_nring, &ctx->cap_nring, std::max(n, 1LL)));
   CK(grow(&ctx->d_ioff, &ctx->cap_ioff, std::max(n, 1LL)));
@@ -365,6 +387,10 @@ SweepBuffers sweep_buffers(const p2m_ctx *ctx) {
   W.seg_start = ctx->d_seg_start;
   W.seg_code = ctx->d_seg_code;
   W.unit_target = ctx->d_unit_target;
+  W.band_chunk0 = ctx->d_band_chunk0;
+  W.chunk_g0 = ctx->d_chunk_g0;
+  W.chunk_cap = ctx->cap_chunks;
+  W.n_chunks = &ctx->d_ctr->n_chunks;
   W.paint_done = ctx->d_paint_done;
   W.drain_done = ctx->d_drain_done;
   W.win = ctx->d_win;
@@ -372,6 +398,9 @@ SweepBuffers sweep_buffers(const p2m_ctx *ctx) {
   for (int m = 0; m < P2M_MAXMAPS; m++) W.out[m] = ctx->d_out[m];
   W.accumulate = ctx->swept ? 1 : 0;
   W.acc = ctx->d_acc64;
+  W.lo = ctx->d_lo;
+  W.tiles = ctx->d_tiles;
+  W.npix = ctx->hp_npix;
   W.sums = ctx->d_sums;
   W.ctr = ctx->d_ctr;
   W.set_rec = ctx->d_set_rec;
@@ -392,6 +421,7 @@ p2m_status sweep(p2m_ctx *ctx, cudaStream_t s) {
       for (int m = 0; m < ctx->cfg.nmaps; m++)
         CK(cudaMemsetAsync(ctx->d_out[m], 0, sizeof(float) * (size_t)ctx->hp_npix, s));
       ctx->swept = true;
+      ctx->outs_zeroed = true;
     }
     return P2M_OK;
   }
@@ -417,31 +447,50 @@ p2m_status sweep(p2m_ctx *ctx, cudaStream_t s) {
                       ctx->d_scan_tmp, s);
   SweepBuffers W = sweep_buffers(ctx);
   if (!ctx->swept) CK(cudaMemsetAsync(ctx->d_sums, 0, sizeof(double) * P2M_MAXMAPS, s));
-  if (ctx->cfg.precision == P2M_PREC_MIXED)
+  if (ctx->window_sweep)
     p2m_launch_units(W, ctx->d_band_item0, ctx->d_band_cand0, ctx->d_seg_start, ctx->d_seg_code,
-                     ctx->d_unit_target, ctx->d_band_pix0, &ctx->d_ctr->n_pix, s);
+                     ctx->d_unit_target, ctx->d_band_chunk0, ctx->d_chunk_g0, ctx->cap_chunks,
+                     ctx->d_band_pix0, &ctx->d_ctr->n_pix, s, ctx->nsm);
   TE(PH_GROUP);
   TB(PH_PAINT);
-  if (ctx->cfg.precision == P2M_PREC_MIXED) {
+  if (ctx->window_sweep) {
     p2m_launch_sweep(P, W, s, ctx->nsm);
     TE(PH_PAINT);
   } else {
     p2m_launch_paint_full(P, W, s, ctx->nsm);
     TE(PH_PAINT);
     TB(PH_READOUT);
-    p2m_launch_finalize_full(P, ctx->d_acc64, ctx->hp_npix, ctx->d_out, ctx->swept ? 1 : 0,
-                             ctx->d_sums, s, ctx->nsm);
+    if (compensated(ctx)) {
+      /* fold the sparse low words into the maps and clear them */
+      p2m_launch_fold_lo(P, W, s, ctx->nsm);
+    } else {
+      /* the read-out also clears the accumulator for the next paint */
+      p2m_launch_finalize_full(P, ctx->d_acc64, ctx->hp_npix, ctx->d_out, ctx->swept ? 1 : 0,
+                               ctx->d_sums, s, ctx->nsm);
+    }
     TE(PH_READOUT);
-    CK(cudaMemsetAsync(ctx->d_acc64, 0, sizeof(double) * (size_t)ctx->cfg.nmaps * (size_t)ctx->hp_npix, s));
   }
   CK(cudaGetLastError());
   p2m_status st = read_counters(ctx, s);
   join_out(ctx, s);
   if (st == P2M_ERR_TIMEOUT || st == P2M_ERR_STATE) {
-    /* windows may hold partial sums: clear them so the context stays usable */
-    cudaMemsetAsync(ctx->d_win, 0, sizeof(float2) * (size_t)(P2M_NBUF * ctx->wpix * ctx->cfg.nmaps), ctx->stream);
+    /* accumulators may hold partial sums: clear them so the context stays usable */
+    if (ctx->d_win)
+      cudaMemsetAsync(ctx->d_win, 0, sizeof(float2) * (size_t)(P2M_NBUF * ctx->wpix * ctx->cfg.nmaps),
+                      ctx->stream);
+    if (ctx->d_acc64)
+      cudaMemsetAsync(ctx->d_acc64, 0, sizeof(double) * (size_t)ctx->cfg.nmaps * (size_t)ctx->hp_npix,
+                      ctx->stream);
+    if (ctx->d_lo) {
+      cudaMemsetAsync(ctx->d_lo, 0, sizeof(float) * (size_t)ctx->cfg.nmaps * (size_t)ctx->hp_npix,
+                      ctx->stream);
+      cudaMemsetAsync(ctx->d_tiles, 0, (size_t)((ctx->hp_npix + 255) >> 8), ctx->stream);
+    }
   }
   if (st) return st;
+  /* warp-chunk start table sized for the next sweep of this size */
+  long long need_chunks = (long long)ctx->h_ctr->n_chunks;
+  if (need_chunks > ctx->cap_chunks) CK(grow(&ctx->d_chunk_g0, &ctx->cap_chunks, need_chunks));
   CK(cudaMemsetAsync(ctx->d_band_hist, 0, sizeof(unsigned) * (size_t)nb, s));
   ctx->n_items = 0;
   ctx->n_halos = 0;
@@ -453,7 +502,9 @@ p2m_status sweep(p2m_ctx *ctx, cudaStream_t s) {
 /* ring bands whose pixels fit one window */
 p2m_status build_bands(p2m_ctx *ctx) {
   const int N = ctx->cfg.nside, nr = 4 * N;
-  long long w = P2M_WINDOW_BYTES / (8LL * ctx->cfg.nmaps);
+  long long wbytes = P2M_WINDOW_BYTES;
+  if (const char *e = getenv("P2M_WINDOW_MB")) wbytes = (long long)(atof(e) * (1 << 20));
+  long long w = wbytes / (8LL * ctx->cfg.nmaps);
   w = std::max(w, 4LL * N); /* at least the widest ring */
   std::vector<int> bor((size_t)nr, 0);
   std::vector<long long> pix0;
@@ -494,7 +545,9 @@ p2m_status build_bands(p2m_ctx *ctx) {
   CK(cudaMalloc((void **)&ctx->d_seg_start, sizeof(int) * (2 * nb + 1)));
   CK(cudaMalloc((void **)&ctx->d_seg_code, sizeof(int) * 2 * nb));
   CK(cudaMalloc((void **)&ctx->d_unit_target, sizeof(int) * 2 * nb));
-  if (ctx->cfg.precision == P2M_PREC_MIXED) {
+  CK(cudaMalloc((void **)&ctx->d_band_chunk0, sizeof(int) * (nb + 1)));
+  CK(grow(&ctx->d_chunk_g0, &ctx->cap_chunks, 1LL << 16));
+  if (ctx->window_sweep) {
     size_t wb = sizeof(float2) * (size_t)(P2M_NBUF * ctx->wpix * ctx->cfg.nmaps);
     CK(cudaMalloc((void **)&ctx->d_win, wb));
     CK(cudaMemset(ctx->d_win, 0, wb));
@@ -514,7 +567,7 @@ p2m_status p2m_create(const p2m_config *cfg, p2m_ctx **out) {
   if (cfg->nside == 0 && cfg->npix_fs == 0) return P2M_ERR_BADARG;
   if (cfg->model < 1 || cfg->model > 3) return P2M_ERR_BADARG;
   if (cfg->nmaps < 1 || cfg->nmaps > P2M_MAXMAPS) return P2M_ERR_BADARG;
-  if (cfg->precision != P2M_PREC_FP64 && cfg->precision != P2M_PREC_MIXED) return P2M_ERR_BADARG;
+  if (cfg->precision < P2M_PREC_FP64 || cfg->precision > P2M_PREC_MIXED_F64) return P2M_ERR_BADARG;
   for (int m = 0; m < cfg->nmaps; m++) {
     if (cfg->map_table[m] < 0 || cfg->map_table[m] >= P2M_MAXTABLES) return P2M_ERR_BADARG;
     if (cfg->map_profile[m] != 1 && cfg->map_profile[m] != 2) return P2M_ERR_BADARG;
@@ -553,7 +606,18 @@ p2m_status p2m_create(const p2m_config *cfg, p2m_ctx **out) {
       CK(cudaMalloc((void **)&ctx->d_out_own[m], sizeof(float) * (size_t)ctx->hp_npix));
       ctx->d_out[m] = ctx->d_out_own[m];
     }
-    if (cfg->precision == P2M_PREC_FP64) {
+    if (cfg->precision != P2M_PREC_FP64) {
+      const char *e = getenv("P2M_ACCUM");
+      ctx->window_sweep = e && strcmp(e, "window") == 0;
+    }
+    if (!ctx->window_sweep && cfg->precision == P2M_PREC_MIXED) {
+      size_t lb = sizeof(float) * (size_t)cfg->nmaps * (size_t)ctx->hp_npix;
+      size_t tb = (size_t)((ctx->hp_npix + 255) >> 8);
+      CK(cudaMalloc((void **)&ctx->d_lo, lb));
+      CK(cudaMemset(ctx->d_lo, 0, lb));
+      CK(cudaMalloc((void **)&ctx->d_tiles, tb));
+      CK(cudaMemset(ctx->d_tiles, 0, tb));
+    } else if (!ctx->window_sweep) {
       size_t ab = sizeof(double) * (size_t)cfg->nmaps * (size_t)ctx->hp_npix;
       CK(cudaMalloc((void **)&ctx->d_acc64, ab));
       CK(cudaMemset(ctx->d_acc64, 0, ab));
@@ -596,8 +660,9 @@ void p2m_destroy(p2m_ctx *ctx) {
                   ctx->d_ioff, ctx->d_fs_items, ctx->d_scan_tmp, ctx->d_items, ctx->d_counts,
                   ctx->d_pix_off, ctx->d_band_item0, ctx->d_band_cand0, ctx->d_band_cursor,
                   ctx->d_paint_done, ctx->d_drain_done, ctx->d_seg_start, ctx->d_seg_code,
-                  ctx->d_unit_target, ctx->d_nitems, ctx->d_sums, ctx->d_set_rec, ctx->d_set_pix,
-                  ctx->d_ctr, ctx->d_prep};
+                  ctx->d_unit_target, ctx->d_band_chunk0, ctx->d_chunk_g0, ctx->d_nitems,
+                  ctx->d_sums, ctx->d_set_rec, ctx->d_set_pix,
+                  ctx->d_ctr, ctx->d_prep, ctx->d_lo, ctx->d_tiles};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   for (int m = 0; m < P2M_MAXMAPS; m++)
@@ -676,6 +741,7 @@ p2m_status p2m_reset_maps(p2m_ctx *ctx) {
   ctx->n_records = 0;
   ctx->dirty = false;
   ctx->swept = false;
+  ctx->outs_zeroed = false;
   if (ctx->d_band_hist) CK(cudaMemsetAsync(ctx->d_band_hist, 0, sizeof(unsigned) * (size_t)ctx->nbands, s));
   if (ctx->d_fs_acc)
     CK(cudaMemsetAsync(ctx->d_fs_acc, 0, 8 * (size_t)ctx->cfg.nmaps * (size_t)ctx->fs_npix, s));
@@ -738,6 +804,7 @@ p2m_status p2m_bind_healpix_device(p2m_ctx *ctx, int32_t map, float *d_out) {
   if (ctx->dirty || ctx->swept)
     return fail(ctx, P2M_ERR_STATE, "bind output buffers right after p2m_reset_maps");
   ctx->d_out[map] = d_out ? d_out : ctx->d_out_own[map];
+  ctx->outs_zeroed = false;
   return P2M_OK;
 }
 
@@ -791,6 +858,13 @@ p2m_status p2m_get_stats(p2m_ctx *ctx, p2m_stats *out) {
   if (!ctx || !out) return P2M_ERR_BADARG;
   CK(cudaSetDevice(ctx->cfg.device));
   ST(sweep(ctx, ctx->stream));
+  /* sums over the HEALPix maps as they now are */
+  if (ctx->cfg.nside > 0) {
+    CK(cudaMemsetAsync(ctx->d_sums, 0, sizeof(double) * P2M_MAXMAPS, ctx->stream));
+    for (int m = 0; m < ctx->cfg.nmaps; m++)
+      p2m_launch_map_sum(ctx->d_out[m], ctx->hp_npix, ctx->d_sums + m, ctx->stream, ctx->nsm);
+    CK(cudaGetLastError());
+  }
   CK(cudaStreamSynchronize(ctx->stream));
   DevCounters h;
   CK(cudaMemcpy(&h, ctx->d_ctr, sizeof(h), cudaMemcpyDeviceToHost));
@@ -859,6 +933,19 @@ int32_t p2m_get_timings(p2m_ctx *ctx, double *ms, int32_t n) {
       ms[k] = (double)t;
     }
   }
+  return P2M_OK;
+}
+
+int32_t p2m_get_diagnostics(p2m_ctx *ctx, int64_t *out, int32_t n) {
+  if (!ctx || !out) return P2M_ERR_BADARG;
+  CK(cudaSetDevice(ctx->cfg.device));
+  CK(cudaStreamSynchronize(ctx->stream));
+  DevCounters h;
+  CK(cudaMemcpy(&h, ctx->d_ctr, sizeof(h), cudaMemcpyDeviceToHost));
+  const int64_t v[7] = {(int64_t)h.sw_wait_polls, (int64_t)h.sw_paint_cycles,
+                        (int64_t)h.sw_drain_cycles, (int64_t)h.sw_paint_units,
+                        (int64_t)h.sw_drain_units, ctx->nbands, ctx->wpix};
+  for (int k = 0; k < n; k++) out[k] = k < 7 ? v[k] : 0;
   return P2M_OK;
 }
 

@@ -28,14 +28,18 @@
 
 #include "p2m_scalar.h"
 
-#define P2M_NBUF 2            /* windows alternating between bands */
-#define P2M_PAINT_UNIT 4096   /* candidates per paint unit (one block) */
-#define P2M_DRAIN_UNIT 32768  /* map pixels per drain unit (one block) */
+#define P2M_NBUF 4            /* windows in rotation between bands */
+#define P2M_LAG 2             /* a band is drained after the next P2M_LAG bands are queued */
 #define P2M_SWEEP_THREADS 256
+#ifndef P2M_SWEEP_MINBLOCKS
+#define P2M_SWEEP_MINBLOCKS 3 /* resident sweep blocks per SM the register budget allows */
+#endif
+#define P2M_WARP_CHUNK 512    /* candidates per paint unit (one warp) */
+#define P2M_DRAIN_UNIT 4096   /* map pixels per drain unit (one warp) */
 
 struct DevCounters {
   /* per call (cleared before every ingest call and every sweep) */
-  unsigned long long n_surv, n_items, n_pix, n_fs_items, n_fs_rows;
+  unsigned long long n_surv, n_items, n_pix, n_fs_items, n_fs_rows, n_chunks;
   unsigned int err, next_unit, abort, pad0;
   /* cumulative since the last reset */
   unsigned long long hp_updates, fs_updates, n_sets, n_recheck, n_shell, n_massive, n_enum,
@@ -43,6 +47,9 @@ struct DevCounters {
   unsigned long long val_checked, val_bad_set, val_bad_index;
   unsigned int val_max_du; /* float bits of the largest |u_fast - u_exact| */
   unsigned int pad1;
+  /* sweep diagnostics: polls spent waiting, SM cycles spent in paint / drain units */
+  unsigned long long sw_wait_polls, sw_paint_cycles, sw_drain_cycles, sw_paint_units,
+      sw_drain_units;
 };
 
 enum {
@@ -71,11 +78,20 @@ struct HaloRec {
 
 /* candidate span of one ring of one disc */
 struct RingItem {
-  int halo, ring, lo, count; /* lo: unwrapped phi index of the first candidate */
+  int halo;
+  int ring_n0;               /* ring << 16 | (n0 & 0xffff) */
+  int lo, count;             /* lo: unwrapped phi index of the first candidate */
   float A, B;                /* chord^2 = A + B sin^2(dphi/2) */
-  float x0;                  /* (lo + kshift/2) - phi0 npr / 2pi, in pixel units */
+  float f0;                  /* x0 = (lo + kshift/2) - phi0 npr / 2pi = n0 + f0 (pixel units):
+                                the k-th candidate sits at x = (n0 + k) + f0, exact integer
+                                part, so x keeps full relative precision near the centre */
   float hdphi;               /* pi / npr */
 };
+
+__host__ __device__ __forceinline__ int item_ring(const RingItem &it) { return it.ring_n0 >> 16; }
+__host__ __device__ __forceinline__ int item_n0(const RingItem &it) {
+  return (int)(short)(it.ring_n0 & 0xffff);
+}
 
 struct FsItem {
   int halo, k, jmin, count;
@@ -131,12 +147,19 @@ struct SweepBuffers {
   const int *seg_start;        /* [2*nbands+1] unit prefix of the segment sequence */
   const int *seg_code;         /* [2*nbands] band | (is_drain << 30) */
   const int *unit_target;      /* [2*nbands] units of P_b at b, of D_b at nbands + b */
+  const int *band_chunk0;      /* [nbands+1] first warp chunk of each band */
+  const long long *chunk_g0;   /* first item of each warp chunk (the first chunk_cap) */
+  long long chunk_cap;
+  unsigned long long *n_chunks;
   unsigned int *paint_done, *drain_done; /* [nbands] */
   float2 *win;                 /* P2M_NBUF windows of wpix * nmaps (hi, lo) */
   long long wpix;
   float *out[P2M_MAXMAPS];     /* float output maps */
   int accumulate;              /* add to the output maps instead of overwriting */
-  void *acc;                   /* plain path: full-sky FP64 accumulator */
+  void *acc;                   /* full-sky accumulator (plain FP64 and FP64-accumulating paths) */
+  float *lo;                   /* compensated path: low words, map m at lo + m * npix */
+  unsigned char *tiles;        /* compensated path: 1 per 256-pixel tile with a nonzero low word */
+  long long npix;
   double *sums;                /* [nmaps] sum over each output map */
   DevCounters *ctr;
   long long *set_rec, *set_pix;
@@ -162,8 +185,9 @@ void p2m_launch_band_scatter(const PaintParams &P, const RingItem *in, long long
 void p2m_launch_scan_single(const unsigned int *in, long long *out, long long n,
                             unsigned long long *total, cudaStream_t s);
 void p2m_launch_units(const SweepBuffers &W, long long *band_item0, long long *band_cand0,
-                      int *seg_start, int *seg_code, int *unit_target, const long long *band_pix0,
-                      unsigned long long *n_pix, cudaStream_t s);
+                      int *seg_start, int *seg_code, int *unit_target, int *band_chunk0,
+                      long long *chunk_g0, long long chunk_cap, const long long *band_pix0,
+                      unsigned long long *n_pix, cudaStream_t s, int nsm);
 void p2m_launch_sweep(const PaintParams &P, const SweepBuffers &W, cudaStream_t s, int nsm);
 void p2m_launch_paint_full(const PaintParams &P, const SweepBuffers &W, cudaStream_t s, int nsm);
 void p2m_launch_finalize_full(const PaintParams &P, const void *acc, long long npix,
@@ -171,6 +195,8 @@ void p2m_launch_finalize_full(const PaintParams &P, const void *acc, long long n
                               int nsm);
 void p2m_launch_finalize_fs(const PaintParams &P, const void *acc, long long npix, float *out,
                             int map, double *sum, cudaStream_t s, int nsm);
+void p2m_launch_fold_lo(const PaintParams &P, const SweepBuffers &W, cudaStream_t s, int nsm);
+void p2m_launch_map_sum(const float *map, long long n, double *sum, cudaStream_t s, int nsm);
 struct TableConsts {
   float y0, tau0, x0const, nu, alpha;
   int model;

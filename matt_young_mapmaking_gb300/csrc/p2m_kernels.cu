@@ -443,13 +443,15 @@ __device__ __forceinline__ RingItem make_item(const PaintParams &P, const HaloRe
       cnt = npr;
     }
   }
+  double x0 = ((double)lo + sh) - q;
+  double n0 = rint(x0); /* |n0| <= npr/2 + 1 <= 16385: fits 16 bits */
   it.halo = h;
-  it.ring = ring;
+  it.ring_n0 = (ring << 16) | ((int)n0 & 0xffff);
   it.lo = lo;
   it.count = cnt;
   it.A = A;
   it.B = Bc;
-  it.x0 = (float)(((double)lo + sh) - q);
+  it.f0 = (float)(x0 - n0);
   it.hdphi = 3.14159265358979f / (float)npr;
   return it;
 }
@@ -517,31 +519,47 @@ __global__ void __launch_bounds__(256) k_fs_emit(PaintParams P, IngestBuffers B)
   }
 }
 
-template <int PREC>
-__device__ __forceinline__ void deposit(void *acc, long long idx, float v) {
-  if (PREC == 0) {
-    atomicAdd((double *)acc + idx, (double)v);
-  } else {
-    float *a = (float *)acc + 2 * idx;
-    float old = atomicAdd(a, v);
-    /* TwoSum: the exact rounding error of old + v, carried in the low word */
-    float s = __fadd_rn(old, v);
-    float bb = __fsub_rn(s, old);
-    float err = __fadd_rn(__fsub_rn(old, __fsub_rn(s, bb)), __fsub_rn(v, bb));
-    if (err != 0.0f) atomicAdd(a + 1, err);
-  }
+/* the halo fields one candidate pixel needs */
+struct HotHalo {
+  float C_in, C_out, chi_t, fc, fm, w1, w2;
+  int zero, ichi, imh;
+  int cb[4];
+};
+
+__device__ __forceinline__ HotHalo hot_of(const HaloRec &H) {
+  HotHalo h;
+  h.C_in = H.C_in;
+  h.C_out = H.C_out;
+  h.chi_t = H.chi_t;
+  h.fc = H.fc;
+  h.fm = H.fm;
+  h.w1 = H.w1;
+  h.w2 = H.w2;
+  h.zero = H.zero;
+  h.ichi = H.ichi;
+  h.imh = H.imh;
+  for (int c = 0; c < 4; c++) h.cb[c] = H.cbase[c];
+  return h;
 }
 
 /* profile values of every map at one pixel (maptable.f90:204-212 with known ir, fr),
-   deposited at slot `slot` of acc (nmaps entries per slot) */
-template <int PREC>
-__device__ __forceinline__ void deposit_maps(const PaintParams &P, const HaloRec &H, void *acc,
-                                             long long slot, int ir, float fr) {
+   deposited at slot `slot` of acc (nmaps entries per slot).  ACC 0: FP64 accumulator
+   (fire-and-forget red.add.f64); ACC 1: two-float (hi, lo) FP32 accumulator, hi by an
+   atomic add that returns the old value, lo the exact TwoSum rounding error.  All maps'
+   adds are issued before any result is used. */
+template <int ACC>
+__device__ __forceinline__ void deposit_maps(const PaintParams &P, const HotHalo &H, void *acc,
+                                             long long slot, int ir, float fr,
+                                             const SweepBuffers *W = nullptr) {
   float ofr = FSUB(1.0f, fr), ofc = FSUB(1.0f, H.fc), ofm = FSUB(1.0f, H.fm);
   float fc = H.fc, fm = H.fm;
-  bool fast = H.cbase[0] >= 0 && H.cbase[1] >= 0 && H.cbase[2] >= 0 && H.cbase[3] >= 0 &&
+  bool fast = H.cb[0] >= 0 && H.cb[1] >= 0 && H.cb[2] >= 0 && H.cb[3] >= 0 &&
               ir >= 1 && ir < P.th.nrt;
-  for (int m = 0; m < P.nmaps; m++) {
+  float vals[P2M_MAXMAPS];
+#pragma unroll
+  for (int m = 0; m < P2M_MAXMAPS; m++) {
+    vals[m] = 0.0f;
+    if (m >= P.nmaps) continue;
     int prof = P.map_profile[m];
     float w = prof == 2 ? H.w2 : H.w1;
     if (w == 0.0f) continue;
@@ -549,10 +567,10 @@ __device__ __forceinline__ void deposit_maps(const PaintParams &P, const HaloRec
     float v;
     if (fast) {
       int rofs = 2 * (ir - 1) + (prof - 1);
-      float t00a = __ldg(tab + H.cbase[0] + rofs), t00b = __ldg(tab + H.cbase[0] + rofs + 2);
-      float t10a = __ldg(tab + H.cbase[1] + rofs), t10b = __ldg(tab + H.cbase[1] + rofs + 2);
-      float t01a = __ldg(tab + H.cbase[2] + rofs), t01b = __ldg(tab + H.cbase[2] + rofs + 2);
-      float t11a = __ldg(tab + H.cbase[3] + rofs), t11b = __ldg(tab + H.cbase[3] + rofs + 2);
+      float t00a = __ldg(tab + H.cb[0] + rofs), t00b = __ldg(tab + H.cb[0] + rofs + 2);
+      float t10a = __ldg(tab + H.cb[1] + rofs), t10b = __ldg(tab + H.cb[1] + rofs + 2);
+      float t01a = __ldg(tab + H.cb[2] + rofs), t01b = __ldg(tab + H.cb[2] + rofs + 2);
+      float t11a = __ldg(tab + H.cb[3] + rofs), t11b = __ldg(tab + H.cb[3] + rofs + 2);
       v = 0.0f;
       v = FADD(v, FMUL(FMUL(FMUL(t00a, ofr), ofc), ofm));
       v = FADD(v, FMUL(FMUL(FMUL(t00b, fr), ofc), ofm));
@@ -563,10 +581,59 @@ __device__ __forceinline__ void deposit_maps(const PaintParams &P, const HaloRec
       v = FADD(v, FMUL(FMUL(FMUL(t11a, ofr), fc), fm));
       v = FADD(v, FMUL(FMUL(FMUL(t11b, fr), fc), fm));
     } else {
-      p2m_hinterp hi = halo_hinterp(H);
+      p2m_hinterp hi;
+      hi.chi_t = H.chi_t;
+      hi.fc = H.fc;
+      hi.fm = H.fm;
+      hi.ichi = H.ichi;
+      hi.imh = H.imh;
+      hi.zero = H.zero;
       v = p2m_blend8(tab, &P.th, &hi, prof, ir, fr);
     }
-    deposit<PREC>(acc, slot * P.nmaps + m, FMUL(w, v));
+    vals[m] = FMUL(w, v);
+  }
+  if (ACC == 0) {
+    double *a = (double *)acc + slot * P.nmaps;
+#pragma unroll
+    for (int m = 0; m < P2M_MAXMAPS; m++)
+      if (m < P.nmaps && vals[m] != 0.0f) atomicAdd(a + m, (double)vals[m]);
+  } else if (ACC == 2) {
+    /* compensated accumulation with the output map as the high word; low words are
+       sparse (nonzero only where an add rounded) and their tiles are flagged */
+    float olds[P2M_MAXMAPS];
+#pragma unroll
+    for (int m = 0; m < P2M_MAXMAPS; m++)
+      olds[m] = (m < P.nmaps && vals[m] != 0.0f) ? atomicAdd(W->out[m] + slot, vals[m]) : 0.0f;
+    bool any = false;
+#pragma unroll
+    for (int m = 0; m < P2M_MAXMAPS; m++) {
+      if (m >= P.nmaps || vals[m] == 0.0f) continue;
+      float old = olds[m], v = vals[m];
+      float sm = __fadd_rn(old, v);
+      float bb = __fsub_rn(sm, old);
+      float err = __fadd_rn(__fsub_rn(old, __fsub_rn(sm, bb)), __fsub_rn(v, bb));
+      if (err != 0.0f) {
+        atomicAdd(W->lo + (long long)m * W->npix + slot, err);
+        any = true;
+      }
+    }
+    if (any) W->tiles[slot >> 8] = 1;
+  } else {
+    float *a = (float *)acc + 2 * slot * P.nmaps;
+    float olds[P2M_MAXMAPS];
+#pragma unroll
+    for (int m = 0; m < P2M_MAXMAPS; m++)
+      olds[m] = (m < P.nmaps && vals[m] != 0.0f) ? atomicAdd(a + 2 * m, vals[m]) : 0.0f;
+#pragma unroll
+    for (int m = 0; m < P2M_MAXMAPS; m++) {
+      if (m >= P.nmaps || vals[m] == 0.0f) continue;
+      float old = olds[m], v = vals[m];
+      /* TwoSum: the exact rounding error of old + v, carried in the low word */
+      float s = __fadd_rn(old, v);
+      float bb = __fsub_rn(s, old);
+      float err = __fadd_rn(__fsub_rn(old, __fsub_rn(s, bb)), __fsub_rn(v, bb));
+      if (err != 0.0f) atomicAdd(a + 2 * m + 1, err);
+    }
   }
 }
 
@@ -599,7 +666,7 @@ __global__ void __launch_bounds__(256) k_paint_fs(PaintParams P, IngestBuffers B
         float fr;
         p2m_rindex(&P.th, r, &ir, &fr);
         long long pix = (long long)(j - 1) + (long long)P.npix_fs * (f.k - 1);
-        deposit_maps<PREC>(P, H, B.fs_acc, pix, ir, fr);
+        deposit_maps<PREC>(P, hot_of(H), B.fs_acc, pix, ir, fr);
       }
     }
   }
@@ -621,7 +688,7 @@ __global__ void __launch_bounds__(256) k_band_scatter(PaintParams P, const RingI
     int band = -1 - lane; /* distinct keys for inactive lanes */
     if (act) {
       it = in[g];
-      band = P.band_of_ring[it.ring];
+      band = P.band_of_ring[item_ring(it)];
     }
     unsigned grp = __match_any_sync(FULL, band);
     int leader = __ffs(grp) - 1;
@@ -636,43 +703,77 @@ __global__ void __launch_bounds__(256) k_band_scatter(PaintParams P, const RingI
   }
 }
 
-/* unit queue of the sweep: segments P0, P1, D0, P2, D1, ..., P_{B-1}, D_{B-2}, D_{B-1}
-   (P_b: paint units of band b, D_b: drain units of band b) */
+/* unit queue of the sweep.  Segments: P_0 .. P_{L-1}, then P_b, D_{b-L} for b = L..B-1,
+   then D_{B-L} .. D_{B-1} (P_b: paint units of band b, D_b: drain units, L = P2M_LAG).
+   D_b waits for P_b; P_b waits for D_{b-NBUF}, which is queued L+... segments earlier
+   (L < NBUF), so every wait is on units claimed before it. */
 __global__ void k_units(SweepBuffers W, long long *band_item0, long long *band_cand0, int *seg_start,
-                        int *seg_code, int *unit_target, const long long *band_pix0,
-                        const unsigned long long *n_pix) {
+                        int *seg_code, int *unit_target, int *band_chunk0,
+                        const long long *band_pix0, const unsigned long long *n_pix,
+                        unsigned long long *n_chunks) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  int nb = W.nbands;
-  long long ni = W.n_items;
-  long long np = (long long)*n_pix;
+  const int nb = W.nbands;
+  const long long ni = W.n_items;
+  const long long np = (long long)*n_pix;
   for (int b = 0; b <= nb; b++) {
     long long i0 = band_item0[b];
     band_cand0[b] = (b == nb || i0 >= ni) ? np : W.pix_off[i0];
   }
+  int ch = 0;
   for (int b = 0; b < nb; b++) {
     long long c = band_cand0[b + 1] - band_cand0[b];
-    unit_target[b] = (int)((c + P2M_PAINT_UNIT - 1) / P2M_PAINT_UNIT);
+    band_chunk0[b] = ch;
+    int nck = (int)((c + P2M_WARP_CHUNK - 1) / P2M_WARP_CHUNK);
+    ch += nck;
+    unit_target[b] = nck;
     long long px = band_pix0[b + 1] - band_pix0[b];
     unit_target[nb + b] = (int)((px + P2M_DRAIN_UNIT - 1) / P2M_DRAIN_UNIT);
   }
+  band_chunk0[nb] = ch;
+  *n_chunks = (unsigned long long)ch;
   int k = 0, acc = 0;
-  for (int b = 0; b < nb; b++) {
-    seg_start[k] = acc;
-    seg_code[k] = b;
-    acc += unit_target[b];
-    k++;
-    if (b >= 1) {
+  for (int b = 0; b < nb + P2M_LAG; b++) {
+    if (b < nb) {
       seg_start[k] = acc;
-      seg_code[k] = (b - 1) | (1 << 30);
-      acc += unit_target[nb + b - 1];
+      seg_code[k] = b;
+      acc += unit_target[b];
+      k++;
+    }
+    int d = b - P2M_LAG;
+    if (d >= 0) {
+      seg_start[k] = acc;
+      seg_code[k] = d | (1 << 30);
+      acc += unit_target[nb + d];
       k++;
     }
   }
   seg_start[k] = acc;
-  seg_code[k] = (nb - 1) | (1 << 30);
-  acc += unit_target[nb + nb - 1];
-  k++;
-  seg_start[k] = acc;
+}
+
+/* first item of every warp chunk (P2M_WARP_CHUNK candidates of one band) */
+__global__ void __launch_bounds__(256) k_chunk_starts(SweepBuffers W, const long long *band_item0,
+                                                      const long long *band_cand0,
+                                                      const int *band_chunk0, long long *chunk_g0,
+                                                      long long cap) {
+  const long long n = min((long long)*W.n_chunks, cap);
+  const int nb = W.nbands;
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n;
+       t += (long long)gridDim.x * blockDim.x) {
+    int lo = 0, hi = nb; /* band: largest b with band_chunk0[b] <= t */
+    while (hi - lo > 1) {
+      int mid = (lo + hi) >> 1;
+      if (band_chunk0[mid] <= t) lo = mid;
+      else hi = mid;
+    }
+    long long c = band_cand0[lo] + (t - band_chunk0[lo]) * P2M_WARP_CHUNK;
+    long long a = band_item0[lo], b = band_item0[lo + 1]; /* largest g in [a, b) with off <= c */
+    while (b - a > 1) {
+      long long mid = (a + b) >> 1;
+      if (W.pix_off[mid] <= c) a = mid;
+      else b = mid;
+    }
+    chunk_g0[t] = a;
+  }
 }
 
 /* ---------------------------------------------------------- sweep: the painting ----- */
@@ -706,7 +807,7 @@ struct ExactRes {
 
 /* the reference's decision and interpolation inputs for one pixel: FP64 pixel centre
    and angular distance (haloproject.f90:63-70), float interpolation (maptable.f90) */
-__device__ ExactRes exact_eval(const PaintParams &P, const HaloRec &H, long long pix) {
+__device__ __noinline__ ExactRes exact_eval(const PaintParams &P, const HaloRec &H, long long pix) {
   ExactRes e;
   e.inside = false;
   e.zero = false;
@@ -745,9 +846,9 @@ __device__ __forceinline__ void record_set(long long *set_rec, long long *set_pi
 /* Fast mixed-precision decision for one candidate.  Returns 0 outside, 1 inside with
    (ir, fr) or zero value, 2 when the exact path must decide. */
 __device__ __forceinline__ int fast_decide(const PaintParams &P, const RingItem &it,
-                                           const HaloRec &H, int k, int &ir, float &fr,
+                                           const HotHalo &H, int k, int &ir, float &fr,
                                            bool &zero_val, float &u_out) {
-  float x = it.x0 + (float)k;
+  float x = (float)(item_n0(it) + k) + it.f0;
   float s = sinf(x * it.hdphi);
   float c2 = it.A + it.B * (s * s);
   if (c2 >= H.C_out) return 0;
@@ -782,52 +883,83 @@ __device__ __forceinline__ int fast_decide(const PaintParams &P, const RingItem 
   return 1;
 }
 
-/* one candidate pixel of the mixed path: deposit into `acc` at slot pix - pix0 */
-__device__ __forceinline__ void mixed_pixel(const PaintParams &P, const SweepBuffers &W,
-                                            const RingItem &it, const HaloRec &H, int k,
-                                            long long pix, void *acc, long long pix0,
-                                            unsigned long long &nupd, unsigned long long &nrc) {
+/* one item of a warp's 32-item window with its halo's hot fields (shared memory) */
+struct CacheEnt {
+  RingItem it;
+  HotHalo h;
+};
+
+/* one candidate pixel: decision (exact or mixed) and deposit into acc at slot pix - pix0 */
+template <int EXACT, int ACC>
+__device__ __forceinline__ void paint_pixel(const PaintParams &P, const SweepBuffers &W,
+                                            const CacheEnt &ce, int k, long long pix, void *acc,
+                                            long long pix0, unsigned long long &nupd,
+                                            unsigned long long &nrc) {
+  const HotHalo &H = ce.h;
   int ir = 0;
   float fr = 0.0f, u = 0.0f;
   bool zero_val = H.zero;
-  int d = fast_decide(P, it, H, k, ir, fr, zero_val, u);
-  if (P.flags & 8) { /* validation: compare every fast decision with the exact path */
-    ExactRes e = exact_eval(P, H, pix);
-    atomicAdd(&W.ctr->val_checked, 1ull);
-    if (d != 2) {
-      if ((d == 1) != e.inside) atomicAdd(&W.ctr->val_bad_set, 1ull);
-      else if (d == 1 && e.inside && !e.zero && !zero_val) {
-        if (e.ir != ir) atomicAdd(&W.ctr->val_bad_index, 1ull);
-        if (u >= 0.0f) atomicMax(&W.ctr->val_max_du, __float_as_uint(fabsf(u - e.u)));
+  int d;
+  if (EXACT) {
+    d = 2;
+  } else {
+    d = fast_decide(P, ce.it, H, k, ir, fr, zero_val, u);
+    if (P.flags & 8) { /* validation: compare every fast decision with the exact path */
+      ExactRes e = exact_eval(P, W.halos[ce.it.halo], pix);
+      atomicAdd(&W.ctr->val_checked, 1ull);
+      if (d != 2) {
+        if ((d == 1) != e.inside) atomicAdd(&W.ctr->val_bad_set, 1ull);
+        else if (d == 1 && e.inside && !e.zero && !zero_val) {
+          if (e.ir != ir) atomicAdd(&W.ctr->val_bad_index, 1ull);
+          if (u >= 0.0f) atomicMax(&W.ctr->val_max_du, __float_as_uint(fabsf(u - e.u)));
+        }
       }
     }
   }
   if (d == 0) return;
   if (d == 2) {
-    nrc++;
-    ExactRes e = exact_eval(P, H, pix);
+    if (!EXACT) nrc++;
+    ExactRes e = exact_eval(P, W.halos[ce.it.halo], pix);
     if (!e.inside) return;
     zero_val = e.zero;
     ir = e.ir;
     fr = e.fr;
   }
   nupd++;
-  if (P.flags & 1) record_set(W.set_rec, W.set_pix, W.set_cap, &W.ctr->n_sets, H.rec, pix);
-  if (!zero_val && !H.zero) deposit_maps<1>(P, H, acc, pix - pix0, ir, fr);
+  if (P.flags & 1)
+    record_set(W.set_rec, W.set_pix, W.set_cap, &W.ctr->n_sets, W.halos[ce.it.halo].rec, pix);
+  if (!zero_val && !H.zero) deposit_maps<ACC>(P, H, acc, pix - pix0, ir, fr, &W);
 }
 
-/* walk candidates [p0, p1) of items [ilo, ihi): one warp; PREC 0 deposits the exact
-   path into a full-sky FP64 accumulator, PREC 1 the mixed path into acc - pix0 */
-template <int PREC>
+/* loads items g0..g0+31 (below ihi) and their halos' hot fields into the warp's cache */
+__device__ __forceinline__ void fill_cache(const SweepBuffers &W, CacheEnt *cache, long long g0,
+                                           long long ihi) {
+  const int lane = threadIdx.x & 31;
+  __syncwarp();
+  long long g = g0 + lane;
+  if (g < ihi) {
+    RingItem it = W.items[g];
+    cache[lane].it = it;
+    cache[lane].h = hot_of(W.halos[it.halo]);
+  }
+  __syncwarp();
+}
+
+/* walk candidates [p0, p1) of items [ilo, ihi): one warp; EXACT 1 decides every candidate
+   by the exact path, EXACT 0 by the mixed-precision path; deposits go to acc at slot
+   pix - pix0.  The 32 items around the current candidates, with their halos' fields, sit
+   in the warp's shared-memory cache, loaded once per window. */
+template <int EXACT, int ACC>
 __device__ void walk_candidates(const PaintParams &P, const SweepBuffers &W, long long p0,
                                 long long p1, long long ilo, long long ihi, void *acc,
                                 long long pix0, unsigned long long &nupd,
-                                unsigned long long &nrc) {
+                                unsigned long long &nrc, long long g_start, CacheEnt *cache) {
   const int lane = threadIdx.x & 31;
   const long long *off = W.pix_off;
-  long long g0 = warp_upper(off, ilo, ihi, p0);
+  long long g0 = g_start >= 0 ? g_start : warp_upper(off, ilo, ihi, p0);
   long long woff = (g0 + lane < ihi) ? off[g0 + lane] : (1LL << 62);
   long long wend = (g0 + 32 < ihi) ? off[g0 + 32] : (1LL << 62);
+  fill_cache(W, cache, g0, ihi);
   for (long long base = p0; base < p1; base += 32) {
     long long p = base + lane;
     bool todo = p < p1;
@@ -846,6 +978,7 @@ __device__ void walk_candidates(const PaintParams &P, const SweepBuffers &W, lon
         else g0 += j0;
         woff = (g0 + lane < ihi) ? off[g0 + lane] : (1LL << 62);
         wend = (g0 + 32 < ihi) ? off[g0 + 32] : (1LL << 62);
+        fill_cache(W, cache, g0, ihi);
       }
       bool here = todo && p < wend;
       int j = 0;
@@ -857,36 +990,27 @@ __device__ void walk_candidates(const PaintParams &P, const SweepBuffers &W, lon
       long long ooff = __shfl_sync(FULL, woff, j);
       if (here) {
         todo = false;
-        const RingItem &it = W.items[g0 + j];
-        const HaloRec &H = W.halos[it.halo];
+        const CacheEnt &ce = cache[j];
         int k = (int)(p - ooff);
         int npr, kshift;
         long long npn;
-        p2m_ring_info(P.nside, it.ring, &npr, &kshift, &npn);
-        int iphi = it.lo + k;
+        p2m_ring_info(P.nside, item_ring(ce.it), &npr, &kshift, &npn);
+        int iphi = ce.it.lo + k;
         if (iphi < 0) iphi += npr;
         if (iphi >= npr) iphi -= npr;
-        long long pix = npn - npr + iphi;
-        if (PREC == 0) {
-          ExactRes e = exact_eval(P, H, pix);
-          if (e.inside) {
-            nupd++;
-            if (P.flags & 1) record_set(W.set_rec, W.set_pix, W.set_cap, &W.ctr->n_sets, H.rec, pix);
-            if (!e.zero) deposit_maps<0>(P, H, acc, pix, e.ir, e.fr);
-          }
-        } else {
-          RingItem itc = it;
-          mixed_pixel(P, W, itc, H, k, pix, acc, pix0, nupd, nrc);
-        }
+        paint_pixel<EXACT, ACC>(P, W, ce, k, npn - npr + iphi, acc, pix0, nupd, nrc);
       }
     }
   }
 }
 
-/* bounded wait for *flag >= target (thread 0 only); false on abort or timeout */
+/* bounded wait for *flag >= target (one lane); false on abort or timeout */
 __device__ bool wait_geq(const unsigned *flag, unsigned target, DevCounters *ctr) {
   for (long it = 0; it < (1L << 23); it++) {
-    if (ld_acquire(flag) >= target) return true;
+    if (ld_acquire(flag) >= target) {
+      if (it) atomicAdd(&ctr->sw_wait_polls, (unsigned long long)it);
+      return true;
+    }
     if (ld_acquire(&ctr->abort)) return false;
     __nanosleep(200);
   }
@@ -896,26 +1020,101 @@ __device__ bool wait_geq(const unsigned *flag, unsigned target, DevCounters *ctr
 }
 
 #define MAX_SEG 4096
+#define SWEEP_WARPS (P2M_SWEEP_THREADS / 32)
 
-/* persistent sweep: claims units in queue order (see k_units) */
-__global__ void __launch_bounds__(P2M_SWEEP_THREADS) k_sweep(PaintParams P, SweepBuffers W) {
+/* warp-reduced add of v into a shared-memory double */
+__device__ __forceinline__ void warp_sum_to(double *dst, double v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(FULL, v, o);
+  if ((threadIdx.x & 31) == 0 && v != 0.0) atomicAdd(dst, v);
+}
+
+/* one warp drains window slice [q0, q1): float maps out, window cleared, map sums into
+   s_sum; eight window loads in flight per lane */
+template <int ACC>
+__device__ __forceinline__ void drain_slice(const PaintParams &P, const SweepBuffers &W, float2 *win,
+                                            long long pix0, long long q0, long long q1,
+                                            double *s_sum) {
+  const int lane = threadIdx.x & 31;
+  if (P.nmaps == 2) {
+    double m0 = 0.0, m1 = 0.0;
+    float4 *w4 = (float4 *)win; /* (hi0, lo0, hi1, lo1) or (double0, double1) per pixel */
+    for (long long p = q0 + lane; p < q1; p += 8 * 32) {
+      float4 a[8];
+#pragma unroll
+      for (int u = 0; u < 8; u++)
+        if (p + u * 32 < q1) a[u] = __ldcg(w4 + (p + u * 32 - pix0));
+#pragma unroll
+      for (int u = 0; u < 8; u++) {
+        long long q = p + u * 32;
+        if (q >= q1) break;
+        float v0, v1;
+        if (ACC == 0) {
+          double2 d = *reinterpret_cast<double2 *>(&a[u]);
+          v0 = (float)d.x;
+          v1 = (float)d.y;
+        } else {
+          v0 = __fadd_rn(a[u].x, a[u].y);
+          v1 = __fadd_rn(a[u].z, a[u].w);
+        }
+        if (W.accumulate) {
+          v0 = __fadd_rn(W.out[0][q], v0);
+          v1 = __fadd_rn(W.out[1][q], v1);
+        }
+        __stcs(W.out[0] + q, v0);
+        __stcs(W.out[1] + q, v1);
+        __stcg(w4 + (q - pix0), make_float4(0.0f, 0.0f, 0.0f, 0.0f));
+        m0 += (double)v0;
+        m1 += (double)v1;
+      }
+    }
+    warp_sum_to(s_sum, m0);
+    warp_sum_to(s_sum + 1, m1);
+    return;
+  }
+  for (int m = 0; m < P.nmaps; m++) {
+    double ms = 0.0;
+    for (long long p = q0 + lane; p < q1; p += 32) {
+      long long e = (p - pix0) * P.nmaps + m;
+      float v;
+      if (ACC == 0) {
+        double *wd = (double *)win;
+        v = (float)__ldcg(wd + e);
+        __stcg(wd + e, 0.0);
+      } else {
+        float2 a = __ldcg(win + e);
+        v = __fadd_rn(a.x, a.y);
+        __stcg(win + e, make_float2(0.0f, 0.0f));
+      }
+      float *o = W.out[m] + p;
+      if (W.accumulate) v = __fadd_rn(*o, v);
+      __stcs(o, v);
+      ms += (double)v;
+    }
+    warp_sum_to(s_sum + m, ms);
+  }
+}
+
+/* persistent sweep: every warp claims units in queue order (see k_units), waits only for
+   the units its unit depends on, and signals its own completion; there are no block-wide
+   barriers inside the loop */
+template <int ACC>
+__global__ void __launch_bounds__(P2M_SWEEP_THREADS, P2M_SWEEP_MINBLOCKS) k_sweep(PaintParams P,
+                                                                                 SweepBuffers W) {
   __shared__ int s_seg[MAX_SEG + 1];
-  __shared__ int s_u, s_ok;
   __shared__ double s_sum[P2M_MAXMAPS];
+  __shared__ CacheEnt s_cache[SWEEP_WARPS][32];
   const int nseg = 2 * W.nbands;
   for (int k = threadIdx.x; k <= nseg; k += blockDim.x) s_seg[k] = W.seg_start[k];
   if (threadIdx.x < P2M_MAXMAPS) s_sum[threadIdx.x] = 0.0;
   __syncthreads();
   const int total = s_seg[nseg];
-  const int wid = threadIdx.x >> 5;
-  const int nwarp = blockDim.x >> 5;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  CacheEnt *cache = s_cache[wid];
   unsigned long long nupd = 0, nrc = 0, ncand = 0;
-  double msum[P2M_MAXMAPS];
-  for (int m = 0; m < P2M_MAXMAPS; m++) msum[m] = 0.0;
   for (;;) {
-    if (threadIdx.x == 0) s_u = ld_acquire(&W.ctr->abort) ? total : (int)atomicAdd(&W.ctr->next_unit, 1u);
-    __syncthreads();
-    const int u = s_u;
+    int u = 0;
+    if (lane == 0) u = ld_acquire(&W.ctr->abort) ? total : (int)atomicAdd(&W.ctr->next_unit, 1u);
+    u = __shfl_sync(FULL, u, 0);
     if (u >= total) break;
     int lo = 0, hi = nseg; /* largest seg with s_seg[seg] <= u */
     while (hi - lo > 1) {
@@ -929,57 +1128,45 @@ __global__ void __launch_bounds__(P2M_SWEEP_THREADS) k_sweep(PaintParams P, Swee
     const int k = u - s_seg[lo];
     float2 *win = W.win + (long long)(band % P2M_NBUF) * W.wpix * P.nmaps;
     const long long pix0 = W.band_pix0[band];
-    if (threadIdx.x == 0) {
-      bool ok = true;
+    int ok = 1;
+    if (lane == 0) {
       if (!drain && band >= P2M_NBUF)
-        ok = wait_geq(&W.drain_done[band - P2M_NBUF], (unsigned)W.unit_target[W.nbands + band - P2M_NBUF], W.ctr);
+        ok = wait_geq(&W.drain_done[band - P2M_NBUF],
+                      (unsigned)W.unit_target[W.nbands + band - P2M_NBUF], W.ctr);
       if (drain) ok = wait_geq(&W.paint_done[band], (unsigned)W.unit_target[band], W.ctr);
       __threadfence();
-      s_ok = ok;
     }
-    __syncthreads();
-    if (!s_ok) break;
+    ok = __shfl_sync(FULL, ok, 0);
+    if (!ok) break;
+    const long long t_unit = clock64();
     if (!drain) {
-      long long c0 = W.band_cand0[band] + (long long)k * P2M_PAINT_UNIT;
-      long long c1 = min(c0 + P2M_PAINT_UNIT, W.band_cand0[band + 1]);
-      const long long per = P2M_PAINT_UNIT / (P2M_SWEEP_THREADS / 32);
-      long long a = c0 + (long long)wid * per, b = min(a + per, c1);
-      if (a < b) {
-        walk_candidates<1>(P, W, a, b, W.band_item0[band], W.band_item0[band + 1], (void *)win, pix0,
-                           nupd, nrc);
-        if ((threadIdx.x & 31) == 0) ncand += (unsigned long long)(b - a);
-      }
+      const long long t = (long long)W.band_chunk0[band] + k;
+      long long a = W.band_cand0[band] + (long long)k * P2M_WARP_CHUNK;
+      long long b = min(a + P2M_WARP_CHUNK, W.band_cand0[band + 1]);
+      walk_candidates<0, ACC>(P, W, a, b, W.band_item0[band], W.band_item0[band + 1], (void *)win,
+                              pix0, nupd, nrc, t < W.chunk_cap ? W.chunk_g0[t] : -1, cache);
+      if (lane == 0) ncand += (unsigned long long)(b - a);
       __threadfence();
-      __syncthreads();
-      if (threadIdx.x == 0) atomicAdd(&W.paint_done[band], 1u);
+      __syncwarp();
+      if (lane == 0) {
+        atomicAdd(&W.paint_done[band], 1u);
+        atomicAdd(&W.ctr->sw_paint_cycles, (unsigned long long)(clock64() - t_unit));
+        atomicAdd(&W.ctr->sw_paint_units, 1ull);
+      }
     } else {
       long long q0 = pix0 + (long long)k * P2M_DRAIN_UNIT;
       long long q1 = min(q0 + P2M_DRAIN_UNIT, W.band_pix0[band + 1]);
-      for (long long p = q0 + threadIdx.x; p < q1; p += blockDim.x) {
-        long long slot = (p - pix0) * P.nmaps;
-        for (int m = 0; m < P.nmaps; m++) {
-          float2 a = __ldcg(win + slot + m);
-          float v = __fadd_rn(a.x, a.y);
-          float *o = W.out[m] + p;
-          if (W.accumulate) v = __fadd_rn(*o, v);
-          __stcs(o, v);
-          __stcg(win + slot + m, make_float2(0.0f, 0.0f));
-          msum[m] += (double)v;
-        }
-      }
+      drain_slice<ACC>(P, W, win, pix0, q0, q1, s_sum);
       __threadfence();
-      __syncthreads();
-      if (threadIdx.x == 0) atomicAdd(&W.drain_done[band], 1u);
+      __syncwarp();
+      if (lane == 0) {
+        atomicAdd(&W.drain_done[band], 1u);
+        atomicAdd(&W.ctr->sw_drain_cycles, (unsigned long long)(clock64() - t_unit));
+        atomicAdd(&W.ctr->sw_drain_units, 1ull);
+      }
     }
-    __syncthreads();
   }
-  (void)nwarp;
   __syncthreads();
-  for (int m = 0; m < P.nmaps; m++) {
-    double v = msum[m];
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(FULL, v, o);
-    if ((threadIdx.x & 31) == 0 && v != 0.0) atomicAdd(&s_sum[m], v);
-  }
   block_count(&W.ctr->hp_updates, nupd);
   block_count(&W.ctr->n_recheck, nrc);
   block_count(&W.ctr->n_cand, ncand);
@@ -988,37 +1175,88 @@ __global__ void __launch_bounds__(P2M_SWEEP_THREADS) k_sweep(PaintParams P, Swee
     atomicAdd(W.sums + threadIdx.x, s_sum[threadIdx.x]);
 }
 
-/* plain FP64 path: every candidate through the exact path into a full-sky accumulator */
+/* full-sky accumulation: every warp walks 1024-candidate chunks of the whole (ring-band
+   ordered) candidate space; EXACT 1 is the plain FP64 path, EXACT 0 the mixed path.
+   ACC 0: FP64 accumulator, ACC 1: two-float accumulator (8 bytes per map and pixel). */
+template <int EXACT, int ACC>
 __global__ void __launch_bounds__(256) k_paint_full(PaintParams P, SweepBuffers W) {
+  __shared__ CacheEnt s_cache[8][32];
   const long long npix_c = (long long)W.ctr->n_pix;
   if (npix_c == 0) return;
   const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
   const long long chunk = 1024;
+  CacheEnt *cache = s_cache[(threadIdx.x >> 5) & 7];
   unsigned long long nupd = 0, nrc = 0, ncand = 0;
   for (long long c = warp; c * chunk < npix_c; c += nwarps) {
     long long p0 = c * chunk, p1 = min(npix_c, p0 + chunk);
-    walk_candidates<0>(P, W, p0, p1, 0, W.n_items, W.acc, 0, nupd, nrc);
+    walk_candidates<EXACT, ACC>(P, W, p0, p1, 0, W.n_items, W.acc, 0, nupd, nrc, -1, cache);
     if ((threadIdx.x & 31) == 0) ncand += (unsigned long long)(p1 - p0);
   }
   warp_count(&W.ctr->hp_updates, nupd);
+  warp_count(&W.ctr->n_recheck, nrc);
   warp_count(&W.ctr->n_cand, ncand);
 }
 
-/* full-sky FP64 accumulator -> float maps (one pass over all maps) and map sums */
-__global__ void __launch_bounds__(256) k_finalize_full(const double *acc, long long npix, int nmaps,
+/* full-sky accumulator -> float maps in one pass over all maps, map sums, and the
+   accumulator cleared for the next paint */
+template <int ACC>
+__global__ void __launch_bounds__(256) k_finalize_full(void *acc, long long npix, int nmaps,
                                                        float *o0, float *o1, float *o2, float *o3,
                                                        float *o4, float *o5, float *o6, float *o7,
                                                        int accumulate, double *sums) {
   float *outs[8] = {o0, o1, o2, o3, o4, o5, o6, o7};
   double s[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-  for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < npix;
-       p += (long long)gridDim.x * blockDim.x) {
-    for (int m = 0; m < nmaps; m++) {
-      float v = (float)__ldcs(acc + p * nmaps + m);
-      if (accumulate) v = __fadd_rn(outs[m][p], v);
-      __stcs(outs[m] + p, v);
-      s[m] += (double)v;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  if (nmaps == 2) {
+    float4 *a4 = (float4 *)acc; /* (double0, double1) or (hi0, lo0, hi1, lo1) */
+    for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < npix; p += 4 * stride) {
+      float4 a[4];
+#pragma unroll
+      for (int u = 0; u < 4; u++)
+        if (p + u * stride < npix) a[u] = __ldcs(a4 + p + u * stride);
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        long long q = p + u * stride;
+        if (q >= npix) break;
+        float v0, v1;
+        if (ACC == 0) {
+          double2 d = *reinterpret_cast<double2 *>(&a[u]);
+          v0 = (float)d.x;
+          v1 = (float)d.y;
+        } else {
+          v0 = __fadd_rn(a[u].x, a[u].y);
+          v1 = __fadd_rn(a[u].z, a[u].w);
+        }
+        if (accumulate) {
+          v0 = __fadd_rn(o0[q], v0);
+          v1 = __fadd_rn(o1[q], v1);
+        }
+        __stcs(o0 + q, v0);
+        __stcs(o1 + q, v1);
+        __stcs(a4 + q, make_float4(0.0f, 0.0f, 0.0f, 0.0f));
+        s[0] += (double)v0;
+        s[1] += (double)v1;
+      }
+    }
+  } else {
+    for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < npix; p += stride) {
+      for (int m = 0; m < nmaps; m++) {
+        float v;
+        if (ACC == 0) {
+          double *ad = (double *)acc + p * nmaps + m;
+          v = (float)__ldcs(ad);
+          __stcs(ad, 0.0);
+        } else {
+          float2 *af = (float2 *)acc + p * nmaps + m;
+          float2 a = __ldcs(af);
+          v = __fadd_rn(a.x, a.y);
+          __stcs(af, make_float2(0.0f, 0.0f));
+        }
+        if (accumulate) v = __fadd_rn(outs[m][p], v);
+        __stcs(outs[m] + p, v);
+        s[m] += (double)v;
+      }
     }
   }
   for (int m = 0; m < nmaps; m++) {
@@ -1026,6 +1264,47 @@ __global__ void __launch_bounds__(256) k_finalize_full(const double *acc, long l
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(FULL, v, o);
     if ((threadIdx.x & 31) == 0 && v != 0.0) atomicAdd(sums + m, v);
   }
+}
+
+/* folds the nonzero low words of the compensated accumulation into the output maps
+   (out = RN(hi + lo)) and clears them; one warp per dirty 256-pixel tile */
+__global__ void __launch_bounds__(256) k_fold_lo(SweepBuffers W, int nmaps) {
+  const int lane = threadIdx.x & 31;
+  const long long ntiles = (W.npix + 255) >> 8;
+  const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+  for (long long t0 = warp * 32; t0 < ntiles; t0 += nwarps * 32) {
+    long long t = t0 + lane;
+    bool dirty = t < ntiles && W.tiles[t];
+    unsigned m = __ballot_sync(FULL, dirty);
+    while (m) {
+      int b = __ffs(m) - 1;
+      m &= m - 1;
+      long long tt = t0 + b;
+      long long p0 = tt << 8, p1 = min(p0 + 256, W.npix);
+      for (int mp = 0; mp < nmaps; mp++) {
+        float *lo = W.lo + (long long)mp * W.npix;
+        for (long long p = p0 + lane; p < p1; p += 32) {
+          float l = lo[p];
+          if (l != 0.0f) {
+            W.out[mp][p] = __fadd_rn(W.out[mp][p], l);
+            lo[p] = 0.0f;
+          }
+        }
+      }
+      if (lane == 0) W.tiles[tt] = 0;
+    }
+  }
+}
+
+/* sum over a float map (double accumulation) */
+__global__ void __launch_bounds__(256) k_map_sum(const float *map, long long n, double *sum) {
+  double s = 0.0;
+  for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < n;
+       p += (long long)gridDim.x * blockDim.x)
+    s += (double)map[p];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(FULL, s, o);
+  if ((threadIdx.x & 31) == 0 && s != 0.0) atomicAdd(sum, s);
 }
 
 /* flat-sky accumulator -> float map */
@@ -1206,8 +1485,8 @@ void p2m_launch_items(const PaintParams &P, const IngestBuffers &B, long long n_
 void p2m_launch_fs(const PaintParams &P, const IngestBuffers &B, long long n_max, cudaStream_t s,
                    int nsm) {
   k_fs_emit<<<grid_for(n_max, 256, nsm, 4), 256, 0, s>>>(P, B);
-  if (P.precision == 0) k_paint_fs<0><<<nsm * 8, 256, 0, s>>>(P, B);
-  else k_paint_fs<1><<<nsm * 8, 256, 0, s>>>(P, B);
+  if (P.precision == 1) k_paint_fs<1><<<nsm * 8, 256, 0, s>>>(P, B);
+  else k_paint_fs<0><<<nsm * 8, 256, 0, s>>>(P, B);
 }
 void p2m_launch_band_scatter(const PaintParams &P, const RingItem *in, long long n,
                              const long long *band_start, unsigned int *band_cursor,
@@ -1220,35 +1499,56 @@ void p2m_launch_scan_single(const unsigned int *in, long long *out, long long n,
   k_scan_single<<<1, 1024, 0, s>>>(in, out, n, total);
 }
 void p2m_launch_units(const SweepBuffers &W, long long *band_item0, long long *band_cand0,
-                      int *seg_start, int *seg_code, int *unit_target, const long long *band_pix0,
-                      unsigned long long *n_pix, cudaStream_t s) {
-  k_units<<<1, 32, 0, s>>>(W, band_item0, band_cand0, seg_start, seg_code, unit_target, band_pix0,
-                           n_pix);
+                      int *seg_start, int *seg_code, int *unit_target, int *band_chunk0,
+                      long long *chunk_g0, long long chunk_cap, const long long *band_pix0,
+                      unsigned long long *n_pix, cudaStream_t s, int nsm) {
+  k_units<<<1, 32, 0, s>>>(W, band_item0, band_cand0, seg_start, seg_code, unit_target, band_chunk0,
+                           band_pix0, n_pix, W.n_chunks);
+  k_chunk_starts<<<nsm * 4, 256, 0, s>>>(W, band_item0, band_cand0, band_chunk0, chunk_g0, chunk_cap);
 }
 void p2m_launch_sweep(const PaintParams &P, const SweepBuffers &W, cudaStream_t s, int nsm) {
   /* one resident wave: every block claims units until the queue is empty */
   int per_sm = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sweep, P2M_SWEEP_THREADS, 0) !=
-          cudaSuccess ||
-      per_sm < 1)
-    per_sm = 1;
-  k_sweep<<<nsm * per_sm, P2M_SWEEP_THREADS, 0, s>>>(P, W);
+  if (P.precision == 1) {
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sweep<1>, P2M_SWEEP_THREADS, 0) !=
+            cudaSuccess || per_sm < 1)
+      per_sm = 1;
+    k_sweep<1><<<nsm * per_sm, P2M_SWEEP_THREADS, 0, s>>>(P, W);
+  } else {
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sweep<0>, P2M_SWEEP_THREADS, 0) !=
+            cudaSuccess || per_sm < 1)
+      per_sm = 1;
+    k_sweep<0><<<nsm * per_sm, P2M_SWEEP_THREADS, 0, s>>>(P, W);
+  }
 }
 void p2m_launch_paint_full(const PaintParams &P, const SweepBuffers &W, cudaStream_t s, int nsm) {
-  k_paint_full<<<nsm * 8, 256, 0, s>>>(P, W);
+  if (P.precision == 0) k_paint_full<1, 0><<<nsm * 8, 256, 0, s>>>(P, W);
+  else if (P.precision == 1) k_paint_full<0, 2><<<nsm * 8, 256, 0, s>>>(P, W);
+  else k_paint_full<0, 0><<<nsm * 8, 256, 0, s>>>(P, W);
+}
+void p2m_launch_fold_lo(const PaintParams &P, const SweepBuffers &W, cudaStream_t s, int nsm) {
+  k_fold_lo<<<nsm * 8, 256, 0, s>>>(W, P.nmaps);
+}
+void p2m_launch_map_sum(const float *map, long long n, double *sum, cudaStream_t s, int nsm) {
+  k_map_sum<<<grid_for(n, 256, nsm, 8), 256, 0, s>>>(map, n, sum);
 }
 void p2m_launch_finalize_full(const PaintParams &P, const void *acc, long long npix,
                               float *const *out, int accumulate, double *sums, cudaStream_t s,
                               int nsm) {
-  k_finalize_full<<<grid_for(npix, 256, nsm, 8), 256, 0, s>>>(
-      (const double *)acc, npix, P.nmaps, out[0], out[1], out[2], out[3], out[4], out[5], out[6],
-      out[7], accumulate, sums);
+  if (P.precision == 1)
+    k_finalize_full<1><<<grid_for(npix, 256, nsm, 8), 256, 0, s>>>(
+        (void *)acc, npix, P.nmaps, out[0], out[1], out[2], out[3], out[4], out[5], out[6], out[7],
+        accumulate, sums);
+  else
+    k_finalize_full<0><<<grid_for(npix, 256, nsm, 8), 256, 0, s>>>(
+        (void *)acc, npix, P.nmaps, out[0], out[1], out[2], out[3], out[4], out[5], out[6], out[7],
+        accumulate, sums);
 }
 void p2m_launch_finalize_fs(const PaintParams &P, const void *acc, long long npix, float *out,
                             int map, double *sum, cudaStream_t s, int nsm) {
   int g = grid_for(npix, 256, nsm, 8);
-  if (P.precision == 0) k_finalize_fs<0><<<g, 256, 0, s>>>(acc, npix, P.nmaps, map, out, sum);
-  else k_finalize_fs<1><<<g, 256, 0, s>>>(acc, npix, P.nmaps, map, out, sum);
+  if (P.precision == 1) k_finalize_fs<1><<<g, 256, 0, s>>>(acc, npix, P.nmaps, map, out, sum);
+  else k_finalize_fs<0><<<g, 256, 0, s>>>(acc, npix, P.nmaps, map, out, sum);
 }
 void p2m_launch_maptable(const PaintParams &P, const TableConsts &K, const p2m_tabhdr &th,
                          float *d_table, cudaStream_t s) {

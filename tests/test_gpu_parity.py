@@ -14,6 +14,7 @@ REL_TOL = 1e-5       # per pixel, where |v| > MASK_FRAC * max|v|
 MASK_FRAC = 1e-3
 SUM_TOL = 1e-7       # map totals
 FLAGS = p2m.FLAG_RECORD_SETS | p2m.FLAG_ALL_HALOS
+PRECISIONS = ["fp64", "mixed", "mixed64"]
 
 
 def run_gpu(records, tables, precision, nside, npix_fs=0, maps=((0, 1),), flags=FLAGS,
@@ -62,7 +63,7 @@ def assert_sets_equal(gpu_sets, ref_sets):
     assert np.array_equal(g, r), "pixel sets differ in %d entries" % (g != r).any(axis=1).sum()
 
 
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("precision", PRECISIONS)
 def test_config1_tsz_nside512(precision):
     """1e5-halo catalogue, shell 100-3000 Mpc, HEALPix Nside 512, 148 GHz table."""
     rec = catalogs.shell(1, 100_000)
@@ -75,7 +76,7 @@ def test_config1_tsz_nside512(precision):
     assert_maps_close(hp[0], rhp[0], rel=1e-6 if precision == "fp64" else REL_TOL)
 
 
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("precision", PRECISIONS)
 def test_tsz_ksz_two_maps_wide_shell(precision):
     """tSZ y (nu = 0) and kSZ from one table, 100-8000 Mpc shell, zmax = 6, Nside 1024."""
     rec = catalogs.shell(2, 40_000, r=(100.0, 8000.0), m=(1e12, 3e15))
@@ -88,7 +89,7 @@ def test_tsz_ksz_two_maps_wide_shell(precision):
         assert_maps_close(hp[m], rhp[m], what="map %d" % m)
 
 
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("precision", PRECISIONS)
 def test_flatsky_and_healpix(precision):
     """Flat-sky 256^2 over 10 deg with halos concentrated in the field, plus HEALPix."""
     rec = catalogs.cone(3, 30_000, (1.0, 0.0, 0.0), 8.0)
@@ -103,7 +104,7 @@ def test_flatsky_and_healpix(precision):
     assert_maps_close(hp[0], rhp[0], what="healpix")
 
 
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("precision", PRECISIONS)
 def test_edge_cases(precision):
     """Poles, phi = 0, cap boundary, very large discs, the radial cut."""
     rec = catalogs.edge_cases()
@@ -222,18 +223,19 @@ def test_maptable_gpu_matches_oracle():
 def test_fast_path_decisions_match_exact_path():
     """Every disc decision and table index the mixed-precision fast path takes on its own
     agrees with the exact FP64 path (the recheck bands are wide enough)."""
-    rec = catalogs.shell(12, 300_000, r=(100.0, 8000.0), m=(1e12, 3e15))
+    rec = catalogs.shell(12, 1_000_000, r=(100.0, 8000.0), m=(1e12, 3e15))
     tab = catalogs.table(nu=0.0, nchit=40, nmht=40, nrt=200)
-    with p2m.Painter(nside=2048, precision="mixed", maps=((0, 1), (0, 2)), zmax=6.0,
+    with p2m.Painter(nside=4096, precision="mixed", maps=((0, 1), (0, 2)), zmax=6.0,
                      flags=p2m.FLAG_VALIDATE, max_records=len(rec)) as pt:
         pt.load_table(0, tab)
         pt.paint_records(rec)
         pt.flush()
         st = pt.stats()
-    assert st["val_checked"] == st["hp_candidates"] > 1_000_000
+    assert st["val_checked"] == st["hp_candidates"] > 2_000_000
     assert st["val_bad_set"] == 0
     assert st["val_bad_index"] == 0
-    assert st["val_max_du"] < 0.2 * 2e-4  # observed error well inside the band half-width
+    # the largest error of the fast r-index coordinate stays well inside the band half-width
+    assert st["val_max_du"] < 0.25 * 2e-4, st
     assert st["n_recheck"] < 2e-3 * st["hp_candidates"]
 
 
