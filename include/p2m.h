@@ -33,7 +33,7 @@ enum {
   P2M_ERR_BADARG = 1,   /* invalid argument or configuration */
   P2M_ERR_CUDA = 2,     /* a CUDA runtime call failed */
   P2M_ERR_CAPACITY = 3, /* a work buffer overflowed (never truncated silently) */
-  P2M_ERR_TIMEOUT = 4,  /* a bounded device wait gave up */
+  P2M_ERR_TIMEOUT = 4,  /* reserved (no kernel of this library waits on another) */
   P2M_ERR_IO = 5,       /* malformed table / catalogue image */
   P2M_ERR_STATE = 6,    /* call out of sequence */
   P2M_ERR_NOMEM = 7     /* device or pinned allocation failed */
@@ -44,8 +44,9 @@ enum {
   P2M_PREC_FP64 = 0,  /* plain drop-in: FP64 pixel geometry (pix2vec_ring + angdist) for
                          every candidate, FP64 accumulation */
   P2M_PREC_MIXED = 1, /* FP32 disc test and profile interpolation with an exact FP64
-                         recheck near every decision boundary; compensated two-float
-                         FP32 accumulation in L2-resident band windows */
+                         recheck near every decision boundary; compensated FP32
+                         accumulation: the float maps hold the high words, the exact
+                         rounding errors are summed apart and added at read-out */
   P2M_PREC_MIXED_F64 = 2 /* the same decisions; FP64 accumulation (atomic adds executed in
                             L2, not on the SM's FP64 units) */
 };

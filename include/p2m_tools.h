@@ -29,16 +29,11 @@ void p2m_philox4x32(const uint32_t c[4], const uint32_t k[2], uint32_t out[4]);
 
 /* Device time (ms) of each phase of the last paint call and of the last map read-out,
    for a context created with P2M_FLAG_TIMING: [0] cut, [1] per-halo set-up, [2] ring
-   histogram scan, [3] item placement, [4] ring spans, [5] candidate scan, [6] paint,
-   [7] exact recheck, [8] flat sky, [9] read-out.  Diagnostics only (the reference
-   prints no timings). */
+   offsets of the large halos, [3] their ring spans, [4] flat sky, [5] their candidate
+   offsets, [6] HEALPix paint, [7] read-out.  Diagnostics only (the reference prints
+   no timings). */
 struct p2m_ctx;
 int32_t p2m_get_timings(struct p2m_ctx *ctx, double *ms, int32_t n);
-
-/* Sweep counters since the last reset: [0] polls spent waiting on unit dependencies,
-   [1] SM cycles in paint units, [2] SM cycles in drain units, [3] paint units,
-   [4] drain units, [5] ring bands, [6] window pixels.  Diagnostics only. */
-int32_t p2m_get_diagnostics(struct p2m_ctx *ctx, int64_t *out, int32_t n);
 
 /* Self-test of the single-precision math the kernels use (fn: 0 log, 1 exp, 2 pow,
    3 asin, 4 atan, 5 sin, 6 cos, 7 tan) evaluated on the GPU over n device floats;

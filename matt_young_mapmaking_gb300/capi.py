@@ -105,7 +105,6 @@ def load_library():
         "p2m_philox4x32": (None, [VP, VP, VP]),
         "p2m_fmath_eval_device": (I32, [I32, I32, VP, VP, VP, I64]),
         "p2m_get_timings": (I32, [VP, VP, I32]),
-        "p2m_get_diagnostics": (I32, [VP, VP, I32]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -123,10 +122,10 @@ def exported_symbols():
             "p2m_bind_healpix_device", "p2m_get_stats",
             "p2m_synchronize", "p2m_get_pixel_sets", "p2m_make_maptable",
             "p2m_generate_catalogue", "p2m_philox4x32", "p2m_fmath_eval_device",
-            "p2m_get_timings", "p2m_get_diagnostics"]
+            "p2m_get_timings"]
 
 
-PHASES = ["cut", "setup", "item_scan", "items", "flatsky", "group", "paint", "readout"]
+PHASES = ["cut", "setup", "big_scan", "big_items", "flatsky", "big_offsets", "paint", "readout"]
 
 
 def _ptr(a):
@@ -267,14 +266,6 @@ class Painter:
         ms = np.zeros(len(PHASES))
         self._check(self._lib.p2m_get_timings(self._h, _ptr(ms), len(PHASES)))
         return dict(zip(PHASES, ms.tolist()))
-
-    def diagnostics(self):
-        """Sweep counters since the last reset (waits, unit cycles, bands, window size)."""
-        v = np.zeros(7, dtype=np.int64)
-        self._check(self._lib.p2m_get_diagnostics(self._h, _ptr(v), 7))
-        keys = ("wait_polls", "paint_cycles", "drain_cycles", "paint_units", "drain_units",
-                "bands", "window_pixels")
-        return dict(zip(keys, v.tolist()))
 
     def pixel_sets(self):
         n = ctypes.c_int64()

@@ -21,9 +21,6 @@
 
 enum { PH_CUT, PH_SETUP, PH_SCAN, PH_ITEMS, PH_FS, PH_GROUP, PH_PAINT, PH_READOUT, P2M_NPHASE };
 
-/* L2 budget of one window (two windows alternate) */
-#define P2M_WINDOW_BYTES (20LL << 20)
-
 struct p2m_ctx {
   p2m_config cfg;
   int nsm = 0;
@@ -32,23 +29,17 @@ struct p2m_ctx {
   p2m_cosmo cosmo;
   std::vector<float> rofz_host, zofr_host;
   float *d_rofz = nullptr, *d_zofr = nullptr;
-  double2 *d_ringtab = nullptr;
+  float4 *d_ringtab = nullptr;
   p2m_tabhdr th;
   bool th_set = false;
   float *d_tab[P2M_MAXTABLES] = {};
   float band_u = 2e-4f;
-  /* ring bands and windows */
-  int nbands = 0;
-  long long wpix = 0;
-  int *d_band_of_ring = nullptr;
-  long long *d_band_pix0 = nullptr;
-  float2 *d_win = nullptr;
+  int big_rings = P2M_BIG_RINGS;
   /* outputs */
   long long hp_npix = 0, fs_npix = 0;
   float *d_out_own[P2M_MAXMAPS] = {};
   float *d_out[P2M_MAXMAPS] = {};
   double *d_acc64 = nullptr; /* full-sky FP64 accumulator (plain and FP64-accumulating paths) */
-  bool window_sweep = false; /* mixed precision: band windows instead of the full sky */
   /* compensated path: the output maps accumulate the high words; low words and their
      dirty-tile flags stay zero between sweeps */
   float *d_lo = nullptr;
@@ -59,9 +50,8 @@ struct p2m_ctx {
   /* ingest state (accumulated until the next sweep) */
   HaloRec *d_halos = nullptr;
   long long cap_halos = 0, n_halos = 0;
-  RingItem *d_items_raw = nullptr;
+  RingItem *d_items_raw = nullptr; /* items of the large halos */
   long long cap_items_raw = 0, n_items = 0;
-  unsigned int *d_band_hist = nullptr;
   long long rec_count = 0;
   bool dirty = false, swept = false;
   /* per-call buffers */
@@ -77,18 +67,10 @@ struct p2m_ctx {
   long long cap_fs = 0;
   long long *d_scan_tmp = nullptr;
   /* sweep buffers */
-  RingItem *d_items = nullptr;
-  long long cap_items = 0;
   unsigned int *d_counts = nullptr;
   long long cap_counts = 0;
   long long *d_pix_off = nullptr;
   long long cap_pix_off = 0;
-  long long *d_band_item0 = nullptr, *d_band_cand0 = nullptr;
-  unsigned int *d_band_cursor = nullptr, *d_paint_done = nullptr, *d_drain_done = nullptr;
-  int *d_seg_start = nullptr, *d_seg_code = nullptr, *d_unit_target = nullptr;
-  int *d_band_chunk0 = nullptr;
-  long long *d_chunk_g0 = nullptr;
-  long long cap_chunks = 0; /* sized from the previous sweep; larger sweeps search instead */
   unsigned long long *d_nitems = nullptr;
   double *d_sums = nullptr; /* [0, MAXMAPS): HEALPix, [MAXMAPS, 2 MAXMAPS): flat sky */
   long long *d_set_rec = nullptr, *d_set_pix = nullptr;
@@ -206,8 +188,8 @@ PaintParams make_params(const p2m_ctx *ctx, int nfloat) {
   P.rofz = ctx->d_rofz;
   P.zofr = ctx->d_zofr;
   P.ringtab = ctx->d_ringtab;
-  P.band_of_ring = ctx->d_band_of_ring;
   P.band_u = ctx->band_u;
+  P.big_rings = ctx->big_rings;
   if (ctx->th_set) {
     float fr;
     int ir;
@@ -229,7 +211,6 @@ IngestBuffers ingest_buffers(const p2m_ctx *ctx, const float *records) {
   B.nring = ctx->d_nring;
   B.ioff = ctx->d_ioff;
   B.items = ctx->d_items_raw + ctx->n_items;
-  B.band_hist = ctx->d_band_hist;
   B.fs_items = ctx->d_fs_items;
   B.fs_cap = ctx->cap_fs;
   B.fs_acc = ctx->d_fs_acc;
@@ -259,8 +240,6 @@ p2m_status read_counters(p2m_ctx *ctx, cudaStream_t s) {
     return fail(ctx, P2M_ERR_STATE, "candidate walk exceeded its round bound (maps are incomplete)");
   if (h.err & P2M_DEVERR_FS_OVERFLOW)
     return fail(ctx, P2M_ERR_CAPACITY, "flat-sky row buffer overflow (maps are incomplete)");
-  if (h.err & P2M_DEVERR_TIMEOUT)
-    return fail(ctx, P2M_ERR_TIMEOUT, "a sweep unit waited past its limit (maps are incomplete)");
   return P2M_OK;
 }
 
@@ -377,31 +356,15 @@ SweepBuffers sweep_buffers(const p2m_ctx *ctx) {
   SweepBuffers W;
   memset(&W, 0, sizeof(W));
   W.halos = ctx->d_halos;
-  W.items = ctx->d_items;
+  W.n_halos = ctx->n_halos;
+  W.items = ctx->d_items_raw;
   W.pix_off = ctx->d_pix_off;
   W.n_items = ctx->n_items;
-  W.nbands = ctx->nbands;
-  W.band_item0 = ctx->d_band_item0;
-  W.band_cand0 = ctx->d_band_cand0;
-  W.band_pix0 = ctx->d_band_pix0;
-  W.seg_start = ctx->d_seg_start;
-  W.seg_code = ctx->d_seg_code;
-  W.unit_target = ctx->d_unit_target;
-  W.band_chunk0 = ctx->d_band_chunk0;
-  W.chunk_g0 = ctx->d_chunk_g0;
-  W.chunk_cap = ctx->cap_chunks;
-  W.n_chunks = &ctx->d_ctr->n_chunks;
-  W.paint_done = ctx->d_paint_done;
-  W.drain_done = ctx->d_drain_done;
-  W.win = ctx->d_win;
-  W.wpix = ctx->wpix;
   for (int m = 0; m < P2M_MAXMAPS; m++) W.out[m] = ctx->d_out[m];
-  W.accumulate = ctx->swept ? 1 : 0;
   W.acc = ctx->d_acc64;
   W.lo = ctx->d_lo;
   W.tiles = ctx->d_tiles;
   W.npix = ctx->hp_npix;
-  W.sums = ctx->d_sums;
   W.ctr = ctx->d_ctr;
   W.set_rec = ctx->d_set_rec;
   W.set_pix = ctx->d_set_pix;
@@ -427,131 +390,55 @@ p2m_status sweep(p2m_ctx *ctx, cudaStream_t s) {
   }
   join_in(ctx, s);
   const long long n = ctx->n_items;
-  const int nb = ctx->nbands;
-  CK(grow(&ctx->d_items, &ctx->cap_items, std::max(n, 1LL)));
-  CK(grow(&ctx->d_counts, &ctx->cap_counts, std::max(n, 1LL)));
-  CK(grow(&ctx->d_pix_off, &ctx->cap_pix_off, std::max(n, 1LL)));
   CK(cudaMemsetAsync(ctx->d_ctr, 0, CALL_CTR_BYTES, s));
-  unsigned long long nn = (unsigned long long)n;
-  CK(cudaMemcpyAsync(ctx->d_nitems, &nn, sizeof(nn), cudaMemcpyHostToDevice, s));
   PaintParams P = make_params(ctx, 7);
   TB(PH_GROUP);
-  p2m_launch_scan_single(ctx->d_band_hist, ctx->d_band_item0, nb, nullptr, s);
-  CK(cudaMemcpyAsync(ctx->d_band_item0 + nb, &n, sizeof(long long), cudaMemcpyHostToDevice, s));
-  CK(cudaMemsetAsync(ctx->d_band_cursor, 0, sizeof(unsigned) * (size_t)nb, s));
-  CK(cudaMemsetAsync(ctx->d_paint_done, 0, sizeof(unsigned) * (size_t)nb, s));
-  CK(cudaMemsetAsync(ctx->d_drain_done, 0, sizeof(unsigned) * (size_t)nb, s));
-  p2m_launch_band_scatter(P, ctx->d_items_raw, n, ctx->d_band_item0, ctx->d_band_cursor,
-                          ctx->d_items, ctx->d_counts, s, ctx->nsm);
-  p2m_launch_scan_u32(ctx->d_counts, ctx->d_nitems, ctx->d_pix_off, &ctx->d_ctr->n_pix,
-                      ctx->d_scan_tmp, s);
-  SweepBuffers W = sweep_buffers(ctx);
-  if (!ctx->swept) CK(cudaMemsetAsync(ctx->d_sums, 0, sizeof(double) * P2M_MAXMAPS, s));
-  if (ctx->window_sweep)
-    p2m_launch_units(W, ctx->d_band_item0, ctx->d_band_cand0, ctx->d_seg_start, ctx->d_seg_code,
-                     ctx->d_unit_target, ctx->d_band_chunk0, ctx->d_chunk_g0, ctx->cap_chunks,
-                     ctx->d_band_pix0, &ctx->d_ctr->n_pix, s, ctx->nsm);
-  TE(PH_GROUP);
-  TB(PH_PAINT);
-  if (ctx->window_sweep) {
-    p2m_launch_sweep(P, W, s, ctx->nsm);
-    TE(PH_PAINT);
-  } else {
-    p2m_launch_paint_full(P, W, s, ctx->nsm);
-    TE(PH_PAINT);
-    TB(PH_READOUT);
-    if (compensated(ctx)) {
-      /* fold the sparse low words into the maps and clear them */
-      p2m_launch_fold_lo(P, W, s, ctx->nsm);
-    } else {
-      /* the read-out also clears the accumulator for the next paint */
-      p2m_launch_finalize_full(P, ctx->d_acc64, ctx->hp_npix, ctx->d_out, ctx->swept ? 1 : 0,
-                               ctx->d_sums, s, ctx->nsm);
-    }
-    TE(PH_READOUT);
+  if (n > 0) {
+    /* candidate offsets of the large halos' items */
+    CK(grow(&ctx->d_counts, &ctx->cap_counts, n));
+    CK(grow(&ctx->d_pix_off, &ctx->cap_pix_off, n));
+    unsigned long long nn = (unsigned long long)n;
+    CK(cudaMemcpyAsync(ctx->d_nitems, &nn, sizeof(nn), cudaMemcpyHostToDevice, s));
+    p2m_launch_item_counts(ctx->d_items_raw, n, ctx->d_counts, s, ctx->nsm);
+    p2m_launch_scan_u32(ctx->d_counts, ctx->d_nitems, ctx->d_pix_off, &ctx->d_ctr->n_pix,
+                        ctx->d_scan_tmp, s);
   }
+  TE(PH_GROUP);
+  SweepBuffers W = sweep_buffers(ctx);
+  TB(PH_PAINT);
+  p2m_launch_paint_halos(P, W, s, ctx->nsm);
+  if (n > 0) p2m_launch_paint_full(P, W, s, ctx->nsm);
+  TE(PH_PAINT);
+  TB(PH_READOUT);
+  if (compensated(ctx)) {
+    /* fold the sparse low words into the maps and clear them */
+    p2m_launch_fold_lo(P, W, s, ctx->nsm);
+  } else {
+    /* the read-out also clears the accumulator for the next paint */
+    p2m_launch_finalize_full(P, ctx->d_acc64, ctx->hp_npix, ctx->d_out, ctx->swept ? 1 : 0, s,
+                             ctx->nsm);
+  }
+  TE(PH_READOUT);
   CK(cudaGetLastError());
   p2m_status st = read_counters(ctx, s);
   join_out(ctx, s);
-  if (st == P2M_ERR_TIMEOUT || st == P2M_ERR_STATE) {
+  if (st) {
     /* accumulators may hold partial sums: clear them so the context stays usable */
-    if (ctx->d_win)
-      cudaMemsetAsync(ctx->d_win, 0, sizeof(float2) * (size_t)(P2M_NBUF * ctx->wpix * ctx->cfg.nmaps),
-                      ctx->stream);
     if (ctx->d_acc64)
       cudaMemsetAsync(ctx->d_acc64, 0, sizeof(double) * (size_t)ctx->cfg.nmaps * (size_t)ctx->hp_npix,
                       ctx->stream);
     if (ctx->d_lo) {
       cudaMemsetAsync(ctx->d_lo, 0, sizeof(float) * (size_t)ctx->cfg.nmaps * (size_t)ctx->hp_npix,
                       ctx->stream);
-      cudaMemsetAsync(ctx->d_tiles, 0, (size_t)((ctx->hp_npix + 255) >> 8), ctx->stream);
+      cudaMemsetAsync(ctx->d_tiles, 0, (size_t)((ctx->hp_npix + P2M_TILE_PIX - 1) >> P2M_TILE_SHIFT),
+                      ctx->stream);
     }
+    return st;
   }
-  if (st) return st;
-  /* warp-chunk start table sized for the next sweep of this size */
-  long long need_chunks = (long long)ctx->h_ctr->n_chunks;
-  if (need_chunks > ctx->cap_chunks) CK(grow(&ctx->d_chunk_g0, &ctx->cap_chunks, need_chunks));
-  CK(cudaMemsetAsync(ctx->d_band_hist, 0, sizeof(unsigned) * (size_t)nb, s));
   ctx->n_items = 0;
   ctx->n_halos = 0;
   ctx->dirty = false;
   ctx->swept = true;
-  return P2M_OK;
-}
-
-/* ring bands whose pixels fit one window */
-p2m_status build_bands(p2m_ctx *ctx) {
-  const int N = ctx->cfg.nside, nr = 4 * N;
-  long long wbytes = P2M_WINDOW_BYTES;
-  if (const char *e = getenv("P2M_WINDOW_MB")) wbytes = (long long)(atof(e) * (1 << 20));
-  long long w = wbytes / (8LL * ctx->cfg.nmaps);
-  w = std::max(w, 4LL * N); /* at least the widest ring */
-  std::vector<int> bor((size_t)nr, 0);
-  std::vector<long long> pix0;
-  long long start = 0, cur = 0;
-  int b = 0;
-  pix0.push_back(0);
-  for (int r = 1; r < nr; r++) {
-    int npr, ks;
-    long long npn;
-    p2m_ring_info(N, r, &npr, &ks, &npn);
-    if (cur + npr > w && cur > 0) {
-      b++;
-      start += cur;
-      pix0.push_back(start);
-      cur = 0;
-    }
-    bor[(size_t)r] = b;
-    cur += npr;
-  }
-  pix0.push_back(start + cur);
-  ctx->nbands = b + 1;
-  if (ctx->nbands > 2047) return fail(ctx, P2M_ERR_BADARG, "too many ring bands");
-  long long wmax = 0;
-  for (int k = 0; k < ctx->nbands; k++) wmax = std::max(wmax, pix0[(size_t)k + 1] - pix0[(size_t)k]);
-  ctx->wpix = wmax;
-  CK(cudaMalloc((void **)&ctx->d_band_of_ring, sizeof(int) * (size_t)nr));
-  CK(cudaMemcpy(ctx->d_band_of_ring, bor.data(), sizeof(int) * (size_t)nr, cudaMemcpyHostToDevice));
-  CK(cudaMalloc((void **)&ctx->d_band_pix0, sizeof(long long) * pix0.size()));
-  CK(cudaMemcpy(ctx->d_band_pix0, pix0.data(), sizeof(long long) * pix0.size(), cudaMemcpyHostToDevice));
-  size_t nb = (size_t)ctx->nbands;
-  CK(cudaMalloc((void **)&ctx->d_band_hist, sizeof(unsigned) * nb));
-  CK(cudaMemset(ctx->d_band_hist, 0, sizeof(unsigned) * nb));
-  CK(cudaMalloc((void **)&ctx->d_band_cursor, sizeof(unsigned) * nb));
-  CK(cudaMalloc((void **)&ctx->d_paint_done, sizeof(unsigned) * nb));
-  CK(cudaMalloc((void **)&ctx->d_drain_done, sizeof(unsigned) * nb));
-  CK(cudaMalloc((void **)&ctx->d_band_item0, sizeof(long long) * (nb + 1)));
-  CK(cudaMalloc((void **)&ctx->d_band_cand0, sizeof(long long) * (nb + 1)));
-  CK(cudaMalloc((void **)&ctx->d_seg_start, sizeof(int) * (2 * nb + 1)));
-  CK(cudaMalloc((void **)&ctx->d_seg_code, sizeof(int) * 2 * nb));
-  CK(cudaMalloc((void **)&ctx->d_unit_target, sizeof(int) * 2 * nb));
-  CK(cudaMalloc((void **)&ctx->d_band_chunk0, sizeof(int) * (nb + 1)));
-  CK(grow(&ctx->d_chunk_g0, &ctx->cap_chunks, 1LL << 16));
-  if (ctx->window_sweep) {
-    size_t wb = sizeof(float2) * (size_t)(P2M_NBUF * ctx->wpix * ctx->cfg.nmaps);
-    CK(cudaMalloc((void **)&ctx->d_win, wb));
-    CK(cudaMemset(ctx->d_win, 0, wb));
-  }
   return P2M_OK;
 }
 
@@ -577,6 +464,8 @@ p2m_status p2m_create(const p2m_config *cfg, p2m_ctx **out) {
   ctx->cfg = *cfg;
   *out = ctx;
   if (const char *e = getenv("P2M_BAND_U")) ctx->band_u = (float)atof(e);
+  /* test hook: route every halo through one painting path (0: stored items only) */
+  if (const char *e = getenv("P2M_BIG_RINGS")) ctx->big_rings = std::max(0, atoi(e));
   CK(cudaSetDevice(cfg->device));
   CK(cudaDeviceGetAttribute(&ctx->nsm, cudaDevAttrMultiProcessorCount, cfg->device));
   CK(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
@@ -592,38 +481,34 @@ p2m_status p2m_create(const p2m_config *cfg, p2m_ctx **out) {
   CK(cudaMemcpy(ctx->d_zofr, ctx->zofr_host.data(), sizeof(float) * P2M_NZTAB, cudaMemcpyHostToDevice));
   if (cfg->nside > 0) {
     int nr = 4 * cfg->nside;
-    std::vector<double2> rt((size_t)nr);
-    rt[0] = make_double2(1.0, 0.0);
+    /* ring z and sin(theta) (pix_tools.F90 ring2z) as (hi, lo) float pairs */
+    std::vector<float4> rt((size_t)nr);
+    rt[0] = make_float4(1.0f, 0.0f, 0.0f, 0.0f);
     for (int r = 1; r < nr; r++) {
       double z, sn;
       p2m_ring_z_sth(cfg->nside, r, &z, &sn);
-      rt[(size_t)r] = make_double2(z, sn);
+      float zh = (float)z, sh = (float)sn;
+      rt[(size_t)r] = make_float4(zh, (float)(z - (double)zh), sh, (float)(sn - (double)sh));
     }
-    CK(cudaMalloc((void **)&ctx->d_ringtab, sizeof(double2) * (size_t)nr));
-    CK(cudaMemcpy(ctx->d_ringtab, rt.data(), sizeof(double2) * (size_t)nr, cudaMemcpyHostToDevice));
+    CK(cudaMalloc((void **)&ctx->d_ringtab, sizeof(float4) * (size_t)nr));
+    CK(cudaMemcpy(ctx->d_ringtab, rt.data(), sizeof(float4) * (size_t)nr, cudaMemcpyHostToDevice));
     ctx->hp_npix = 12LL * cfg->nside * cfg->nside;
     for (int m = 0; m < cfg->nmaps; m++) {
       CK(cudaMalloc((void **)&ctx->d_out_own[m], sizeof(float) * (size_t)ctx->hp_npix));
       ctx->d_out[m] = ctx->d_out_own[m];
     }
-    if (cfg->precision != P2M_PREC_FP64) {
-      const char *e = getenv("P2M_ACCUM");
-      ctx->window_sweep = e && strcmp(e, "window") == 0;
-    }
-    if (!ctx->window_sweep && cfg->precision == P2M_PREC_MIXED) {
+    if (cfg->precision == P2M_PREC_MIXED) {
       size_t lb = sizeof(float) * (size_t)cfg->nmaps * (size_t)ctx->hp_npix;
-      size_t tb = (size_t)((ctx->hp_npix + 255) >> 8);
+      size_t tb = (size_t)((ctx->hp_npix + P2M_TILE_PIX - 1) >> P2M_TILE_SHIFT);
       CK(cudaMalloc((void **)&ctx->d_lo, lb));
       CK(cudaMemset(ctx->d_lo, 0, lb));
       CK(cudaMalloc((void **)&ctx->d_tiles, tb));
       CK(cudaMemset(ctx->d_tiles, 0, tb));
-    } else if (!ctx->window_sweep) {
+    } else {
       size_t ab = sizeof(double) * (size_t)cfg->nmaps * (size_t)ctx->hp_npix;
       CK(cudaMalloc((void **)&ctx->d_acc64, ab));
       CK(cudaMemset(ctx->d_acc64, 0, ab));
     }
-    p2m_status st = build_bands(ctx);
-    if (st) return st;
   }
   if (cfg->npix_fs > 0) {
     ctx->fs_npix = (long long)cfg->npix_fs * cfg->npix_fs;
@@ -654,14 +539,10 @@ void p2m_destroy(p2m_ctx *ctx) {
   if (!ctx) return;
   cudaSetDevice(ctx->cfg.device);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
-  void *ptrs[] = {ctx->d_rofz, ctx->d_zofr, ctx->d_ringtab, ctx->d_band_of_ring, ctx->d_band_pix0,
-                  ctx->d_win, ctx->d_acc64, ctx->d_fs_acc, ctx->d_fs_out, ctx->d_halos,
-                  ctx->d_items_raw, ctx->d_band_hist, ctx->d_records, ctx->d_surv, ctx->d_nring,
-                  ctx->d_ioff, ctx->d_fs_items, ctx->d_scan_tmp, ctx->d_items, ctx->d_counts,
-                  ctx->d_pix_off, ctx->d_band_item0, ctx->d_band_cand0, ctx->d_band_cursor,
-                  ctx->d_paint_done, ctx->d_drain_done, ctx->d_seg_start, ctx->d_seg_code,
-                  ctx->d_unit_target, ctx->d_band_chunk0, ctx->d_chunk_g0, ctx->d_nitems,
-                  ctx->d_sums, ctx->d_set_rec, ctx->d_set_pix,
+  void *ptrs[] = {ctx->d_rofz, ctx->d_zofr, ctx->d_ringtab, ctx->d_acc64, ctx->d_fs_acc,
+                  ctx->d_fs_out, ctx->d_halos, ctx->d_items_raw, ctx->d_records, ctx->d_surv,
+                  ctx->d_nring, ctx->d_ioff, ctx->d_fs_items, ctx->d_scan_tmp, ctx->d_counts,
+                  ctx->d_pix_off, ctx->d_nitems, ctx->d_sums, ctx->d_set_rec, ctx->d_set_pix,
                   ctx->d_ctr, ctx->d_prep, ctx->d_lo, ctx->d_tiles};
   for (void *p : ptrs)
     if (p) cudaFree(p);
@@ -742,7 +623,6 @@ p2m_status p2m_reset_maps(p2m_ctx *ctx) {
   ctx->dirty = false;
   ctx->swept = false;
   ctx->outs_zeroed = false;
-  if (ctx->d_band_hist) CK(cudaMemsetAsync(ctx->d_band_hist, 0, sizeof(unsigned) * (size_t)ctx->nbands, s));
   if (ctx->d_fs_acc)
     CK(cudaMemsetAsync(ctx->d_fs_acc, 0, 8 * (size_t)ctx->cfg.nmaps * (size_t)ctx->fs_npix, s));
   CK(cudaMemsetAsync(ctx->d_ctr, 0, sizeof(DevCounters), s));
@@ -933,19 +813,6 @@ int32_t p2m_get_timings(p2m_ctx *ctx, double *ms, int32_t n) {
       ms[k] = (double)t;
     }
   }
-  return P2M_OK;
-}
-
-int32_t p2m_get_diagnostics(p2m_ctx *ctx, int64_t *out, int32_t n) {
-  if (!ctx || !out) return P2M_ERR_BADARG;
-  CK(cudaSetDevice(ctx->cfg.device));
-  CK(cudaStreamSynchronize(ctx->stream));
-  DevCounters h;
-  CK(cudaMemcpy(&h, ctx->d_ctr, sizeof(h), cudaMemcpyDeviceToHost));
-  const int64_t v[7] = {(int64_t)h.sw_wait_polls, (int64_t)h.sw_paint_cycles,
-                        (int64_t)h.sw_drain_cycles, (int64_t)h.sw_paint_units,
-                        (int64_t)h.sw_drain_units, ctx->nbands, ctx->wpix};
-  for (int k = 0; k < n; k++) out[k] = k < 7 ? v[k] : 0;
   return P2M_OK;
 }
 

@@ -1,24 +1,22 @@
 /*
  * p2m_internal.h -- device data layout and kernel launchers of the halo painter.
  *
- * A paint call ingests catalogue records; the maps are produced by a sweep when they
- * are read.  Ingest (one stream, one host round trip to size the item buffer):
+ * A paint call ingests catalogue records; the HEALPix maps are produced by a sweep when
+ * they are read.  Ingest (one stream, one host round trip to size the item buffer):
  *   k_cut      records -> halos inside the radial cut with mass >= mmin whose table
  *              value is not identically zero (block-aggregated compaction)
  *   k_setup    per halo: the loop quantities of pks2map.f90:284-298, disc radius and
  *              centre, interpolation constants, candidate ring range, flat-sky box
- *   scan       rings per halo -> item offsets
- *   k_items    per (halo, ring) item: FP32 superset of the ring's pixel span and the
- *              ring constants of the disc test; histogram of items per ring band
+ *   scan       rings of the large halos (more than big_rings rings) -> item offsets
+ *   k_items    per (large halo, ring) item: FP32 superset of the ring's pixel span and
+ *              the ring constants of the disc test
  *   k_paint_fs flat-sky rows (exact float sequence of the reference)
- * Sweep (mixed precision):
- *   scan + k_band_scatter   items grouped by ring band (a band's pixels fit in L2)
- *   scan       candidate counts -> candidate offsets; k_units: the unit queue
- *   k_sweep    persistent: claims units in order; a paint unit deposits one slice of a
- *              band's candidates into that band's L2-resident window (two-float
- *              atomics), a drain unit converts one slice of a painted window to the
- *              float output maps and clears it.  Two windows alternate between bands.
- * Sweep (plain FP64): k_paint_full into a full-sky FP64 accumulator, k_finalize_full.
+ * Sweep:
+ *   k_paint_halos  the other halos, enumeration fused with painting: a warp builds the
+ *              ring spans of 32 halos in registers and paints their candidates
+ *   scan + k_paint_full  the large halos' items, load-balanced over candidate pixels
+ *   read-out   mixed precision: the maps hold the high words of a compensated sum and
+ *              k_fold_lo adds the sparse low words; FP64 accumulation: k_finalize_full
  */
 #ifndef P2M_INTERNAL_H
 #define P2M_INTERNAL_H
@@ -28,40 +26,32 @@
 
 #include "p2m_scalar.h"
 
-#define P2M_NBUF 4            /* windows in rotation between bands */
-#define P2M_LAG 2             /* a band is drained after the next P2M_LAG bands are queued */
-#define P2M_SWEEP_THREADS 256
-#ifndef P2M_SWEEP_MINBLOCKS
-#define P2M_SWEEP_MINBLOCKS 3 /* resident sweep blocks per SM the register budget allows */
-#endif
-#define P2M_WARP_CHUNK 512    /* candidates per paint unit (one warp) */
-#define P2M_DRAIN_UNIT 4096   /* map pixels per drain unit (one warp) */
+#define P2M_BIG_RINGS 64      /* default: halos spanning more rings go through the item buffer */
+#define P2M_TILE_SHIFT 5      /* compensated path: a flagged tile is 32 pixels (128 bytes) */
+#define P2M_TILE_PIX (1 << P2M_TILE_SHIFT)
 
 struct DevCounters {
   /* per call (cleared before every ingest call and every sweep) */
-  unsigned long long n_surv, n_items, n_pix, n_fs_items, n_fs_rows, n_chunks;
-  unsigned int err, next_unit, abort, pad0;
+  unsigned long long n_surv, n_items, n_pix, n_fs_items, n_fs_rows;
+  unsigned int err, next_unit;
   /* cumulative since the last reset */
   unsigned long long hp_updates, fs_updates, n_sets, n_recheck, n_shell, n_massive, n_enum,
       n_cand;
   unsigned long long val_checked, val_bad_set, val_bad_index;
   unsigned int val_max_du; /* float bits of the largest |u_fast - u_exact| */
   unsigned int pad1;
-  /* sweep diagnostics: polls spent waiting, SM cycles spent in paint / drain units */
-  unsigned long long sw_wait_polls, sw_paint_cycles, sw_drain_cycles, sw_paint_units,
-      sw_drain_units;
 };
 
 enum {
   P2M_DEVERR_FS_OVERFLOW = 2,
   P2M_DEVERR_RADIUS = 4,
-  P2M_DEVERR_ITEMS = 8,
-  P2M_DEVERR_TIMEOUT = 16
+  P2M_DEVERR_ITEMS = 8
 };
 
 /* one enumerated halo */
 struct HaloRec {
-  double z0, sth0, phi0f; /* unit disc centre: z, sin(theta), phi / 2pi */
+  float z0h, z0l, s0h, s0l, p0h, p0l; /* unit disc centre: z, sin(theta), phi / 2pi as
+                                         (hi, lo) float pairs, hi + lo = the FP64 value */
   float hv[3];            /* hpvec1 of haloproject.f90:51-53 (float values) */
   float T;                /* dtheta_halo (float value), haloproject.f90:47 */
   float C_in, C_out, C_span; /* chord^2 thresholds: certainly inside / outside / span */
@@ -108,10 +98,10 @@ struct PaintParams {
   int ir_c;     /* r-index and fraction for r < rmint (r = rmint + 1e-5) */
   float fr_c;
   float band_u;  /* half-width of the r-index recheck band (cell units) */
+  int big_rings; /* halos spanning more rings are painted from stored items */
   const float *tables[P2M_MAXTABLES];
   const float *rofz, *zofr;
-  const double2 *ringtab; /* (z, sin theta) of rings 1..4N-1 at index ring */
-  const int *band_of_ring;
+  const float4 *ringtab; /* (z hi, z lo, sin theta hi, sin theta lo) of ring i at index i */
 };
 
 /* buffers of one ingest call */
@@ -121,10 +111,9 @@ struct IngestBuffers {
   int *surv;            /* record indices of enumerated halos (call-local) */
   HaloRec *halos;       /* halos[0..n_surv) of this call */
   long long halo_base;  /* global index of halos[0] */
-  unsigned int *nring;  /* rings per halo */
+  unsigned int *nring;  /* rings per large halo, 0 for the others */
   long long *ioff;      /* item offset per halo (call-local) */
   RingItem *items;      /* items of this call */
-  unsigned int *band_hist;
   FsItem *fs_items;
   long long fs_cap;
   void *fs_acc;
@@ -137,30 +126,15 @@ struct IngestBuffers {
 /* buffers of one sweep */
 struct SweepBuffers {
   const HaloRec *halos;
-  const RingItem *items;   /* grouped by band */
-  const long long *pix_off;
+  long long n_halos;
+  const RingItem *items;       /* items of the large halos */
+  const long long *pix_off;    /* candidate offset of each item */
   long long n_items;
-  int nbands;
-  const long long *band_item0; /* [nbands+1] */
-  const long long *band_cand0; /* [nbands+1] */
-  const long long *band_pix0;  /* [nbands+1] first map pixel of each band */
-  const int *seg_start;        /* [2*nbands+1] unit prefix of the segment sequence */
-  const int *seg_code;         /* [2*nbands] band | (is_drain << 30) */
-  const int *unit_target;      /* [2*nbands] units of P_b at b, of D_b at nbands + b */
-  const int *band_chunk0;      /* [nbands+1] first warp chunk of each band */
-  const long long *chunk_g0;   /* first item of each warp chunk (the first chunk_cap) */
-  long long chunk_cap;
-  unsigned long long *n_chunks;
-  unsigned int *paint_done, *drain_done; /* [nbands] */
-  float2 *win;                 /* P2M_NBUF windows of wpix * nmaps (hi, lo) */
-  long long wpix;
   float *out[P2M_MAXMAPS];     /* float output maps */
-  int accumulate;              /* add to the output maps instead of overwriting */
-  void *acc;                   /* full-sky accumulator (plain FP64 and FP64-accumulating paths) */
+  void *acc;                   /* full-sky FP64 accumulator (FP64-accumulating paths) */
   float *lo;                   /* compensated path: low words, map m at lo + m * npix */
-  unsigned char *tiles;        /* compensated path: 1 per 256-pixel tile with a nonzero low word */
+  unsigned char *tiles;        /* compensated path: 1 per tile with a nonzero low word */
   long long npix;
-  double *sums;                /* [nmaps] sum over each output map */
   DevCounters *ctr;
   long long *set_rec, *set_pix;
   long long set_cap;
@@ -179,20 +153,12 @@ void p2m_launch_items(const PaintParams &P, const IngestBuffers &B, long long n_
                       cudaStream_t s, int nsm);
 void p2m_launch_fs(const PaintParams &P, const IngestBuffers &B, long long n_max, cudaStream_t s,
                    int nsm);
-void p2m_launch_band_scatter(const PaintParams &P, const RingItem *in, long long n,
-                             const long long *band_start, unsigned int *band_cursor,
-                             RingItem *out, unsigned int *counts, cudaStream_t s, int nsm);
-void p2m_launch_scan_single(const unsigned int *in, long long *out, long long n,
-                            unsigned long long *total, cudaStream_t s);
-void p2m_launch_units(const SweepBuffers &W, long long *band_item0, long long *band_cand0,
-                      int *seg_start, int *seg_code, int *unit_target, int *band_chunk0,
-                      long long *chunk_g0, long long chunk_cap, const long long *band_pix0,
-                      unsigned long long *n_pix, cudaStream_t s, int nsm);
-void p2m_launch_sweep(const PaintParams &P, const SweepBuffers &W, cudaStream_t s, int nsm);
+void p2m_launch_item_counts(const RingItem *items, long long n, unsigned int *counts,
+                            cudaStream_t s, int nsm);
+void p2m_launch_paint_halos(const PaintParams &P, const SweepBuffers &W, cudaStream_t s, int nsm);
 void p2m_launch_paint_full(const PaintParams &P, const SweepBuffers &W, cudaStream_t s, int nsm);
 void p2m_launch_finalize_full(const PaintParams &P, const void *acc, long long npix,
-                              float *const *out, int accumulate, double *sums, cudaStream_t s,
-                              int nsm);
+                              float *const *out, int accumulate, cudaStream_t s, int nsm);
 void p2m_launch_finalize_fs(const PaintParams &P, const void *acc, long long npix, float *out,
                             int map, double *sum, cudaStream_t s, int nsm);
 void p2m_launch_fold_lo(const PaintParams &P, const SweepBuffers &W, cudaStream_t s, int nsm);

@@ -1,11 +1,13 @@
 /*
  * p2m_kernels.cu -- sm_103a kernels of the halo painter (pipeline in p2m_internal.h).
  *
- * Load balance is at the level of candidate pixels: per-ring candidate spans are
- * prefix-summed and each warp walks a contiguous range of the candidate space, finding
- * each lane's item with a 32-wide search over offsets held in registers.  Deposits of
- * the mixed-precision path go to an L2-resident window of one ring band; the HBM
- * traffic of the maps is then one float write per map pixel.
+ * The bulk of the halos is enumerated and painted by one fused kernel: a warp builds
+ * the (halo, ring) candidate spans of 32 halos in registers and paints their candidate
+ * pixels 32 at a time, so no per-item data goes through memory.  Halos spanning many
+ * rings are load-balanced at the level of candidate pixels instead: their spans are
+ * stored and prefix-summed, and each warp walks a contiguous range of the candidate
+ * space.  Mixed precision accumulates into the float maps with the exact rounding
+ * error of every add kept apart (compensated summation).
  */
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -56,11 +58,6 @@ __device__ __forceinline__ p2m_hinterp halo_hinterp(const HaloRec &H) {
   return hi;
 }
 
-__device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
-  unsigned v;
-  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-  return v;
-}
 
 /* ---------------------------------------------------------------- ingest: cut ----- */
 
@@ -189,7 +186,7 @@ __device__ void halo_geometry(const PaintParams &P, float xh, float yh, float zh
   /* HEALPix disc (haloproject.f90:51-55) */
   H.ir_lo = 1;
   H.ir_hi = 0;
-  H.z0 = H.sth0 = H.phi0f = 0.0;
+  H.z0h = H.z0l = H.s0h = H.s0l = H.p0h = H.p0l = 0.0f;
   H.C_in = H.C_out = H.C_span = 0.0f;
   if (P.nside > 0) {
     H.hv[0] = FDIV(zf, chih);
@@ -201,15 +198,20 @@ __device__ void halo_geometry(const PaintParams &P, float xh, float yh, float zh
       double a = (double)H.hv[0], b = (double)H.hv[1], c = (double)H.hv[2];
       double rxy = DSQRT(DADD(DMUL(a, a), DMUL(b, b)));
       double nrm = DSQRT(DADD(DADD(DMUL(a, a), DMUL(b, b)), DMUL(c, c)));
-      H.z0 = DDIV(c, nrm);
-      H.sth0 = DDIV(rxy, nrm);
+      double z0 = DDIV(c, nrm), s0 = DDIV(rxy, nrm);
       double phi0 = (a != 0.0 || b != 0.0) ? atan2(b, a) : 0.0;
-      H.phi0f = phi0 / P2M_HP_TWOPI;
+      double pf = phi0 / P2M_HP_TWOPI;
+      H.z0h = (float)z0;
+      H.z0l = (float)(z0 - (double)H.z0h);
+      H.s0h = (float)s0;
+      H.s0l = (float)(s0 - (double)H.s0h);
+      H.p0h = (float)pf;
+      H.p0l = (float)(pf - (double)H.p0h);
       H.C_in = chord2(T * (1.0f - 2e-6f));
       H.C_out = chord2(T * (1.0f + 2e-6f));
       float tspan = T * (1.0f + 2e-5f) + 1e-6f;
       H.C_span = chord2(tspan);
-      float theta0 = atan2f((float)H.sth0, (float)H.z0);
+      float theta0 = atan2f(H.s0h, H.z0h);
       float tmin = theta0 - tspan, tmax = theta0 + tspan;
       int n4 = 4 * P.nside;
       int lo = 1, hi_ = n4 - 1;
@@ -224,7 +226,9 @@ __device__ void halo_geometry(const PaintParams &P, float xh, float yh, float zh
 __device__ __forceinline__ void store_halo(const PaintParams &P, const IngestBuffers &B, long long s,
                                            const HaloRec &H, unsigned long long &fsrows) {
   B.halos[s] = H;
-  B.nring[s] = H.ir_hi >= H.ir_lo ? (unsigned)(H.ir_hi - H.ir_lo + 1) : 0u;
+  /* items are made at ingest for the large halos only; the sweep enumerates the others */
+  int nr = H.ir_hi - H.ir_lo + 1;
+  B.nring[s] = nr > P.big_rings ? (unsigned)nr : 0u;
   if (H.jmin <= H.jmax && H.kmin <= H.kmax) fsrows += (unsigned long long)(H.kmax - H.kmin + 1);
 }
 
@@ -296,42 +300,6 @@ __global__ void __launch_bounds__(256) k_setup_prepared(PaintParams P, IngestBuf
 
 /* --------------------------------------------------------------------- scans ----- */
 
-/* exclusive scan of n uint32 in one block; out[i] int64; *total = sum */
-__global__ void __launch_bounds__(1024) k_scan_single(const unsigned int *in, long long *out,
-                                                      long long n, unsigned long long *total) {
-  __shared__ long long warp_sums[32];
-  __shared__ long long carry;
-  if (threadIdx.x == 0) carry = 0;
-  __syncthreads();
-  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  for (long long base = 0; base < n; base += blockDim.x) {
-    long long i = base + threadIdx.x;
-    long long v = i < n ? (long long)in[i] : 0;
-    long long x = v;
-    for (int o = 1; o < 32; o <<= 1) {
-      long long y = __shfl_up_sync(FULL, x, o);
-      if (lane >= o) x += y;
-    }
-    if (lane == 31) warp_sums[wid] = x;
-    __syncthreads();
-    if (wid == 0) {
-      long long ws = lane < (int)(blockDim.x >> 5) ? warp_sums[lane] : 0;
-      for (int o = 1; o < 32; o <<= 1) {
-        long long y = __shfl_up_sync(FULL, ws, o);
-        if (lane >= o) ws += y;
-      }
-      warp_sums[lane] = ws;
-    }
-    __syncthreads();
-    long long wofs = wid > 0 ? warp_sums[wid - 1] : 0;
-    if (i < n) out[i] = carry + wofs + x - v;
-    __syncthreads();
-    if (threadIdx.x == blockDim.x - 1) carry += wofs + x;
-    __syncthreads();
-  }
-  if (threadIdx.x == 0 && total) *total = (unsigned long long)carry;
-}
-
 #define SCAN_BLOCKS 1024
 
 __global__ void __launch_bounds__(256) k_scan_partial(const unsigned int *in,
@@ -400,21 +368,48 @@ __global__ void __launch_bounds__(256) k_scan_apply(const unsigned int *in,
 
 /* --------------------------------------------------------------- ingest: items ----- */
 
-/* candidate span of ring `ring` of halo H: every pixel centre with chord^2 <= C_span
-   (a disc 2e-5 wider than dtheta) lies in [lo, lo+count); FP32 with a margin */
-__device__ __forceinline__ RingItem make_item(const PaintParams &P, const HaloRec &H, int h,
+/* a disc centre as the span construction reads it */
+struct DiscGeom {
+  float zh, zl, sh, sl, ph, pl, cspan;
+  int irlo;
+};
+
+__device__ __forceinline__ DiscGeom geom_of(const HaloRec &H) {
+  DiscGeom g;
+  g.zh = H.z0h;
+  g.zl = H.z0l;
+  g.sh = H.s0h;
+  g.sl = H.s0l;
+  g.ph = H.p0h;
+  g.pl = H.p0l;
+  g.cspan = H.C_span;
+  g.irlo = H.ir_lo;
+  return g;
+}
+
+/* Candidate span of ring `ring` of a disc: every pixel centre with chord^2 <= C_span (a
+   disc 2e-5 wider than dtheta) lies in [lo, lo+count).  FP32 only: the centre's z,
+   sin(theta) and phi/2pi are (hi, lo) pairs like the ring table's z and sin(theta), so
+   the differences lose nothing to cancellation (close hi parts subtract exactly), and
+   phi0 npr / 2pi is carried as an exact two-product.  The span keeps a margin of 0.02
+   pixel + 1e-5 of its half-width over the FP32 rounding of its centre (< 2e-3 pixel). */
+__device__ __forceinline__ RingItem make_item(const PaintParams &P, const DiscGeom &g, int h,
                                               int ring) {
   RingItem it;
-  double2 zs = P.ringtab[ring];
-  double dz = zs.x - H.z0, ds = zs.y - H.sth0;
-  float A = (float)(dz * dz + ds * ds);
-  float Bc = (float)(4.0 * zs.y * H.sth0);
+  const float4 zs = P.ringtab[ring];
+  const float dz = __fadd_rn(__fsub_rn(zs.x, g.zh), __fsub_rn(zs.y, g.zl));
+  const float ds = __fadd_rn(__fsub_rn(zs.z, g.sh), __fsub_rn(zs.w, g.sl));
+  const float A = __fadd_rn(__fmul_rn(dz, dz), __fmul_rn(ds, ds));
+  const float Bc = __fmul_rn(4.0f, __fmul_rn(zs.z, g.sh));
   int npr, kshift;
   long long npn;
   p2m_ring_info(P.nside, ring, &npr, &kshift, &npn);
-  double q = H.phi0f * (double)npr;
-  double sh = 0.5 * kshift;
-  float cspan = H.C_span;
+  const float fn = (float)npr;
+  /* q = phi0 npr / 2pi = qh + ql */
+  const float qh = __fmul_rn(g.ph, fn);
+  const float ql = __fmaf_rn(g.pl, fn, __fmaf_rn(g.ph, fn, -qh));
+  const float sh = kshift ? 0.5f : 0.0f;
+  const float cspan = g.cspan;
   int lo = 0, cnt = 0;
   bool full = false, empty = false;
   float hw = 0.0f;
@@ -425,38 +420,46 @@ __device__ __forceinline__ RingItem make_item(const PaintParams &P, const HaloRe
     float t = (cspan - A) / Bc;
     if (t <= 0.0f) empty = true;
     else if (t >= 1.0f) full = true;
-    else hw = asinf(sqrtf(t)) * ((float)npr * 0.318309886f);
+    else hw = asinf(sqrtf(t)) * (fn * 0.318309886f);
   }
   if (!empty) {
-    double eps = 0.02 + 1e-5 * (double)hw;
+    const float c = __fadd_rn(__fsub_rn(qh, sh), ql); /* span centre, index units */
     if (!full) {
-      long long l = (long long)ceil(q - sh - (double)hw - eps);
-      long long hh = (long long)floor(q - sh + (double)hw + eps);
-      if (hh - l + 1 >= npr) full = true;
+      const float eps = 0.02f + 1e-5f * hw;
+      const float l = ceilf(c - hw - eps), hh = floorf(c + hw + eps);
+      if (hh - l + 1.0f >= fn) full = true;
       else if (hh >= l) {
         lo = (int)l;
-        cnt = (int)(hh - l + 1);
+        cnt = (int)(hh - l) + 1;
       }
     }
     if (full) {
-      lo = (int)ceil(q - sh - 0.5 * (double)npr);
+      lo = (int)ceilf(c - 0.5f * fn);
       cnt = npr;
     }
   }
-  double x0 = ((double)lo + sh) - q;
-  double n0 = rint(x0); /* |n0| <= npr/2 + 1 <= 16385: fits 16 bits */
+  /* x0 = lo + sh - q = n0 + f0 with n0 = lo - a + rf, a = rint(qh) (qh - a exact) and rf the
+     integer nearest to sh - (qh - a) - ql.  f0 = ((sh - rf) - d) - ql: sh - rf is exact and
+     each subtraction rounds relative to its own result, so f0 keeps full relative precision
+     however close the candidates come to the centre's longitude.  |n0| <= npr/2 + 1. */
+  const float a = rintf(qh);
+  const float d = __fsub_rn(qh, a);
+  const float rf = rintf(__fsub_rn(__fsub_rn(sh, d), ql));
+  const float f0 = __fsub_rn(__fsub_rn(sh - rf, d), ql);
+  const int n0 = lo - (int)a + (int)rf;
   it.halo = h;
-  it.ring_n0 = (ring << 16) | ((int)n0 & 0xffff);
+  it.ring_n0 = (ring << 16) | (n0 & 0xffff);
   it.lo = lo;
   it.count = cnt;
   it.A = A;
   it.B = Bc;
-  it.f0 = (float)(x0 - n0);
-  it.hdphi = 3.14159265358979f / (float)npr;
+  it.f0 = f0;
+  it.hdphi = 3.14159265358979f / fn;
   return it;
 }
 
-/* one warp expands 32 consecutive halos into their (halo, ring) items */
+/* one warp expands 32 consecutive halos into their (halo, ring) items; only the large
+   halos have rings here (nring 0 for the others) */
 __global__ void __launch_bounds__(256) k_items(PaintParams P, IngestBuffers B) {
   const long long n = (long long)B.ctr->n_surv;
   const int lane = threadIdx.x & 31;
@@ -482,12 +485,8 @@ __global__ void __launch_bounds__(256) k_items(PaintParams P, IngestBuffers B) {
       if (act) {
         long long hh = h0 + j;
         const HaloRec &H = B.halos[hh];
-        int ring = H.ir_lo + (t - relj);
-        RingItem it = make_item(P, H, (int)(B.halo_base + hh), ring);
-        B.items[off0 + t] = it;
-        int band = P.band_of_ring[ring];
-        unsigned grp = __match_any_sync(__activemask(), band);
-        if ((int)(__ffs(grp) - 1) == lane) atomicAdd(&B.band_hist[band], (unsigned)__popc(grp));
+        B.items[off0 + t] =
+            make_item(P, geom_of(H), (int)(B.halo_base + hh), H.ir_lo + (t - relj));
       }
     }
   }
@@ -617,7 +616,7 @@ __device__ __forceinline__ void deposit_maps(const PaintParams &P, const HotHalo
         any = true;
       }
     }
-    if (any) W->tiles[slot >> 8] = 1;
+    if (any) W->tiles[slot >> P2M_TILE_SHIFT] = 1;
   } else {
     float *a = (float *)acc + 2 * slot * P.nmaps;
     float olds[P2M_MAXMAPS];
@@ -671,109 +670,6 @@ __global__ void __launch_bounds__(256) k_paint_fs(PaintParams P, IngestBuffers B
     }
   }
   warp_count(&B.ctr->fs_updates, nupd);
-}
-
-/* ------------------------------------------------------------ sweep: grouping ----- */
-
-__global__ void __launch_bounds__(256) k_band_scatter(PaintParams P, const RingItem *in, long long n,
-                                                      const long long *band_start,
-                                                      unsigned int *band_cursor, RingItem *out,
-                                                      unsigned int *counts) {
-  const int lane = threadIdx.x & 31;
-  for (long long base = (long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < n;
-       base += (long long)gridDim.x * blockDim.x) {
-    long long g = base + lane;
-    bool act = g < n;
-    RingItem it;
-    int band = -1 - lane; /* distinct keys for inactive lanes */
-    if (act) {
-      it = in[g];
-      band = P.band_of_ring[item_ring(it)];
-    }
-    unsigned grp = __match_any_sync(FULL, band);
-    int leader = __ffs(grp) - 1;
-    unsigned k0 = 0;
-    if (act && lane == leader) k0 = atomicAdd(&band_cursor[band], (unsigned)__popc(grp));
-    k0 = __shfl_sync(FULL, k0, leader);
-    if (act) {
-      long long pos = band_start[band] + k0 + __popc(grp & ((1u << lane) - 1u));
-      out[pos] = it;
-      counts[pos] = (unsigned)it.count;
-    }
-  }
-}
-
-/* unit queue of the sweep.  Segments: P_0 .. P_{L-1}, then P_b, D_{b-L} for b = L..B-1,
-   then D_{B-L} .. D_{B-1} (P_b: paint units of band b, D_b: drain units, L = P2M_LAG).
-   D_b waits for P_b; P_b waits for D_{b-NBUF}, which is queued L+... segments earlier
-   (L < NBUF), so every wait is on units claimed before it. */
-__global__ void k_units(SweepBuffers W, long long *band_item0, long long *band_cand0, int *seg_start,
-                        int *seg_code, int *unit_target, int *band_chunk0,
-                        const long long *band_pix0, const unsigned long long *n_pix,
-                        unsigned long long *n_chunks) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  const int nb = W.nbands;
-  const long long ni = W.n_items;
-  const long long np = (long long)*n_pix;
-  for (int b = 0; b <= nb; b++) {
-    long long i0 = band_item0[b];
-    band_cand0[b] = (b == nb || i0 >= ni) ? np : W.pix_off[i0];
-  }
-  int ch = 0;
-  for (int b = 0; b < nb; b++) {
-    long long c = band_cand0[b + 1] - band_cand0[b];
-    band_chunk0[b] = ch;
-    int nck = (int)((c + P2M_WARP_CHUNK - 1) / P2M_WARP_CHUNK);
-    ch += nck;
-    unit_target[b] = nck;
-    long long px = band_pix0[b + 1] - band_pix0[b];
-    unit_target[nb + b] = (int)((px + P2M_DRAIN_UNIT - 1) / P2M_DRAIN_UNIT);
-  }
-  band_chunk0[nb] = ch;
-  *n_chunks = (unsigned long long)ch;
-  int k = 0, acc = 0;
-  for (int b = 0; b < nb + P2M_LAG; b++) {
-    if (b < nb) {
-      seg_start[k] = acc;
-      seg_code[k] = b;
-      acc += unit_target[b];
-      k++;
-    }
-    int d = b - P2M_LAG;
-    if (d >= 0) {
-      seg_start[k] = acc;
-      seg_code[k] = d | (1 << 30);
-      acc += unit_target[nb + d];
-      k++;
-    }
-  }
-  seg_start[k] = acc;
-}
-
-/* first item of every warp chunk (P2M_WARP_CHUNK candidates of one band) */
-__global__ void __launch_bounds__(256) k_chunk_starts(SweepBuffers W, const long long *band_item0,
-                                                      const long long *band_cand0,
-                                                      const int *band_chunk0, long long *chunk_g0,
-                                                      long long cap) {
-  const long long n = min((long long)*W.n_chunks, cap);
-  const int nb = W.nbands;
-  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n;
-       t += (long long)gridDim.x * blockDim.x) {
-    int lo = 0, hi = nb; /* band: largest b with band_chunk0[b] <= t */
-    while (hi - lo > 1) {
-      int mid = (lo + hi) >> 1;
-      if (band_chunk0[mid] <= t) lo = mid;
-      else hi = mid;
-    }
-    long long c = band_cand0[lo] + (t - band_chunk0[lo]) * P2M_WARP_CHUNK;
-    long long a = band_item0[lo], b = band_item0[lo + 1]; /* largest g in [a, b) with off <= c */
-    while (b - a > 1) {
-      long long mid = (a + b) >> 1;
-      if (W.pix_off[mid] <= c) a = mid;
-      else b = mid;
-    }
-    chunk_g0[t] = a;
-  }
 }
 
 /* ---------------------------------------------------------- sweep: the painting ----- */
@@ -889,13 +785,13 @@ struct CacheEnt {
   HotHalo h;
 };
 
-/* one candidate pixel: decision (exact or mixed) and deposit into acc at slot pix - pix0 */
+/* one candidate pixel (the k-th of item it, halo fields H): decision (exact or mixed)
+   and deposit at map pixel pix */
 template <int EXACT, int ACC>
 __device__ __forceinline__ void paint_pixel(const PaintParams &P, const SweepBuffers &W,
-                                            const CacheEnt &ce, int k, long long pix, void *acc,
-                                            long long pix0, unsigned long long &nupd,
+                                            const RingItem &it, const HotHalo &H, int k,
+                                            long long pix, unsigned long long &nupd,
                                             unsigned long long &nrc) {
-  const HotHalo &H = ce.h;
   int ir = 0;
   float fr = 0.0f, u = 0.0f;
   bool zero_val = H.zero;
@@ -903,9 +799,9 @@ __device__ __forceinline__ void paint_pixel(const PaintParams &P, const SweepBuf
   if (EXACT) {
     d = 2;
   } else {
-    d = fast_decide(P, ce.it, H, k, ir, fr, zero_val, u);
+    d = fast_decide(P, it, H, k, ir, fr, zero_val, u);
     if (P.flags & 8) { /* validation: compare every fast decision with the exact path */
-      ExactRes e = exact_eval(P, W.halos[ce.it.halo], pix);
+      ExactRes e = exact_eval(P, W.halos[it.halo], pix);
       atomicAdd(&W.ctr->val_checked, 1ull);
       if (d != 2) {
         if ((d == 1) != e.inside) atomicAdd(&W.ctr->val_bad_set, 1ull);
@@ -919,7 +815,7 @@ __device__ __forceinline__ void paint_pixel(const PaintParams &P, const SweepBuf
   if (d == 0) return;
   if (d == 2) {
     if (!EXACT) nrc++;
-    ExactRes e = exact_eval(P, W.halos[ce.it.halo], pix);
+    ExactRes e = exact_eval(P, W.halos[it.halo], pix);
     if (!e.inside) return;
     zero_val = e.zero;
     ir = e.ir;
@@ -927,8 +823,8 @@ __device__ __forceinline__ void paint_pixel(const PaintParams &P, const SweepBuf
   }
   nupd++;
   if (P.flags & 1)
-    record_set(W.set_rec, W.set_pix, W.set_cap, &W.ctr->n_sets, W.halos[ce.it.halo].rec, pix);
-  if (!zero_val && !H.zero) deposit_maps<ACC>(P, H, acc, pix - pix0, ir, fr, &W);
+    record_set(W.set_rec, W.set_pix, W.set_cap, &W.ctr->n_sets, W.halos[it.halo].rec, pix);
+  if (!zero_val && !H.zero) deposit_maps<ACC>(P, H, W.acc, pix, ir, fr, &W);
 }
 
 /* loads items g0..g0+31 (below ihi) and their halos' hot fields into the warp's cache */
@@ -945,18 +841,28 @@ __device__ __forceinline__ void fill_cache(const SweepBuffers &W, CacheEnt *cach
   __syncwarp();
 }
 
-/* walk candidates [p0, p1) of items [ilo, ihi): one warp; EXACT 1 decides every candidate
-   by the exact path, EXACT 0 by the mixed-precision path; deposits go to acc at slot
-   pix - pix0.  The 32 items around the current candidates, with their halos' fields, sit
-   in the warp's shared-memory cache, loaded once per window. */
+/* map pixel of the k-th candidate of item it */
+__device__ __forceinline__ long long item_pixel(const PaintParams &P, const RingItem &it, int k) {
+  int npr, kshift;
+  long long npn;
+  p2m_ring_info(P.nside, item_ring(it), &npr, &kshift, &npn);
+  int iphi = it.lo + k;
+  if (iphi < 0) iphi += npr;
+  if (iphi >= npr) iphi -= npr;
+  return npn - npr + iphi;
+}
+
+/* walk candidates [p0, p1) of items [0, ihi): one warp; EXACT 1 decides every candidate
+   by the exact path, EXACT 0 by the mixed-precision path.  The 32 items around the
+   current candidates, with their halos' fields, sit in the warp's shared-memory cache,
+   loaded once per window. */
 template <int EXACT, int ACC>
 __device__ void walk_candidates(const PaintParams &P, const SweepBuffers &W, long long p0,
-                                long long p1, long long ilo, long long ihi, void *acc,
-                                long long pix0, unsigned long long &nupd,
-                                unsigned long long &nrc, long long g_start, CacheEnt *cache) {
+                                long long p1, long long ihi, unsigned long long &nupd,
+                                unsigned long long &nrc, CacheEnt *cache) {
   const int lane = threadIdx.x & 31;
   const long long *off = W.pix_off;
-  long long g0 = g_start >= 0 ? g_start : warp_upper(off, ilo, ihi, p0);
+  long long g0 = warp_upper(off, 0, ihi, p0);
   long long woff = (g0 + lane < ihi) ? off[g0 + lane] : (1LL << 62);
   long long wend = (g0 + 32 < ihi) ? off[g0 + 32] : (1LL << 62);
   fill_cache(W, cache, g0, ihi);
@@ -974,7 +880,7 @@ __device__ void walk_candidates(const PaintParams &P, const SweepBuffers &W, lon
       unsigned m = __ballot_sync(FULL, woff <= pmin);
       int j0 = m ? 31 - __clz(m) : -1;
       if (j0 != 0 || pmin >= wend) {
-        if (j0 < 0 || pmin >= wend) g0 = warp_upper(off, ilo, ihi, pmin);
+        if (j0 < 0 || pmin >= wend) g0 = warp_upper(off, 0, ihi, pmin);
         else g0 += j0;
         woff = (g0 + lane < ihi) ? off[g0 + lane] : (1LL << 62);
         wend = (g0 + 32 < ihi) ? off[g0 + 32] : (1LL << 62);
@@ -992,192 +898,15 @@ __device__ void walk_candidates(const PaintParams &P, const SweepBuffers &W, lon
         todo = false;
         const CacheEnt &ce = cache[j];
         int k = (int)(p - ooff);
-        int npr, kshift;
-        long long npn;
-        p2m_ring_info(P.nside, item_ring(ce.it), &npr, &kshift, &npn);
-        int iphi = ce.it.lo + k;
-        if (iphi < 0) iphi += npr;
-        if (iphi >= npr) iphi -= npr;
-        paint_pixel<EXACT, ACC>(P, W, ce, k, npn - npr + iphi, acc, pix0, nupd, nrc);
+        paint_pixel<EXACT, ACC>(P, W, ce.it, ce.h, k, item_pixel(P, ce.it, k), nupd, nrc);
       }
     }
   }
 }
 
-/* bounded wait for *flag >= target (one lane); false on abort or timeout */
-__device__ bool wait_geq(const unsigned *flag, unsigned target, DevCounters *ctr) {
-  for (long it = 0; it < (1L << 23); it++) {
-    if (ld_acquire(flag) >= target) {
-      if (it) atomicAdd(&ctr->sw_wait_polls, (unsigned long long)it);
-      return true;
-    }
-    if (ld_acquire(&ctr->abort)) return false;
-    __nanosleep(200);
-  }
-  atomicOr(&ctr->err, (unsigned)P2M_DEVERR_TIMEOUT);
-  atomicExch(&ctr->abort, 1u);
-  return false;
-}
-
-#define MAX_SEG 4096
-#define SWEEP_WARPS (P2M_SWEEP_THREADS / 32)
-
-/* warp-reduced add of v into a shared-memory double */
-__device__ __forceinline__ void warp_sum_to(double *dst, double v) {
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(FULL, v, o);
-  if ((threadIdx.x & 31) == 0 && v != 0.0) atomicAdd(dst, v);
-}
-
-/* one warp drains window slice [q0, q1): float maps out, window cleared, map sums into
-   s_sum; eight window loads in flight per lane */
-template <int ACC>
-__device__ __forceinline__ void drain_slice(const PaintParams &P, const SweepBuffers &W, float2 *win,
-                                            long long pix0, long long q0, long long q1,
-                                            double *s_sum) {
-  const int lane = threadIdx.x & 31;
-  if (P.nmaps == 2) {
-    double m0 = 0.0, m1 = 0.0;
-    float4 *w4 = (float4 *)win; /* (hi0, lo0, hi1, lo1) or (double0, double1) per pixel */
-    for (long long p = q0 + lane; p < q1; p += 8 * 32) {
-      float4 a[8];
-#pragma unroll
-      for (int u = 0; u < 8; u++)
-        if (p + u * 32 < q1) a[u] = __ldcg(w4 + (p + u * 32 - pix0));
-#pragma unroll
-      for (int u = 0; u < 8; u++) {
-        long long q = p + u * 32;
-        if (q >= q1) break;
-        float v0, v1;
-        if (ACC == 0) {
-          double2 d = *reinterpret_cast<double2 *>(&a[u]);
-          v0 = (float)d.x;
-          v1 = (float)d.y;
-        } else {
-          v0 = __fadd_rn(a[u].x, a[u].y);
-          v1 = __fadd_rn(a[u].z, a[u].w);
-        }
-        if (W.accumulate) {
-          v0 = __fadd_rn(W.out[0][q], v0);
-          v1 = __fadd_rn(W.out[1][q], v1);
-        }
-        __stcs(W.out[0] + q, v0);
-        __stcs(W.out[1] + q, v1);
-        __stcg(w4 + (q - pix0), make_float4(0.0f, 0.0f, 0.0f, 0.0f));
-        m0 += (double)v0;
-        m1 += (double)v1;
-      }
-    }
-    warp_sum_to(s_sum, m0);
-    warp_sum_to(s_sum + 1, m1);
-    return;
-  }
-  for (int m = 0; m < P.nmaps; m++) {
-    double ms = 0.0;
-    for (long long p = q0 + lane; p < q1; p += 32) {
-      long long e = (p - pix0) * P.nmaps + m;
-      float v;
-      if (ACC == 0) {
-        double *wd = (double *)win;
-        v = (float)__ldcg(wd + e);
-        __stcg(wd + e, 0.0);
-      } else {
-        float2 a = __ldcg(win + e);
-        v = __fadd_rn(a.x, a.y);
-        __stcg(win + e, make_float2(0.0f, 0.0f));
-      }
-      float *o = W.out[m] + p;
-      if (W.accumulate) v = __fadd_rn(*o, v);
-      __stcs(o, v);
-      ms += (double)v;
-    }
-    warp_sum_to(s_sum + m, ms);
-  }
-}
-
-/* persistent sweep: every warp claims units in queue order (see k_units), waits only for
-   the units its unit depends on, and signals its own completion; there are no block-wide
-   barriers inside the loop */
-template <int ACC>
-__global__ void __launch_bounds__(P2M_SWEEP_THREADS, P2M_SWEEP_MINBLOCKS) k_sweep(PaintParams P,
-                                                                                 SweepBuffers W) {
-  __shared__ int s_seg[MAX_SEG + 1];
-  __shared__ double s_sum[P2M_MAXMAPS];
-  __shared__ CacheEnt s_cache[SWEEP_WARPS][32];
-  const int nseg = 2 * W.nbands;
-  for (int k = threadIdx.x; k <= nseg; k += blockDim.x) s_seg[k] = W.seg_start[k];
-  if (threadIdx.x < P2M_MAXMAPS) s_sum[threadIdx.x] = 0.0;
-  __syncthreads();
-  const int total = s_seg[nseg];
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  CacheEnt *cache = s_cache[wid];
-  unsigned long long nupd = 0, nrc = 0, ncand = 0;
-  for (;;) {
-    int u = 0;
-    if (lane == 0) u = ld_acquire(&W.ctr->abort) ? total : (int)atomicAdd(&W.ctr->next_unit, 1u);
-    u = __shfl_sync(FULL, u, 0);
-    if (u >= total) break;
-    int lo = 0, hi = nseg; /* largest seg with s_seg[seg] <= u */
-    while (hi - lo > 1) {
-      int mid = (lo + hi) >> 1;
-      if (s_seg[mid] <= u) lo = mid;
-      else hi = mid;
-    }
-    const int code = W.seg_code[lo];
-    const int band = code & 0x3fffffff;
-    const bool drain = (code >> 30) & 1;
-    const int k = u - s_seg[lo];
-    float2 *win = W.win + (long long)(band % P2M_NBUF) * W.wpix * P.nmaps;
-    const long long pix0 = W.band_pix0[band];
-    int ok = 1;
-    if (lane == 0) {
-      if (!drain && band >= P2M_NBUF)
-        ok = wait_geq(&W.drain_done[band - P2M_NBUF],
-                      (unsigned)W.unit_target[W.nbands + band - P2M_NBUF], W.ctr);
-      if (drain) ok = wait_geq(&W.paint_done[band], (unsigned)W.unit_target[band], W.ctr);
-      __threadfence();
-    }
-    ok = __shfl_sync(FULL, ok, 0);
-    if (!ok) break;
-    const long long t_unit = clock64();
-    if (!drain) {
-      const long long t = (long long)W.band_chunk0[band] + k;
-      long long a = W.band_cand0[band] + (long long)k * P2M_WARP_CHUNK;
-      long long b = min(a + P2M_WARP_CHUNK, W.band_cand0[band + 1]);
-      walk_candidates<0, ACC>(P, W, a, b, W.band_item0[band], W.band_item0[band + 1], (void *)win,
-                              pix0, nupd, nrc, t < W.chunk_cap ? W.chunk_g0[t] : -1, cache);
-      if (lane == 0) ncand += (unsigned long long)(b - a);
-      __threadfence();
-      __syncwarp();
-      if (lane == 0) {
-        atomicAdd(&W.paint_done[band], 1u);
-        atomicAdd(&W.ctr->sw_paint_cycles, (unsigned long long)(clock64() - t_unit));
-        atomicAdd(&W.ctr->sw_paint_units, 1ull);
-      }
-    } else {
-      long long q0 = pix0 + (long long)k * P2M_DRAIN_UNIT;
-      long long q1 = min(q0 + P2M_DRAIN_UNIT, W.band_pix0[band + 1]);
-      drain_slice<ACC>(P, W, win, pix0, q0, q1, s_sum);
-      __threadfence();
-      __syncwarp();
-      if (lane == 0) {
-        atomicAdd(&W.drain_done[band], 1u);
-        atomicAdd(&W.ctr->sw_drain_cycles, (unsigned long long)(clock64() - t_unit));
-        atomicAdd(&W.ctr->sw_drain_units, 1ull);
-      }
-    }
-  }
-  __syncthreads();
-  block_count(&W.ctr->hp_updates, nupd);
-  block_count(&W.ctr->n_recheck, nrc);
-  block_count(&W.ctr->n_cand, ncand);
-  __syncthreads();
-  if (threadIdx.x < P.nmaps && s_sum[threadIdx.x] != 0.0)
-    atomicAdd(W.sums + threadIdx.x, s_sum[threadIdx.x]);
-}
-
-/* full-sky accumulation: every warp walks 1024-candidate chunks of the whole (ring-band
-   ordered) candidate space; EXACT 1 is the plain FP64 path, EXACT 0 the mixed path.
-   ACC 0: FP64 accumulator, ACC 1: two-float accumulator (8 bytes per map and pixel). */
+/* the large halos' items: every warp walks 1024-candidate chunks of their candidate
+   space.  EXACT 1 is the plain FP64 path, EXACT 0 the mixed path; ACC 0 deposits into the
+   FP64 accumulator, ACC 2 into the maps with compensation. */
 template <int EXACT, int ACC>
 __global__ void __launch_bounds__(256) k_paint_full(PaintParams P, SweepBuffers W) {
   __shared__ CacheEnt s_cache[8][32];
@@ -1190,7 +919,7 @@ __global__ void __launch_bounds__(256) k_paint_full(PaintParams P, SweepBuffers 
   unsigned long long nupd = 0, nrc = 0, ncand = 0;
   for (long long c = warp; c * chunk < npix_c; c += nwarps) {
     long long p0 = c * chunk, p1 = min(npix_c, p0 + chunk);
-    walk_candidates<EXACT, ACC>(P, W, p0, p1, 0, W.n_items, W.acc, 0, nupd, nrc, -1, cache);
+    walk_candidates<EXACT, ACC>(P, W, p0, p1, W.n_items, nupd, nrc, cache);
     if ((threadIdx.x & 31) == 0) ncand += (unsigned long long)(p1 - p0);
   }
   warp_count(&W.ctr->hp_updates, nupd);
@@ -1198,101 +927,186 @@ __global__ void __launch_bounds__(256) k_paint_full(PaintParams P, SweepBuffers 
   warp_count(&W.ctr->n_cand, ncand);
 }
 
-/* full-sky accumulator -> float maps in one pass over all maps, map sums, and the
-   accumulator cleared for the next paint */
-template <int ACC>
-__global__ void __launch_bounds__(256) k_finalize_full(void *acc, long long npix, int nmaps,
+/* warp-wide inclusive prefix sum */
+__device__ __forceinline__ int warp_incl_scan(int v) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    int y = __shfl_up_sync(FULL, v, o);
+    if (lane >= o) v += y;
+  }
+  return v;
+}
+
+/* largest lane j with key_j <= t, for keys non-decreasing over the lanes (key_0 <= t) */
+__device__ __forceinline__ int warp_find(int key, int t) {
+  int j = 0;
+#pragma unroll
+  for (int step = 16; step > 0; step >>= 1) {
+    int o = __shfl_sync(FULL, key, j + step);
+    if (o <= t) j += step;
+  }
+  return j;
+}
+
+/* Enumeration fused with painting for the halos spanning at most big_rings rings.
+   A warp claims 32 consecutive halos and prefix-sums their ring counts in registers;
+   each lane builds the candidate span of one (halo, ring) item; the warp prefix-sums
+   those spans and paints their candidates 32 at a time, each lane fetching its item's
+   fields from the lane that built it.  The halos' interpolation fields sit in shared
+   memory.  Nothing is written to memory between the stages. */
+template <int EXACT, int ACC>
+__global__ void __launch_bounds__(256) k_paint_halos(PaintParams P, SweepBuffers W) {
+  __shared__ HotHalo s_hot[8][32];
+  const int lane = threadIdx.x & 31;
+  HotHalo *hot = s_hot[(threadIdx.x >> 5) & 7];
+  const long long nh = W.n_halos;
+  unsigned long long nupd = 0, nrc = 0, ncand = 0;
+  for (;;) {
+    long long h0 = 0;
+    if (lane == 0) h0 = 32LL * (long long)atomicAdd(&W.ctr->next_unit, 1u);
+    h0 = __shfl_sync(FULL, h0, 0);
+    if (h0 >= nh) break;
+    DiscGeom g;
+    g.zh = g.zl = g.sh = g.sl = g.ph = g.pl = g.cspan = 0.0f;
+    g.irlo = 0;
+    int nr = 0;
+    __syncwarp();
+    if (h0 + lane < nh) {
+      const HaloRec &H = W.halos[h0 + lane];
+      int r = H.ir_hi - H.ir_lo + 1;
+      if (r > 0 && r <= P.big_rings) {
+        nr = r;
+        g = geom_of(H);
+        hot[lane] = hot_of(H);
+      }
+    }
+    __syncwarp();
+    const int rx = warp_incl_scan(nr);
+    const int rel = rx - nr, total = __shfl_sync(FULL, rx, 31);
+    for (int t0 = 0; t0 < total; t0 += 32) {
+      /* item t of the batch: ring rel_j..rel_j+nr_j-1 of halo lane j */
+      const int t = t0 + lane;
+      const int j = warp_find(rel, t);
+      DiscGeom gj;
+      gj.zh = __shfl_sync(FULL, g.zh, j);
+      gj.zl = __shfl_sync(FULL, g.zl, j);
+      gj.sh = __shfl_sync(FULL, g.sh, j);
+      gj.sl = __shfl_sync(FULL, g.sl, j);
+      gj.ph = __shfl_sync(FULL, g.ph, j);
+      gj.pl = __shfl_sync(FULL, g.pl, j);
+      gj.cspan = __shfl_sync(FULL, g.cspan, j);
+      const int ring = __shfl_sync(FULL, g.irlo, j) + t - __shfl_sync(FULL, rel, j);
+      RingItem it;
+      it.count = 0;
+      if (t < total) it = make_item(P, gj, (int)(h0 + j), ring);
+      const int cx = warp_incl_scan(it.count);
+      const int cex = cx - it.count, ctot = __shfl_sync(FULL, cx, 31);
+      for (int c0 = 0; c0 < ctot; c0 += 32) {
+        const int c = c0 + lane;
+        const int i = warp_find(cex, c);
+        RingItem ci;
+        ci.halo = __shfl_sync(FULL, it.halo, i);
+        ci.ring_n0 = __shfl_sync(FULL, it.ring_n0, i);
+        ci.lo = __shfl_sync(FULL, it.lo, i);
+        ci.A = __shfl_sync(FULL, it.A, i);
+        ci.B = __shfl_sync(FULL, it.B, i);
+        ci.f0 = __shfl_sync(FULL, it.f0, i);
+        ci.hdphi = __shfl_sync(FULL, it.hdphi, i);
+        const int jj = __shfl_sync(FULL, j, i);
+        const int k = c - __shfl_sync(FULL, cex, i);
+        if (c < ctot)
+          paint_pixel<EXACT, ACC>(P, W, ci, hot[jj], k, item_pixel(P, ci, k), nupd, nrc);
+      }
+      if (lane == 0) ncand += (unsigned long long)ctot;
+    }
+  }
+  warp_count(&W.ctr->hp_updates, nupd);
+  warp_count(&W.ctr->n_recheck, nrc);
+  warp_count(&W.ctr->n_cand, ncand);
+}
+
+/* candidate counts of items (input of the candidate-offset scan) */
+__global__ void __launch_bounds__(256) k_item_counts(const RingItem *items, long long n,
+                                                     unsigned int *counts) {
+  for (long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x; g < n;
+       g += (long long)gridDim.x * blockDim.x)
+    counts[g] = (unsigned)items[g].count;
+}
+
+/* FP64 accumulator -> float maps in one pass over all maps (added to the maps after the
+   first sweep since the reset); the accumulator is cleared for the next paint */
+__global__ void __launch_bounds__(256) k_finalize_full(double *acc, long long npix, int nmaps,
                                                        float *o0, float *o1, float *o2, float *o3,
                                                        float *o4, float *o5, float *o6, float *o7,
-                                                       int accumulate, double *sums) {
+                                                       int accumulate) {
   float *outs[8] = {o0, o1, o2, o3, o4, o5, o6, o7};
-  double s[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   const long long stride = (long long)gridDim.x * blockDim.x;
   if (nmaps == 2) {
-    float4 *a4 = (float4 *)acc; /* (double0, double1) or (hi0, lo0, hi1, lo1) */
+    double2 *a2 = (double2 *)acc;
     for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < npix; p += 4 * stride) {
-      float4 a[4];
+      double2 a[4];
 #pragma unroll
       for (int u = 0; u < 4; u++)
-        if (p + u * stride < npix) a[u] = __ldcs(a4 + p + u * stride);
+        if (p + u * stride < npix) a[u] = __ldcs(a2 + p + u * stride);
 #pragma unroll
       for (int u = 0; u < 4; u++) {
         long long q = p + u * stride;
         if (q >= npix) break;
-        float v0, v1;
-        if (ACC == 0) {
-          double2 d = *reinterpret_cast<double2 *>(&a[u]);
-          v0 = (float)d.x;
-          v1 = (float)d.y;
-        } else {
-          v0 = __fadd_rn(a[u].x, a[u].y);
-          v1 = __fadd_rn(a[u].z, a[u].w);
-        }
+        float v0 = (float)a[u].x, v1 = (float)a[u].y;
         if (accumulate) {
           v0 = __fadd_rn(o0[q], v0);
           v1 = __fadd_rn(o1[q], v1);
         }
         __stcs(o0 + q, v0);
         __stcs(o1 + q, v1);
-        __stcs(a4 + q, make_float4(0.0f, 0.0f, 0.0f, 0.0f));
-        s[0] += (double)v0;
-        s[1] += (double)v1;
+        __stcs(a2 + q, make_double2(0.0, 0.0));
       }
     }
   } else {
     for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < npix; p += stride) {
       for (int m = 0; m < nmaps; m++) {
-        float v;
-        if (ACC == 0) {
-          double *ad = (double *)acc + p * nmaps + m;
-          v = (float)__ldcs(ad);
-          __stcs(ad, 0.0);
-        } else {
-          float2 *af = (float2 *)acc + p * nmaps + m;
-          float2 a = __ldcs(af);
-          v = __fadd_rn(a.x, a.y);
-          __stcs(af, make_float2(0.0f, 0.0f));
-        }
+        double *ad = acc + p * nmaps + m;
+        float v = (float)__ldcs(ad);
+        __stcs(ad, 0.0);
         if (accumulate) v = __fadd_rn(outs[m][p], v);
         __stcs(outs[m] + p, v);
-        s[m] += (double)v;
       }
     }
-  }
-  for (int m = 0; m < nmaps; m++) {
-    double v = s[m];
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(FULL, v, o);
-    if ((threadIdx.x & 31) == 0 && v != 0.0) atomicAdd(sums + m, v);
   }
 }
 
 /* folds the nonzero low words of the compensated accumulation into the output maps
-   (out = RN(hi + lo)) and clears them; one warp per dirty 256-pixel tile */
+   (out = RN(hi + lo)) and clears them.  A warp reads the flags of 32 consecutive
+   tiles and visits each flagged tile (one pixel per lane) */
 __global__ void __launch_bounds__(256) k_fold_lo(SweepBuffers W, int nmaps) {
   const int lane = threadIdx.x & 31;
-  const long long ntiles = (W.npix + 255) >> 8;
+  const long long ntiles = (W.npix + P2M_TILE_PIX - 1) >> P2M_TILE_SHIFT;
   const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
   for (long long t0 = warp * 32; t0 < ntiles; t0 += nwarps * 32) {
     long long t = t0 + lane;
     bool dirty = t < ntiles && W.tiles[t];
     unsigned m = __ballot_sync(FULL, dirty);
+    if (dirty) W.tiles[t] = 0;
     while (m) {
       int b = __ffs(m) - 1;
       m &= m - 1;
-      long long tt = t0 + b;
-      long long p0 = tt << 8, p1 = min(p0 + 256, W.npix);
-      for (int mp = 0; mp < nmaps; mp++) {
-        float *lo = W.lo + (long long)mp * W.npix;
-        for (long long p = p0 + lane; p < p1; p += 32) {
-          float l = lo[p];
-          if (l != 0.0f) {
-            W.out[mp][p] = __fadd_rn(W.out[mp][p], l);
-            lo[p] = 0.0f;
-          }
+      long long p = ((t0 + b) << P2M_TILE_SHIFT) + lane;
+      if (p >= W.npix) continue;
+      float l[P2M_MAXMAPS], h[P2M_MAXMAPS];
+#pragma unroll
+      for (int mp = 0; mp < P2M_MAXMAPS; mp++)
+        if (mp < nmaps) l[mp] = W.lo[(long long)mp * W.npix + p];
+#pragma unroll
+      for (int mp = 0; mp < P2M_MAXMAPS; mp++)
+        if (mp < nmaps && l[mp] != 0.0f) h[mp] = W.out[mp][p];
+#pragma unroll
+      for (int mp = 0; mp < P2M_MAXMAPS; mp++)
+        if (mp < nmaps && l[mp] != 0.0f) {
+          W.out[mp][p] = __fadd_rn(h[mp], l[mp]);
+          W.lo[(long long)mp * W.npix + p] = 0.0f;
         }
-      }
-      if (lane == 0) W.tiles[tt] = 0;
     }
   }
 }
@@ -1488,43 +1302,20 @@ void p2m_launch_fs(const PaintParams &P, const IngestBuffers &B, long long n_max
   if (P.precision == 1) k_paint_fs<1><<<nsm * 8, 256, 0, s>>>(P, B);
   else k_paint_fs<0><<<nsm * 8, 256, 0, s>>>(P, B);
 }
-void p2m_launch_band_scatter(const PaintParams &P, const RingItem *in, long long n,
-                             const long long *band_start, unsigned int *band_cursor,
-                             RingItem *out, unsigned int *counts, cudaStream_t s, int nsm) {
-  k_band_scatter<<<grid_for(n, 256, nsm, 8), 256, 0, s>>>(P, in, n, band_start, band_cursor, out,
-                                                          counts);
-}
-void p2m_launch_scan_single(const unsigned int *in, long long *out, long long n,
-                            unsigned long long *total, cudaStream_t s) {
-  k_scan_single<<<1, 1024, 0, s>>>(in, out, n, total);
-}
-void p2m_launch_units(const SweepBuffers &W, long long *band_item0, long long *band_cand0,
-                      int *seg_start, int *seg_code, int *unit_target, int *band_chunk0,
-                      long long *chunk_g0, long long chunk_cap, const long long *band_pix0,
-                      unsigned long long *n_pix, cudaStream_t s, int nsm) {
-  k_units<<<1, 32, 0, s>>>(W, band_item0, band_cand0, seg_start, seg_code, unit_target, band_chunk0,
-                           band_pix0, n_pix, W.n_chunks);
-  k_chunk_starts<<<nsm * 4, 256, 0, s>>>(W, band_item0, band_cand0, band_chunk0, chunk_g0, chunk_cap);
-}
-void p2m_launch_sweep(const PaintParams &P, const SweepBuffers &W, cudaStream_t s, int nsm) {
-  /* one resident wave: every block claims units until the queue is empty */
-  int per_sm = 0;
-  if (P.precision == 1) {
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sweep<1>, P2M_SWEEP_THREADS, 0) !=
-            cudaSuccess || per_sm < 1)
-      per_sm = 1;
-    k_sweep<1><<<nsm * per_sm, P2M_SWEEP_THREADS, 0, s>>>(P, W);
-  } else {
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sweep<0>, P2M_SWEEP_THREADS, 0) !=
-            cudaSuccess || per_sm < 1)
-      per_sm = 1;
-    k_sweep<0><<<nsm * per_sm, P2M_SWEEP_THREADS, 0, s>>>(P, W);
-  }
-}
 void p2m_launch_paint_full(const PaintParams &P, const SweepBuffers &W, cudaStream_t s, int nsm) {
   if (P.precision == 0) k_paint_full<1, 0><<<nsm * 8, 256, 0, s>>>(P, W);
   else if (P.precision == 1) k_paint_full<0, 2><<<nsm * 8, 256, 0, s>>>(P, W);
   else k_paint_full<0, 0><<<nsm * 8, 256, 0, s>>>(P, W);
+}
+void p2m_launch_paint_halos(const PaintParams &P, const SweepBuffers &W, cudaStream_t s, int nsm) {
+  /* warps claim 32-halo batches until none is left */
+  if (P.precision == 0) k_paint_halos<1, 0><<<nsm * 8, 256, 0, s>>>(P, W);
+  else if (P.precision == 1) k_paint_halos<0, 2><<<nsm * 8, 256, 0, s>>>(P, W);
+  else k_paint_halos<0, 0><<<nsm * 8, 256, 0, s>>>(P, W);
+}
+void p2m_launch_item_counts(const RingItem *items, long long n, unsigned int *counts,
+                            cudaStream_t s, int nsm) {
+  k_item_counts<<<grid_for(n, 256, nsm, 8), 256, 0, s>>>(items, n, counts);
 }
 void p2m_launch_fold_lo(const PaintParams &P, const SweepBuffers &W, cudaStream_t s, int nsm) {
   k_fold_lo<<<nsm * 8, 256, 0, s>>>(W, P.nmaps);
@@ -1533,16 +1324,10 @@ void p2m_launch_map_sum(const float *map, long long n, double *sum, cudaStream_t
   k_map_sum<<<grid_for(n, 256, nsm, 8), 256, 0, s>>>(map, n, sum);
 }
 void p2m_launch_finalize_full(const PaintParams &P, const void *acc, long long npix,
-                              float *const *out, int accumulate, double *sums, cudaStream_t s,
-                              int nsm) {
-  if (P.precision == 1)
-    k_finalize_full<1><<<grid_for(npix, 256, nsm, 8), 256, 0, s>>>(
-        (void *)acc, npix, P.nmaps, out[0], out[1], out[2], out[3], out[4], out[5], out[6], out[7],
-        accumulate, sums);
-  else
-    k_finalize_full<0><<<grid_for(npix, 256, nsm, 8), 256, 0, s>>>(
-        (void *)acc, npix, P.nmaps, out[0], out[1], out[2], out[3], out[4], out[5], out[6], out[7],
-        accumulate, sums);
+                              float *const *out, int accumulate, cudaStream_t s, int nsm) {
+  k_finalize_full<<<grid_for(npix, 256, nsm, 8), 256, 0, s>>>(
+      (double *)acc, npix, P.nmaps, out[0], out[1], out[2], out[3], out[4], out[5], out[6], out[7],
+      accumulate);
 }
 void p2m_launch_finalize_fs(const PaintParams &P, const void *acc, long long npix, float *out,
                             int map, double *sum, cudaStream_t s, int nsm) {
