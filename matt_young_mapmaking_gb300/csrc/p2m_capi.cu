@@ -182,6 +182,8 @@ PaintParams make_params(const p2m_ctx *ctx, int nfloat) {
     P.map_profile[m] = m < c.nmaps ? c.map_profile[m] : 1;
     if (m < c.nmaps && c.map_profile[m] == 2) P.any_ksz = 1;
   }
+  P.paired = c.nmaps == 2 && c.map_table[0] == c.map_table[1] && c.map_profile[0] == 1 &&
+             c.map_profile[1] == 2;
   P.mass_fac = FMUL(FMUL(4.0f / 3.0f, mypi), ctx->cosmo.rho_0);
   P.th = ctx->th;
   for (int t = 0; t < P2M_MAXTABLES; t++) P.tables[t] = ctx->d_tab[t];
@@ -464,7 +466,10 @@ p2m_status p2m_create(const p2m_config *cfg, p2m_ctx **out) {
   ctx->cfg = *cfg;
   *out = ctx;
   if (const char *e = getenv("P2M_BAND_U")) ctx->band_u = (float)atof(e);
-  /* test hook: route every halo through one painting path (0: stored items only) */
+  /* the plain FP64 path is fastest with every halo on the stored-item path, which balances
+     its heavy per-candidate work over candidates; test hook: P2M_BIG_RINGS routes every
+     halo through one painting path (0: stored items only) */
+  if (cfg->precision == P2M_PREC_FP64) ctx->big_rings = 0;
   if (const char *e = getenv("P2M_BIG_RINGS")) ctx->big_rings = std::max(0, atoi(e));
   CK(cudaSetDevice(cfg->device));
   CK(cudaDeviceGetAttribute(&ctx->nsm, cudaDevAttrMultiProcessorCount, cfg->device));

@@ -92,6 +92,7 @@ struct PaintParams {
   float fov, dpix, hf, cut_low, cut_high, chihview, bbps_delta;
   int map_table[P2M_MAXMAPS], map_profile[P2M_MAXMAPS];
   int any_ksz;
+  int paired;   /* two maps: profiles 1 and 2 of one table */
   float mass_fac; /* (4./3.*mypi)*rho_0 of pks2map.f90:264 */
   p2m_cosmo cosmo;
   p2m_tabhdr th;

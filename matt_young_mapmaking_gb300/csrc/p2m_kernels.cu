@@ -541,11 +541,60 @@ __device__ __forceinline__ HotHalo hot_of(const HaloRec &H) {
   return h;
 }
 
-/* profile values of every map at one pixel (maptable.f90:204-212 with known ir, fr),
-   deposited at slot `slot` of acc (nmaps entries per slot).  ACC 0: FP64 accumulator
+/* adds one pixel's values (nmaps of them) at slot `slot`.  ACC 0: FP64 accumulator
    (fire-and-forget red.add.f64); ACC 1: two-float (hi, lo) FP32 accumulator, hi by an
-   atomic add that returns the old value, lo the exact TwoSum rounding error.  All maps'
-   adds are issued before any result is used. */
+   atomic add that returns the old value, lo the exact TwoSum rounding error; ACC 2:
+   compensated accumulation with the float output map as the high word, the low words
+   sparse (nonzero only where an add rounded) and their tiles flagged.  All maps' adds are
+   issued before any result is used. */
+template <int ACC>
+__device__ __forceinline__ void accumulate_vals(const PaintParams &P, void *acc, long long slot,
+                                                const float *vals, const SweepBuffers *W) {
+  if (ACC == 0) {
+    double *a = (double *)acc + slot * P.nmaps;
+#pragma unroll
+    for (int m = 0; m < P2M_MAXMAPS; m++)
+      if (m < P.nmaps && vals[m] != 0.0f) atomicAdd(a + m, (double)vals[m]);
+  } else if (ACC == 2) {
+    float olds[P2M_MAXMAPS];
+#pragma unroll
+    for (int m = 0; m < P2M_MAXMAPS; m++)
+      olds[m] = (m < P.nmaps && vals[m] != 0.0f) ? atomicAdd(W->out[m] + slot, vals[m]) : 0.0f;
+    bool any = false;
+#pragma unroll
+    for (int m = 0; m < P2M_MAXMAPS; m++) {
+      if (m >= P.nmaps || vals[m] == 0.0f) continue;
+      float old = olds[m], v = vals[m];
+      float sm = __fadd_rn(old, v);
+      float bb = __fsub_rn(sm, old);
+      float err = __fadd_rn(__fsub_rn(old, __fsub_rn(sm, bb)), __fsub_rn(v, bb));
+      if (err != 0.0f) {
+        atomicAdd(W->lo + (long long)m * W->npix + slot, err);
+        any = true;
+      }
+    }
+    if (any) W->tiles[slot >> P2M_TILE_SHIFT] = 1;
+  } else {
+    float *a = (float *)acc + 2 * slot * P.nmaps;
+    float olds[P2M_MAXMAPS];
+#pragma unroll
+    for (int m = 0; m < P2M_MAXMAPS; m++)
+      olds[m] = (m < P.nmaps && vals[m] != 0.0f) ? atomicAdd(a + 2 * m, vals[m]) : 0.0f;
+#pragma unroll
+    for (int m = 0; m < P2M_MAXMAPS; m++) {
+      if (m >= P.nmaps || vals[m] == 0.0f) continue;
+      float old = olds[m], v = vals[m];
+      /* TwoSum: the exact rounding error of old + v, carried in the low word */
+      float sm = __fadd_rn(old, v);
+      float bb = __fsub_rn(sm, old);
+      float err = __fadd_rn(__fsub_rn(old, __fsub_rn(sm, bb)), __fsub_rn(v, bb));
+      if (err != 0.0f) atomicAdd(a + 2 * m + 1, err);
+    }
+  }
+}
+
+/* profile values of every map at one pixel (maptable.f90:204-212 with known ir, fr: the
+   reference's float sequence), deposited at slot `slot` */
 template <int ACC>
 __device__ __forceinline__ void deposit_maps(const PaintParams &P, const HotHalo &H, void *acc,
                                              long long slot, int ir, float fr,
@@ -591,49 +640,45 @@ __device__ __forceinline__ void deposit_maps(const PaintParams &P, const HotHalo
     }
     vals[m] = FMUL(w, v);
   }
-  if (ACC == 0) {
-    double *a = (double *)acc + slot * P.nmaps;
-#pragma unroll
-    for (int m = 0; m < P2M_MAXMAPS; m++)
-      if (m < P.nmaps && vals[m] != 0.0f) atomicAdd(a + m, (double)vals[m]);
-  } else if (ACC == 2) {
-    /* compensated accumulation with the output map as the high word; low words are
-       sparse (nonzero only where an add rounded) and their tiles are flagged */
-    float olds[P2M_MAXMAPS];
-#pragma unroll
-    for (int m = 0; m < P2M_MAXMAPS; m++)
-      olds[m] = (m < P.nmaps && vals[m] != 0.0f) ? atomicAdd(W->out[m] + slot, vals[m]) : 0.0f;
-    bool any = false;
-#pragma unroll
-    for (int m = 0; m < P2M_MAXMAPS; m++) {
-      if (m >= P.nmaps || vals[m] == 0.0f) continue;
-      float old = olds[m], v = vals[m];
-      float sm = __fadd_rn(old, v);
-      float bb = __fsub_rn(sm, old);
-      float err = __fadd_rn(__fsub_rn(old, __fsub_rn(sm, bb)), __fsub_rn(v, bb));
-      if (err != 0.0f) {
-        atomicAdd(W->lo + (long long)m * W->npix + slot, err);
-        any = true;
-      }
-    }
-    if (any) W->tiles[slot >> P2M_TILE_SHIFT] = 1;
-  } else {
-    float *a = (float *)acc + 2 * slot * P.nmaps;
-    float olds[P2M_MAXMAPS];
-#pragma unroll
-    for (int m = 0; m < P2M_MAXMAPS; m++)
-      olds[m] = (m < P.nmaps && vals[m] != 0.0f) ? atomicAdd(a + 2 * m, vals[m]) : 0.0f;
-#pragma unroll
-    for (int m = 0; m < P2M_MAXMAPS; m++) {
-      if (m >= P.nmaps || vals[m] == 0.0f) continue;
-      float old = olds[m], v = vals[m];
-      /* TwoSum: the exact rounding error of old + v, carried in the low word */
-      float s = __fadd_rn(old, v);
-      float bb = __fsub_rn(s, old);
-      float err = __fadd_rn(__fsub_rn(old, __fsub_rn(s, bb)), __fsub_rn(v, bb));
-      if (err != 0.0f) atomicAdd(a + 2 * m + 1, err);
-    }
+  accumulate_vals<ACC>(P, acc, slot, vals, W);
+}
+
+/* Mixed-precision deposit for the common pair of maps, profiles 1 and 2 of one table
+   (tSZ and kSZ): both profiles of a (corner, r-index) entry come from one 8-byte load,
+   and the bilinear-in-(chi, M), linear-in-log r blend uses corner weights formed once
+   and fused multiply-adds (a few ulp from the reference's sequence, far inside the
+   mixed path's tolerance).  Other map sets and clamped corners use deposit_maps. */
+template <int ACC>
+__device__ __forceinline__ void deposit_mixed(const PaintParams &P, const HotHalo &H,
+                                              long long slot, int ir, float fr,
+                                              const SweepBuffers *W) {
+  if (!P.paired || H.cb[0] < 0 || H.cb[1] < 0 || H.cb[2] < 0 || H.cb[3] < 0 || ir < 1 ||
+      ir >= P.th.nrt) {
+    deposit_maps<ACC>(P, H, W->acc, slot, ir, fr, W);
+    return;
   }
+  const float2 *tab = (const float2 *)P.tables[P.map_table[0]];
+  const int r = ir - 1; /* (cb + 2 (ir - 1)) / 2: the (profile 1, profile 2) pair at ir */
+  const float2 a0 = __ldg(tab + (H.cb[0] >> 1) + r), b0 = __ldg(tab + (H.cb[0] >> 1) + r + 1);
+  const float2 a1 = __ldg(tab + (H.cb[1] >> 1) + r), b1 = __ldg(tab + (H.cb[1] >> 1) + r + 1);
+  const float2 a2 = __ldg(tab + (H.cb[2] >> 1) + r), b2 = __ldg(tab + (H.cb[2] >> 1) + r + 1);
+  const float2 a3 = __ldg(tab + (H.cb[3] >> 1) + r), b3 = __ldg(tab + (H.cb[3] >> 1) + r + 1);
+  const float ofr = 1.0f - fr, fc = H.fc, fm = H.fm, ofc = 1.0f - fc, ofm = 1.0f - fm;
+  const float w0 = ofc * ofm, w1 = fc * ofm, w2 = ofc * fm, w3 = fc * fm;
+  float v1 = w0 * fmaf(a0.x, ofr, b0.x * fr);
+  v1 = fmaf(w1, fmaf(a1.x, ofr, b1.x * fr), v1);
+  v1 = fmaf(w2, fmaf(a2.x, ofr, b2.x * fr), v1);
+  v1 = fmaf(w3, fmaf(a3.x, ofr, b3.x * fr), v1);
+  float v2 = w0 * fmaf(a0.y, ofr, b0.y * fr);
+  v2 = fmaf(w1, fmaf(a1.y, ofr, b1.y * fr), v2);
+  v2 = fmaf(w2, fmaf(a2.y, ofr, b2.y * fr), v2);
+  v2 = fmaf(w3, fmaf(a3.y, ofr, b3.y * fr), v2);
+  float vals[P2M_MAXMAPS];
+#pragma unroll
+  for (int m = 0; m < P2M_MAXMAPS; m++) vals[m] = 0.0f;
+  vals[0] = H.w1 * v1;
+  vals[1] = H.w2 * v2;
+  accumulate_vals<ACC>(P, W->acc, slot, vals, W);
 }
 
 /* haloproject.f90:136-152: one warp per (halo, row); every operation is the
@@ -824,7 +869,9 @@ __device__ __forceinline__ void paint_pixel(const PaintParams &P, const SweepBuf
   nupd++;
   if (P.flags & 1)
     record_set(W.set_rec, W.set_pix, W.set_cap, &W.ctr->n_sets, W.halos[it.halo].rec, pix);
-  if (!zero_val && !H.zero) deposit_maps<ACC>(P, H, W.acc, pix, ir, fr, &W);
+  if (zero_val || H.zero) return;
+  if (EXACT) deposit_maps<ACC>(P, H, W.acc, pix, ir, fr, &W);
+  else deposit_mixed<ACC>(P, H, pix, ir, fr, &W);
 }
 
 /* loads items g0..g0+31 (below ihi) and their halos' hot fields into the warp's cache */
@@ -955,8 +1002,13 @@ __device__ __forceinline__ int warp_find(int key, int t) {
    those spans and paints their candidates 32 at a time, each lane fetching its item's
    fields from the lane that built it.  The halos' interpolation fields sit in shared
    memory.  Nothing is written to memory between the stages. */
+#ifndef P2M_HALOS_MINBLOCKS
+#define P2M_HALOS_MINBLOCKS 4 /* resident blocks per SM the register budget must allow */
+#endif
+
 template <int EXACT, int ACC>
-__global__ void __launch_bounds__(256) k_paint_halos(PaintParams P, SweepBuffers W) {
+__global__ void __launch_bounds__(256, P2M_HALOS_MINBLOCKS) k_paint_halos(PaintParams P,
+                                                                         SweepBuffers W) {
   __shared__ HotHalo s_hot[8][32];
   const int lane = threadIdx.x & 31;
   HotHalo *hot = s_hot[(threadIdx.x >> 5) & 7];
@@ -997,9 +1049,16 @@ __global__ void __launch_bounds__(256) k_paint_halos(PaintParams P, SweepBuffers
       gj.pl = __shfl_sync(FULL, g.pl, j);
       gj.cspan = __shfl_sync(FULL, g.cspan, j);
       const int ring = __shfl_sync(FULL, g.irlo, j) + t - __shfl_sync(FULL, rel, j);
-      RingItem it;
-      it.count = 0;
-      if (t < total) it = make_item(P, gj, (int)(h0 + j), ring);
+      RingItem it = {};
+      int npr = 0;
+      long long rbase = 0; /* RING index of the ring's first pixel */
+      if (t < total) {
+        it = make_item(P, gj, (int)(h0 + j), ring);
+        int ks;
+        long long npn;
+        p2m_ring_info(P.nside, ring, &npr, &ks, &npn);
+        rbase = npn - npr;
+      }
       const int cx = warp_incl_scan(it.count);
       const int cex = cx - it.count, ctot = __shfl_sync(FULL, cx, 31);
       for (int c0 = 0; c0 < ctot; c0 += 32) {
@@ -1015,8 +1074,14 @@ __global__ void __launch_bounds__(256) k_paint_halos(PaintParams P, SweepBuffers
         ci.hdphi = __shfl_sync(FULL, it.hdphi, i);
         const int jj = __shfl_sync(FULL, j, i);
         const int k = c - __shfl_sync(FULL, cex, i);
-        if (c < ctot)
-          paint_pixel<EXACT, ACC>(P, W, ci, hot[jj], k, item_pixel(P, ci, k), nupd, nrc);
+        const int np = __shfl_sync(FULL, npr, i);
+        const long long rb = __shfl_sync(FULL, rbase, i);
+        if (c < ctot) {
+          int iphi = ci.lo + k;
+          if (iphi < 0) iphi += np;
+          if (iphi >= np) iphi -= np;
+          paint_pixel<EXACT, ACC>(P, W, ci, hot[jj], k, rb + iphi, nupd, nrc);
+        }
       }
       if (lane == 0) ncand += (unsigned long long)ctot;
     }
