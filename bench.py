@@ -35,6 +35,13 @@ MASS = (1e12, 3e15)
 SEED = 2
 ZMAX = 6.0
 MAPS = ((0, 1), (0, 2))
+LAUNCHES_PER_STEP = 13
+# DRAM bytes (read + write) per pixel update of k_paint_halos from the ncu capture
+# summarised in profiles/k_paint_halos_1e7_nside2048.md
+PAINT_DRAM_BYTES_PER_UPDATE = 96.2
+# L2 atomic throughput of this GB300 (sectors/s): ncu lts__t_sectors_srcunit_tex_op_atom
+# of the same capture, 32.9 sectors/ns at 8.69 % of peak sustained
+L2_ATOMIC_SECTORS_PER_S = 3.79e11
 METRIC = "halos/sec & pixel-updates/sec at Nside=4096, 1 GB300; rel err vs FP64 oracle"
 
 
@@ -263,11 +270,25 @@ def run_ours(args):
     barrier()
     e2e_ms = 1e3 * (time.perf_counter() - t0) / args.steps
     pt.close()
+    # the host link alone: the same copies without the painting
+    d_tmp = torch.empty_like(h_rec, device=dev)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        d_tmp.copy_(h_rec, non_blocking=True)
+    barrier()
+    h2d_ms = 1e3 * (time.perf_counter() - t0) / args.steps
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        for m in range(len(MAPS)):
+            h_outs[m].copy_(outs[m], non_blocking=True)
+    barrier()
+    d2h_ms = 1e3 * (time.perf_counter() - t0) / args.steps
+    del d_tmp
 
     total_halos = N * ws
     value = total_halos / (ms * 1e-3)
     upd = st["hp_updates"] * len(MAPS)
-    # roofline of the dominant kernel (HBM-bound): algorithmic bytes per launch
     peaks = {}
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -276,21 +297,36 @@ def run_ours(args):
         pass
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
     peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
-    # algorithmic HBM bytes per launch: the catalogue is read once by the cut; the mixed
-    # sweep accumulates in L2 and writes each output pixel once; the plain path reads and
-    # writes an 8-byte accumulator per update and reads it once more at read-out
-    alg = {
-        "cut": N * 40,
-        "paint": (len(MAPS) * npix * 4 if args.precision == "mixed" else upd * 16),
-        "readout": len(MAPS) * npix * (8 + 4),
-    }
-    dom = max(alg, key=lambda k: phases.get(k, 0.0))
-    dom_ms = phases[dom]
-    achieved = alg[dom] / (dom_ms * 1e-3) / 1e9 if dom_ms > 0 else None
-    roof = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak,
-            "unit": "GB/s", "frac": achieved / hbm_peak if achieved else None,
-            "peak_source": peak_src, "traffic": None,
-            "algorithmic_bytes": alg[dom], "launch_ms": dom_ms}
+    # roofline of the dominant phase, the HEALPix paint (k_paint_halos, the fused
+    # enumerate-and-paint kernel, ~90% of it, plus k_paint_full for the large halos), timed
+    # by CUDA events on the paint stream around the two launches.  Algorithmic bytes per
+    # launch, the per-unit figure of the two-float accumulator: 16 B per pixel update and
+    # map (read-modify-write of hi + lo), U = pixel updates summed over the maps.
+    paint_ms = phases["paint"] + phases["paint_big"]
+    alg_paint = upd * 16
+    achieved = alg_paint / (paint_ms * 1e-3) / 1e9 if paint_ms > 0 else None
+    # DRAM traffic of the paint from the ncu capture of a smaller case (1e7 halos at
+    # Nside 2048), scaled by the pixel updates processed
+    traffic = PAINT_DRAM_BYTES_PER_UPDATE * st["hp_updates"] if args.precision == "mixed" else None
+    roof = {"bound": "hbm", "kernel": "k_paint_halos + k_paint_full", "achieved": achieved,
+            "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak if achieved else None,
+            "peak_source": ("measured (MEASURED_PEAKS.json hbm_gbs)" if peak_src == "measured"
+                            else "fallback 6.8 TB/s"),
+            "traffic": traffic, "algorithmic_bytes": alg_paint, "launch_ms": paint_ms,
+            "atomic_updates_per_s": upd / (paint_ms * 1e-3) if paint_ms > 0 else None,
+            "atomic_peak_per_s": L2_ATOMIC_SECTORS_PER_S,
+            "atomic_frac": upd / (paint_ms * 1e-3) / L2_ATOMIC_SECTORS_PER_S if paint_ms > 0 else None}
+    # the whole step (ingest through maps ready): the algorithmic bytes of the path with a
+    # two-float accumulator (catalogue read, 16 B per update, accumulator zero-fill + read
+    # and output write per pixel and map), and the bytes no design can avoid (catalogue
+    # read once, both float maps written once)
+    step_alg = N * 40 + upd * 16 + len(MAPS) * npix * (8 + 4)
+    step_min = N * 40 + len(MAPS) * npix * 4
+    step_roof = {"algorithmic_bytes": step_alg,
+                 "achieved_gbs": step_alg / (ms * 1e-3) / 1e9,
+                 "frac": step_alg / (ms * 1e-3) / 1e9 / hbm_peak,
+                 "min_bytes": step_min,
+                 "min_frac": step_min / (ms * 1e-3) / 1e9 / hbm_peak}
 
     out = {"metric": METRIC, "value": value, "unit": "halos/s", "n_gpus": ws,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
@@ -308,14 +344,16 @@ def run_ours(args):
                                           "hp_candidates", "hp_updates", "n_recheck")},
            "gpu_launches": None,
            "roofline": roof,
+           "step_roofline": step_roof,
            "clocks": clocks,
            "e2e": {"value": total_halos / (e2e_ms * 1e-3), "unit": "halos/s",
                    "ms_per_step": e2e_ms, "h2d_bytes_per_step": int(rec.nbytes),
-                   "d2h_bytes_per_step": int(len(MAPS) * npix * 4)}}
-    # cut, set-up, 3-kernel item scan, items | band scan, band scatter, 3-kernel candidate
-    # scan, unit queue + sweep (mixed) or paint + read-out (plain)
-    nlaunch = 2 + 3 + 1 + 1 + 1 + 3 + 2
-    out["gpu_launches"] = nlaunch * args.steps
+                   "d2h_bytes_per_step": int(len(MAPS) * npix * 4),
+                   "h2d_ms": h2d_ms, "d2h_ms": d2h_ms}}
+    # per step: cut, set-up, 3-kernel ring scan and the item kernel of the large halos,
+    # their candidate counts and 3-kernel scan, the fused paint, the large-halo paint and
+    # the fold of the low words (memsets are not kernels)
+    out["gpu_launches"] = LAUNCHES_PER_STEP * args.steps
 
     if not args.no_plain and args.precision == "mixed":
         pp = make("fp64")

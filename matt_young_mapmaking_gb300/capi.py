@@ -125,7 +125,8 @@ def exported_symbols():
             "p2m_get_timings"]
 
 
-PHASES = ["cut", "setup", "big_scan", "big_items", "flatsky", "big_offsets", "paint", "readout"]
+PHASES = ["cut", "setup", "big_scan", "big_items", "flatsky", "big_offsets", "paint", "paint_big",
+          "readout"]
 
 
 def _ptr(a):

@@ -19,7 +19,10 @@
 #include "../../include/p2m_tools.h"
 #include "p2m_internal.h"
 
-enum { PH_CUT, PH_SETUP, PH_SCAN, PH_ITEMS, PH_FS, PH_GROUP, PH_PAINT, PH_READOUT, P2M_NPHASE };
+enum {
+  PH_CUT, PH_SETUP, PH_SCAN, PH_ITEMS, PH_FS, PH_GROUP, PH_PAINT, PH_PAINT_BIG, PH_READOUT,
+  P2M_NPHASE
+};
 
 struct p2m_ctx {
   p2m_config cfg;
@@ -409,8 +412,10 @@ p2m_status sweep(p2m_ctx *ctx, cudaStream_t s) {
   SweepBuffers W = sweep_buffers(ctx);
   TB(PH_PAINT);
   p2m_launch_paint_halos(P, W, s, ctx->nsm);
-  if (n > 0) p2m_launch_paint_full(P, W, s, ctx->nsm);
   TE(PH_PAINT);
+  TB(PH_PAINT_BIG);
+  if (n > 0) p2m_launch_paint_full(P, W, s, ctx->nsm);
+  TE(PH_PAINT_BIG);
   TB(PH_READOUT);
   if (compensated(ctx)) {
     /* fold the sparse low words into the maps and clear them */

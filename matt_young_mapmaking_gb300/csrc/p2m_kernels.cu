@@ -835,8 +835,8 @@ struct CacheEnt {
 template <int EXACT, int ACC>
 __device__ __forceinline__ void paint_pixel(const PaintParams &P, const SweepBuffers &W,
                                             const RingItem &it, const HotHalo &H, int k,
-                                            long long pix, unsigned long long &nupd,
-                                            unsigned long long &nrc) {
+                                            long long pix, unsigned int &nupd,
+                                            unsigned int &nrc) {
   int ir = 0;
   float fr = 0.0f, u = 0.0f;
   bool zero_val = H.zero;
@@ -905,8 +905,8 @@ __device__ __forceinline__ long long item_pixel(const PaintParams &P, const Ring
    loaded once per window. */
 template <int EXACT, int ACC>
 __device__ void walk_candidates(const PaintParams &P, const SweepBuffers &W, long long p0,
-                                long long p1, long long ihi, unsigned long long &nupd,
-                                unsigned long long &nrc, CacheEnt *cache) {
+                                long long p1, long long ihi, unsigned int &nupd,
+                                unsigned int &nrc, CacheEnt *cache) {
   const int lane = threadIdx.x & 31;
   const long long *off = W.pix_off;
   long long g0 = warp_upper(off, 0, ihi, p0);
@@ -963,7 +963,8 @@ __global__ void __launch_bounds__(256) k_paint_full(PaintParams P, SweepBuffers 
   const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
   const long long chunk = 1024;
   CacheEnt *cache = s_cache[(threadIdx.x >> 5) & 7];
-  unsigned long long nupd = 0, nrc = 0, ncand = 0;
+  unsigned int nupd = 0, nrc = 0;
+  unsigned long long ncand = 0;
   for (long long c = warp; c * chunk < npix_c; c += nwarps) {
     long long p0 = c * chunk, p1 = min(npix_c, p0 + chunk);
     walk_candidates<EXACT, ACC>(P, W, p0, p1, W.n_items, nupd, nrc, cache);
@@ -996,32 +997,43 @@ __device__ __forceinline__ int warp_find(int key, int t) {
   return j;
 }
 
-/* Enumeration fused with painting for the halos spanning at most big_rings rings.
-   A warp claims 32 consecutive halos and prefix-sums their ring counts in registers;
-   each lane builds the candidate span of one (halo, ring) item; the warp prefix-sums
-   those spans and paints their candidates 32 at a time, each lane fetching its item's
-   fields from the lane that built it.  The halos' interpolation fields sit in shared
-   memory.  Nothing is written to memory between the stages. */
 #ifndef P2M_HALOS_MINBLOCKS
 #define P2M_HALOS_MINBLOCKS 4 /* resident blocks per SM the register budget must allow */
 #endif
 
+/* per-warp shared-memory stage of the fused painter: the disc geometry and
+   interpolation fields of the warp's 32 halos, and the 32 (halo, ring) items of the
+   current round (structure of arrays: lanes reading different entries hit different
+   banks) */
+struct WarpStage {
+  HotHalo hot[32];
+  float gzh[32], gzl[32], gsh[32], gsl[32], gph[32], gpl[32], gcs[32];
+  int girlo[32];
+  float iA[32], iB[32], if0[32], ihd[32];
+  int ilo[32], in0[32], inpr[32], ij[32];
+  long long irb[32]; /* RING index of the item ring's first pixel */
+};
+
+/* Enumeration fused with painting for the halos spanning at most big_rings rings.
+   A warp claims 32 consecutive halos, stages their fields and prefix-sums their ring
+   counts; each lane builds the candidate span of one (halo, ring) item and stages it;
+   the warp prefix-sums the spans and paints their candidates 32 at a time, each lane
+   finding its item with a 32-wide search.  Nothing goes to global memory between the
+   stages. */
 template <int EXACT, int ACC>
 __global__ void __launch_bounds__(256, P2M_HALOS_MINBLOCKS) k_paint_halos(PaintParams P,
                                                                          SweepBuffers W) {
-  __shared__ HotHalo s_hot[8][32];
+  __shared__ WarpStage s_stage[8];
   const int lane = threadIdx.x & 31;
-  HotHalo *hot = s_hot[(threadIdx.x >> 5) & 7];
+  WarpStage &S = s_stage[(threadIdx.x >> 5) & 7];
   const long long nh = W.n_halos;
-  unsigned long long nupd = 0, nrc = 0, ncand = 0;
+  unsigned int nupd = 0, nrc = 0;
+  unsigned long long ncand = 0;
   for (;;) {
     long long h0 = 0;
     if (lane == 0) h0 = 32LL * (long long)atomicAdd(&W.ctr->next_unit, 1u);
     h0 = __shfl_sync(FULL, h0, 0);
     if (h0 >= nh) break;
-    DiscGeom g;
-    g.zh = g.zl = g.sh = g.sl = g.ph = g.pl = g.cspan = 0.0f;
-    g.irlo = 0;
     int nr = 0;
     __syncwarp();
     if (h0 + lane < nh) {
@@ -1029,58 +1041,74 @@ __global__ void __launch_bounds__(256, P2M_HALOS_MINBLOCKS) k_paint_halos(PaintP
       int r = H.ir_hi - H.ir_lo + 1;
       if (r > 0 && r <= P.big_rings) {
         nr = r;
-        g = geom_of(H);
-        hot[lane] = hot_of(H);
+        S.gzh[lane] = H.z0h;
+        S.gzl[lane] = H.z0l;
+        S.gsh[lane] = H.s0h;
+        S.gsl[lane] = H.s0l;
+        S.gph[lane] = H.p0h;
+        S.gpl[lane] = H.p0l;
+        S.gcs[lane] = H.C_span;
+        S.girlo[lane] = H.ir_lo;
+        S.hot[lane] = hot_of(H);
       }
     }
-    __syncwarp();
     const int rx = warp_incl_scan(nr);
     const int rel = rx - nr, total = __shfl_sync(FULL, rx, 31);
     for (int t0 = 0; t0 < total; t0 += 32) {
-      /* item t of the batch: ring rel_j..rel_j+nr_j-1 of halo lane j */
+      /* item t of the batch: ring t - rel_j of halo lane j */
       const int t = t0 + lane;
       const int j = warp_find(rel, t);
-      DiscGeom gj;
-      gj.zh = __shfl_sync(FULL, g.zh, j);
-      gj.zl = __shfl_sync(FULL, g.zl, j);
-      gj.sh = __shfl_sync(FULL, g.sh, j);
-      gj.sl = __shfl_sync(FULL, g.sl, j);
-      gj.ph = __shfl_sync(FULL, g.ph, j);
-      gj.pl = __shfl_sync(FULL, g.pl, j);
-      gj.cspan = __shfl_sync(FULL, g.cspan, j);
-      const int ring = __shfl_sync(FULL, g.irlo, j) + t - __shfl_sync(FULL, rel, j);
-      RingItem it = {};
-      int npr = 0;
-      long long rbase = 0; /* RING index of the ring's first pixel */
+      const int relj = __shfl_sync(FULL, rel, j);
+      int cnt = 0;
+      __syncwarp(); /* the stage's halos are written; the previous round's items are read */
       if (t < total) {
-        it = make_item(P, gj, (int)(h0 + j), ring);
-        int ks;
+        DiscGeom g;
+        g.zh = S.gzh[j];
+        g.zl = S.gzl[j];
+        g.sh = S.gsh[j];
+        g.sl = S.gsl[j];
+        g.ph = S.gph[j];
+        g.pl = S.gpl[j];
+        g.cspan = S.gcs[j];
+        const int ring = S.girlo[j] + (t - relj);
+        const RingItem it = make_item(P, g, 0, ring);
+        int npr, ks;
         long long npn;
         p2m_ring_info(P.nside, ring, &npr, &ks, &npn);
-        rbase = npn - npr;
+        S.iA[lane] = it.A;
+        S.iB[lane] = it.B;
+        S.if0[lane] = it.f0;
+        S.ihd[lane] = it.hdphi;
+        S.ilo[lane] = it.lo;
+        S.in0[lane] = it.ring_n0 & 0xffff;
+        S.inpr[lane] = npr;
+        S.ij[lane] = j;
+        S.irb[lane] = npn - npr;
+        cnt = it.count;
       }
-      const int cx = warp_incl_scan(it.count);
-      const int cex = cx - it.count, ctot = __shfl_sync(FULL, cx, 31);
+      __syncwarp();
+      const int cx = warp_incl_scan(cnt);
+      const int cex = cx - cnt, ctot = __shfl_sync(FULL, cx, 31);
       for (int c0 = 0; c0 < ctot; c0 += 32) {
         const int c = c0 + lane;
         const int i = warp_find(cex, c);
-        RingItem ci;
-        ci.halo = __shfl_sync(FULL, it.halo, i);
-        ci.ring_n0 = __shfl_sync(FULL, it.ring_n0, i);
-        ci.lo = __shfl_sync(FULL, it.lo, i);
-        ci.A = __shfl_sync(FULL, it.A, i);
-        ci.B = __shfl_sync(FULL, it.B, i);
-        ci.f0 = __shfl_sync(FULL, it.f0, i);
-        ci.hdphi = __shfl_sync(FULL, it.hdphi, i);
-        const int jj = __shfl_sync(FULL, j, i);
         const int k = c - __shfl_sync(FULL, cex, i);
-        const int np = __shfl_sync(FULL, npr, i);
-        const long long rb = __shfl_sync(FULL, rbase, i);
         if (c < ctot) {
+          RingItem ci;
+          const int jj = S.ij[i];
+          ci.halo = (int)(h0 + jj);
+          ci.ring_n0 = S.in0[i];
+          ci.lo = S.ilo[i];
+          ci.count = 0;
+          ci.A = S.iA[i];
+          ci.B = S.iB[i];
+          ci.f0 = S.if0[i];
+          ci.hdphi = S.ihd[i];
+          const int np = S.inpr[i];
           int iphi = ci.lo + k;
           if (iphi < 0) iphi += np;
           if (iphi >= np) iphi -= np;
-          paint_pixel<EXACT, ACC>(P, W, ci, hot[jj], k, rb + iphi, nupd, nrc);
+          paint_pixel<EXACT, ACC>(P, W, ci, S.hot[jj], k, S.irb[i] + iphi, nupd, nrc);
         }
       }
       if (lane == 0) ncand += (unsigned long long)ctot;
@@ -1176,12 +1204,19 @@ __global__ void __launch_bounds__(256) k_fold_lo(SweepBuffers W, int nmaps) {
   }
 }
 
-/* sum over a float map (double accumulation) */
+/* sum over a float map: float-float (TwoSum) accumulation per thread, FP64 only for the
+   per-thread totals (FP64 adds run at a small fraction of the FP32 rate here) */
 __global__ void __launch_bounds__(256) k_map_sum(const float *map, long long n, double *sum) {
-  double s = 0.0;
+  float hi = 0.0f, lo = 0.0f;
   for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < n;
-       p += (long long)gridDim.x * blockDim.x)
-    s += (double)map[p];
+       p += (long long)gridDim.x * blockDim.x) {
+    const float x = map[p];
+    const float sm = __fadd_rn(hi, x);
+    const float bb = __fsub_rn(sm, hi);
+    lo = __fadd_rn(lo, __fadd_rn(__fsub_rn(hi, __fsub_rn(sm, bb)), __fsub_rn(x, bb)));
+    hi = sm;
+  }
+  double s = (double)hi + (double)lo;
   for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(FULL, s, o);
   if ((threadIdx.x & 31) == 0 && s != 0.0) atomicAdd(sum, s);
 }
@@ -1372,11 +1407,23 @@ void p2m_launch_paint_full(const PaintParams &P, const SweepBuffers &W, cudaStre
   else if (P.precision == 1) k_paint_full<0, 2><<<nsm * 8, 256, 0, s>>>(P, W);
   else k_paint_full<0, 0><<<nsm * 8, 256, 0, s>>>(P, W);
 }
-void p2m_launch_paint_halos(const PaintParams &P, const SweepBuffers &W, cudaStream_t s, int nsm) {
+template <int EXACT, int ACC>
+static void launch_paint_halos(const PaintParams &P, const SweepBuffers &W, cudaStream_t s,
+                               int nsm) {
+  /* the shared-memory stage (32 KB per block) must not be what limits residency */
+  static bool carveout = false;
+  if (!carveout) {
+    cudaFuncSetAttribute(k_paint_halos<EXACT, ACC>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                         (int)cudaSharedmemCarveoutMaxShared);
+    carveout = true;
+  }
   /* warps claim 32-halo batches until none is left */
-  if (P.precision == 0) k_paint_halos<1, 0><<<nsm * 8, 256, 0, s>>>(P, W);
-  else if (P.precision == 1) k_paint_halos<0, 2><<<nsm * 8, 256, 0, s>>>(P, W);
-  else k_paint_halos<0, 0><<<nsm * 8, 256, 0, s>>>(P, W);
+  k_paint_halos<EXACT, ACC><<<nsm * 8, 256, 0, s>>>(P, W);
+}
+void p2m_launch_paint_halos(const PaintParams &P, const SweepBuffers &W, cudaStream_t s, int nsm) {
+  if (P.precision == 0) launch_paint_halos<1, 0>(P, W, s, nsm);
+  else if (P.precision == 1) launch_paint_halos<0, 2>(P, W, s, nsm);
+  else launch_paint_halos<0, 0>(P, W, s, nsm);
 }
 void p2m_launch_item_counts(const RingItem *items, long long n, unsigned int *counts,
                             cudaStream_t s, int nsm) {
