@@ -36,6 +36,21 @@ void p2m_philox4x32(const uint32_t c[4], const uint32_t k[2], uint32_t out[4]);
 struct p2m_ctx;
 int32_t p2m_get_timings(struct p2m_ctx *ctx, double *ms, int32_t n);
 
+/* Sums (FP64 totals of float-float partial sums) of nmaps float maps of npix pixels each,
+   already in device memory on the current device, written to host sums[0..nmaps).
+   No counterpart in the reference (its map sums are module-array loops on the host).
+   Allocates nothing: the scratch is a file-scope device array of P2M_NOALLOC_MAXMAPS
+   doubles per device, cleared by the call itself on `stream` (NULL = the legacy default
+   stream) before use.  For callers that may not allocate device memory (a host
+   framework whose caching allocator owns the device, or a loop that cannot afford the
+   device-wide synchronisation of cudaFree).  The first call on a device looks up the
+   scratch address and may load the module: make it before any stream capture.  Calls on
+   one device share the scratch, so overlapping calls race and must be serialised by the
+   caller.  Synchronous.  nmaps > P2M_NOALLOC_MAXMAPS: P2M_ERR_CAPACITY. */
+#define P2M_NOALLOC_MAXMAPS 8
+int32_t p2m_map_sums_noalloc(const float *const *d_maps, int32_t nmaps, int64_t npix,
+                             double *sums, void *stream);
+
 /* Self-test of the single-precision math the kernels use (fn: 0 log, 1 exp, 2 pow,
    3 asin, 4 atan, 5 sin, 6 cos, 7 tan) evaluated on the GPU over n device floats;
    d_y is read only for pow.  Synchronous.  Returns 0 or a CUDA error code. */

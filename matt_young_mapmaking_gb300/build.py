@@ -25,7 +25,7 @@ MAPTABLE_CLI = os.path.join(PKG, "make_maptable")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",
               "-I" + CSRC, "-I" + INCLUDE]
-CU_SOURCES = ["p2m_kernels.cu", "p2m_capi.cu"]
+CU_SOURCES = ["p2m_kernels.cu", "p2m_capi.cu", "p2m_noalloc.cu"]
 CPP_SOURCES = ["p2m_tools.cpp"]
 
 
@@ -52,7 +52,7 @@ def _stale(target, sources):
 
 def _headers():
     hs = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".h")]
-    return hs + [os.path.join(INCLUDE, "p2m.h")]
+    return hs + [os.path.join(INCLUDE, "p2m.h"), os.path.join(INCLUDE, "p2m_tools.h")]
 
 
 def build_lib(force=False, verbose=False):

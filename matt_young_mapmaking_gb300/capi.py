@@ -16,6 +16,8 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "libp2m_gb300.so")
 
 MAXMAPS = 8
+NOALLOC_MAXMAPS = 8  # P2M_NOALLOC_MAXMAPS of include/p2m_tools.h
+P2M_OK, P2M_ERR_BADARG, P2M_ERR_CUDA, P2M_ERR_CAPACITY = 0, 1, 2, 3
 PREC_FP64, PREC_MIXED, PREC_MIXED_F64 = 0, 1, 2
 FLAG_RECORD_SETS, FLAG_ALL_HALOS, FLAG_TIMING, FLAG_VALIDATE = 1, 2, 4, 8
 STATUS = {0: "OK", 1: "BADARG", 2: "CUDA", 3: "CAPACITY", 4: "TIMEOUT", 5: "IO", 6: "STATE",
@@ -105,6 +107,7 @@ def load_library():
         "p2m_philox4x32": (None, [VP, VP, VP]),
         "p2m_fmath_eval_device": (I32, [I32, I32, VP, VP, VP, I64]),
         "p2m_get_timings": (I32, [VP, VP, I32]),
+        "p2m_map_sums_noalloc": (I32, [VP, I32, I64, VP, VP]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -122,7 +125,7 @@ def exported_symbols():
             "p2m_bind_healpix_device", "p2m_get_stats",
             "p2m_synchronize", "p2m_get_pixel_sets", "p2m_make_maptable",
             "p2m_generate_catalogue", "p2m_philox4x32", "p2m_fmath_eval_device",
-            "p2m_get_timings"]
+            "p2m_get_timings", "p2m_map_sums_noalloc"]
 
 
 PHASES = ["cut", "setup", "big_scan", "big_items", "flatsky", "big_offsets", "paint", "paint_big",
