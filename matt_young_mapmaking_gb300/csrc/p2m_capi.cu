@@ -84,6 +84,10 @@ struct p2m_ctx {
   std::vector<float> prep;
   long long n_records = 0;
   cudaEvent_t ev_join = nullptr, ev_back = nullptr;
+  /* the compensated path's output clear runs on its own stream, beside the ingest */
+  cudaStream_t zstream = nullptr;
+  cudaEvent_t ev_zero_start = nullptr, ev_zero_done = nullptr;
+  bool zero_pending = false;
   cudaEvent_t tev[P2M_NPHASE][2] = {};
   bool tev_used[P2M_NPHASE] = {};
 };
@@ -194,6 +198,7 @@ PaintParams make_params(const p2m_ctx *ctx, int nfloat) {
   P.zofr = ctx->d_zofr;
   P.ringtab = ctx->d_ringtab;
   P.band_u = ctx->band_u;
+  P.inv_drt = ctx->th_set ? 1.0f / ctx->th.drt : 0.0f;
   P.big_rings = ctx->big_rings;
   if (ctx->th_set) {
     float fr;
@@ -287,12 +292,27 @@ p2m_status ingest_tail(p2m_ctx *ctx, const PaintParams &P, long long n_max, cuda
 bool compensated(const p2m_ctx *ctx) { return ctx->d_lo != nullptr; }
 
 /* the compensated path accumulates into the output maps: clear them before the first
-   paint after a reset (the buffers bound at that time) */
+   paint after a reset (the buffers bound at that time).  The clear is bandwidth-bound
+   and independent of the ingest, so it runs on a side stream after the work already on
+   s; the sweep waits for it before painting. */
 p2m_status zero_outputs(p2m_ctx *ctx, cudaStream_t s) {
   if (!compensated(ctx) || ctx->outs_zeroed) return P2M_OK;
+  CK(cudaEventRecord(ctx->ev_zero_start, s));
+  CK(cudaStreamWaitEvent(ctx->zstream, ctx->ev_zero_start, 0));
   for (int m = 0; m < ctx->cfg.nmaps; m++)
-    CK(cudaMemsetAsync(ctx->d_out[m], 0, sizeof(float) * (size_t)ctx->hp_npix, s));
+    CK(cudaMemsetAsync(ctx->d_out[m], 0, sizeof(float) * (size_t)ctx->hp_npix, ctx->zstream));
+  CK(cudaEventRecord(ctx->ev_zero_done, ctx->zstream));
+  ctx->zero_pending = true;
   ctx->outs_zeroed = true;
+  return P2M_OK;
+}
+
+/* orders s after a pending clear of the output maps */
+p2m_status wait_zero(p2m_ctx *ctx, cudaStream_t s) {
+  if (!ctx->zero_pending) return P2M_OK;
+  CK(cudaStreamWaitEvent(s, ctx->ev_zero_done, 0));
+  if (s != ctx->stream) CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_zero_done, 0));
+  ctx->zero_pending = false;
   return P2M_OK;
 }
 
@@ -380,6 +400,7 @@ SweepBuffers sweep_buffers(const p2m_ctx *ctx) {
 /* produces the HEALPix output maps from everything ingested since the last sweep */
 p2m_status sweep(p2m_ctx *ctx, cudaStream_t s) {
   ST(flush_prepared(ctx));
+  ST(wait_zero(ctx, s));
   if (ctx->cfg.nside <= 0) {
     ctx->dirty = false;
     return P2M_OK;
@@ -481,6 +502,9 @@ p2m_status p2m_create(const p2m_config *cfg, p2m_ctx **out) {
   CK(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
   CK(cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming));
   CK(cudaEventCreateWithFlags(&ctx->ev_back, cudaEventDisableTiming));
+  CK(cudaStreamCreateWithFlags(&ctx->zstream, cudaStreamNonBlocking));
+  CK(cudaEventCreateWithFlags(&ctx->ev_zero_start, cudaEventDisableTiming));
+  CK(cudaEventCreateWithFlags(&ctx->ev_zero_done, cudaEventDisableTiming));
   /* cosmology tables, built once on the host with the reference's float sequence */
   ctx->rofz_host.assign(P2M_NZTAB, 0.0f);
   ctx->zofr_host.assign(P2M_NZTAB, 0.0f);
@@ -549,6 +573,7 @@ void p2m_destroy(p2m_ctx *ctx) {
   if (!ctx) return;
   cudaSetDevice(ctx->cfg.device);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  if (ctx->zstream) cudaStreamSynchronize(ctx->zstream);
   void *ptrs[] = {ctx->d_rofz, ctx->d_zofr, ctx->d_ringtab, ctx->d_acc64, ctx->d_fs_acc,
                   ctx->d_fs_out, ctx->d_halos, ctx->d_items_raw, ctx->d_records, ctx->d_surv,
                   ctx->d_nring, ctx->d_ioff, ctx->d_fs_items, ctx->d_scan_tmp, ctx->d_counts,
@@ -563,6 +588,9 @@ void p2m_destroy(p2m_ctx *ctx) {
   if (ctx->h_ctr) cudaFreeHost(ctx->h_ctr);
   if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
   if (ctx->ev_back) cudaEventDestroy(ctx->ev_back);
+  if (ctx->ev_zero_start) cudaEventDestroy(ctx->ev_zero_start);
+  if (ctx->ev_zero_done) cudaEventDestroy(ctx->ev_zero_done);
+  if (ctx->zstream) cudaStreamDestroy(ctx->zstream);
   for (int k = 0; k < P2M_NPHASE; k++)
     for (int e = 0; e < 2; e++)
       if (ctx->tev[k][e]) cudaEventDestroy(ctx->tev[k][e]);
@@ -785,6 +813,7 @@ p2m_status p2m_get_stats(p2m_ctx *ctx, p2m_stats *out) {
 p2m_status p2m_synchronize(p2m_ctx *ctx) {
   if (!ctx) return P2M_ERR_BADARG;
   CK(cudaSetDevice(ctx->cfg.device));
+  CK(cudaStreamSynchronize(ctx->zstream));
   CK(cudaStreamSynchronize(ctx->stream));
   return P2M_OK;
 }

@@ -99,6 +99,7 @@ struct PaintParams {
   int ir_c;     /* r-index and fraction for r < rmint (r = rmint + 1e-5) */
   float fr_c;
   float band_u;  /* half-width of the r-index recheck band (cell units) */
+  float inv_drt; /* 1 / drt of the table */
   int big_rings; /* halos spanning more rings are painted from stored items */
   const float *tables[P2M_MAXTABLES];
   const float *rofz, *zofr;

@@ -784,13 +784,28 @@ __device__ __forceinline__ void record_set(long long *set_rec, long long *set_pi
   }
 }
 
+/* sin(y) by its Taylor series through y^15, for the half longitude offset y of a candidate
+   from the disc centre: |y| < pi/2 + pi/npr <= 2.37, where the truncation stays below 1e-8
+   and the rounding is a few ulp */
+__device__ __forceinline__ float sin_half_offset(float y) {
+  const float y2 = y * y;
+  float p = 1.0f / 1307674368000.0f;      /* 1/15! */
+  p = fmaf(p, y2, -1.0f / 6227020800.0f); /* -1/13! */
+  p = fmaf(p, y2, 1.0f / 39916800.0f);    /* 1/11! */
+  p = fmaf(p, y2, -1.0f / 362880.0f);     /* -1/9! */
+  p = fmaf(p, y2, 1.0f / 5040.0f);        /* 1/7! */
+  p = fmaf(p, y2, -1.0f / 120.0f);        /* -1/5! */
+  p = fmaf(p, y2, 1.0f / 6.0f);           /* 1/3! */
+  return fmaf(-y * y2, p, y);             /* y - y^3 (1/3! - y^2/5! + ...) */
+}
+
 /* Fast mixed-precision decision for one candidate.  Returns 0 outside, 1 inside with
    (ir, fr) or zero value, 2 when the exact path must decide. */
 __device__ __forceinline__ int fast_decide(const PaintParams &P, const RingItem &it,
                                            const HotHalo &H, int k, int &ir, float &fr,
                                            bool &zero_val, float &u_out) {
   float x = (float)(item_n0(it) + k) + it.f0;
-  float s = sinf(x * it.hdphi);
+  float s = sin_half_offset(x * it.hdphi);
   float c2 = it.A + it.B * (s * s);
   if (c2 >= H.C_out) return 0;
   if (c2 > H.C_in) return 2;
@@ -814,7 +829,7 @@ __device__ __forceinline__ int fast_decide(const PaintParams &P, const RingItem 
   }
   if (r <= P.th.rmint * (1.0f + dr)) return 2;
   float lr = __logf(r);
-  float u = (lr - P.th.lrmin) / P.th.drt;
+  float u = (lr - P.th.lrmin) * P.inv_drt;
   int iu = (int)u;
   float fu = u - (float)iu;
   if (fu < P.band_u || fu > 1.0f - P.band_u || iu < 0 || iu > P.th.nrt - 2) return 2;
@@ -1170,8 +1185,9 @@ __global__ void __launch_bounds__(256) k_finalize_full(double *acc, long long np
 }
 
 /* folds the nonzero low words of the compensated accumulation into the output maps
-   (out = RN(hi + lo)) and clears them.  A warp reads the flags of 32 consecutive
-   tiles and visits each flagged tile (one pixel per lane) */
+   (out = RN(hi + lo)) and clears them.  A warp reads the flags of 32 consecutive tiles
+   and visits the flagged ones (one pixel per lane), up to four tiles with all their loads
+   in flight at once for the usual two maps */
 __global__ void __launch_bounds__(256) k_fold_lo(SweepBuffers W, int nmaps) {
   const int lane = threadIdx.x & 31;
   const long long ntiles = (W.npix + P2M_TILE_PIX - 1) >> P2M_TILE_SHIFT;
@@ -1182,6 +1198,46 @@ __global__ void __launch_bounds__(256) k_fold_lo(SweepBuffers W, int nmaps) {
     bool dirty = t < ntiles && W.tiles[t];
     unsigned m = __ballot_sync(FULL, dirty);
     if (dirty) W.tiles[t] = 0;
+    if (nmaps == 2) {
+      float *lo0 = W.lo, *lo1 = W.lo + W.npix, *o0 = W.out[0], *o1 = W.out[1];
+      while (m) {
+        long long p[4];
+        int cnt = 0;
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+          p[u] = -1;
+          if (m) {
+            int b = __ffs(m) - 1;
+            m &= m - 1;
+            long long q = ((t0 + b) << P2M_TILE_SHIFT) + lane;
+            p[u] = q < W.npix ? q : -1;
+            cnt++;
+          }
+        }
+        float l0[4], l1[4], h0[4], h1[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++)
+          if (u < cnt && p[u] >= 0) {
+            l0[u] = lo0[p[u]];
+            l1[u] = lo1[p[u]];
+            h0[u] = o0[p[u]];
+            h1[u] = o1[p[u]];
+          }
+#pragma unroll
+        for (int u = 0; u < 4; u++)
+          if (u < cnt && p[u] >= 0) {
+            if (l0[u] != 0.0f) {
+              o0[p[u]] = __fadd_rn(h0[u], l0[u]);
+              lo0[p[u]] = 0.0f;
+            }
+            if (l1[u] != 0.0f) {
+              o1[p[u]] = __fadd_rn(h1[u], l1[u]);
+              lo1[p[u]] = 0.0f;
+            }
+          }
+      }
+      continue;
+    }
     while (m) {
       int b = __ffs(m) - 1;
       m &= m - 1;
