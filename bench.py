@@ -298,11 +298,12 @@ def run_ours(args):
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
     peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
     # roofline of the dominant phase, the HEALPix paint (k_paint_halos, the fused
-    # enumerate-and-paint kernel, ~90% of it, plus k_paint_full for the large halos), timed
-    # by CUDA events on the paint stream around the two launches.  Algorithmic bytes per
-    # launch, the per-unit figure of the two-float accumulator: 16 B per pixel update and
-    # map (read-modify-write of hi + lo), U = pixel updates summed over the maps.
-    paint_ms = phases["paint"] + phases["paint_big"]
+    # enumerate-and-paint kernel, ~90% of it, and k_paint_full for the large halos on a side
+    # stream), timed by CUDA events on the paint stream from before the two launches to
+    # their join.  Algorithmic bytes per launch, the per-unit figure of the two-float
+    # accumulator: 16 B per pixel update and map (read-modify-write of hi + lo), U = pixel
+    # updates summed over the maps.
+    paint_ms = phases["paint"]
     alg_paint = upd * 16
     achieved = alg_paint / (paint_ms * 1e-3) / 1e9 if paint_ms > 0 else None
     # DRAM traffic of the paint from the ncu capture of a smaller case (1e7 halos at

@@ -30,8 +30,8 @@ void p2m_philox4x32(const uint32_t c[4], const uint32_t k[2], uint32_t out[4]);
 /* Device time (ms) of each phase of the last paint call and of the last map read-out,
    for a context created with P2M_FLAG_TIMING: [0] cut, [1] per-halo set-up, [2] ring
    offsets of the large halos, [3] their ring spans, [4] flat sky, [5] their candidate
-   offsets, [6] HEALPix paint of the other halos (fused enumeration), [7] HEALPix paint
-   of the large halos, [8] read-out.  Diagnostics only (the reference prints no
+   offsets, [6] HEALPix paint (both painting kernels, which run concurrently), [7] the
+   large halos' painting kernel alone, [8] read-out.  Diagnostics only (the reference prints no
    timings). */
 struct p2m_ctx;
 int32_t p2m_get_timings(struct p2m_ctx *ctx, double *ms, int32_t n);

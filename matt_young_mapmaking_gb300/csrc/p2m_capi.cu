@@ -431,12 +431,20 @@ p2m_status sweep(p2m_ctx *ctx, cudaStream_t s) {
   }
   TE(PH_GROUP);
   SweepBuffers W = sweep_buffers(ctx);
-  TB(PH_PAINT);
+  TB(PH_PAINT); /* the paint phase spans both painting kernels */
+  if (n > 0) {
+    /* the large halos' items are painted on the side stream, beside the fused kernel's
+       uneven tail; the read-out waits for both */
+    CK(cudaEventRecord(ctx->ev_zero_start, s));
+    CK(cudaStreamWaitEvent(ctx->zstream, ctx->ev_zero_start, 0));
+    tmark(ctx, PH_PAINT_BIG, 0, ctx->zstream);
+    p2m_launch_paint_full(P, W, ctx->zstream, ctx->nsm);
+    tmark(ctx, PH_PAINT_BIG, 1, ctx->zstream);
+    CK(cudaEventRecord(ctx->ev_zero_done, ctx->zstream));
+  }
   p2m_launch_paint_halos(P, W, s, ctx->nsm);
+  if (n > 0) CK(cudaStreamWaitEvent(s, ctx->ev_zero_done, 0));
   TE(PH_PAINT);
-  TB(PH_PAINT_BIG);
-  if (n > 0) p2m_launch_paint_full(P, W, s, ctx->nsm);
-  TE(PH_PAINT_BIG);
   TB(PH_READOUT);
   if (compensated(ctx)) {
     /* fold the sparse low words into the maps and clear them */

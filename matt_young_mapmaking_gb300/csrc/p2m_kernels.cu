@@ -648,15 +648,11 @@ __device__ __forceinline__ void deposit_maps(const PaintParams &P, const HotHalo
    and the bilinear-in-(chi, M), linear-in-log r blend uses corner weights formed once
    and fused multiply-adds (a few ulp from the reference's sequence, far inside the
    mixed path's tolerance).  Other map sets and clamped corners use deposit_maps. */
-template <int ACC>
-__device__ __forceinline__ void deposit_mixed(const PaintParams &P, const HotHalo &H,
-                                              long long slot, int ir, float fr,
-                                              const SweepBuffers *W) {
+__device__ __forceinline__ bool paired_values(const PaintParams &P, const HotHalo &H, int ir,
+                                              float fr, float &v1, float &v2) {
   if (!P.paired || H.cb[0] < 0 || H.cb[1] < 0 || H.cb[2] < 0 || H.cb[3] < 0 || ir < 1 ||
-      ir >= P.th.nrt) {
-    deposit_maps<ACC>(P, H, W->acc, slot, ir, fr, W);
-    return;
-  }
+      ir >= P.th.nrt)
+    return false;
   const float2 *tab = (const float2 *)P.tables[P.map_table[0]];
   const int r = ir - 1; /* (cb + 2 (ir - 1)) / 2: the (profile 1, profile 2) pair at ir */
   const float2 a0 = __ldg(tab + (H.cb[0] >> 1) + r), b0 = __ldg(tab + (H.cb[0] >> 1) + r + 1);
@@ -665,20 +661,62 @@ __device__ __forceinline__ void deposit_mixed(const PaintParams &P, const HotHal
   const float2 a3 = __ldg(tab + (H.cb[3] >> 1) + r), b3 = __ldg(tab + (H.cb[3] >> 1) + r + 1);
   const float ofr = 1.0f - fr, fc = H.fc, fm = H.fm, ofc = 1.0f - fc, ofm = 1.0f - fm;
   const float w0 = ofc * ofm, w1 = fc * ofm, w2 = ofc * fm, w3 = fc * fm;
-  float v1 = w0 * fmaf(a0.x, ofr, b0.x * fr);
-  v1 = fmaf(w1, fmaf(a1.x, ofr, b1.x * fr), v1);
-  v1 = fmaf(w2, fmaf(a2.x, ofr, b2.x * fr), v1);
-  v1 = fmaf(w3, fmaf(a3.x, ofr, b3.x * fr), v1);
-  float v2 = w0 * fmaf(a0.y, ofr, b0.y * fr);
-  v2 = fmaf(w1, fmaf(a1.y, ofr, b1.y * fr), v2);
-  v2 = fmaf(w2, fmaf(a2.y, ofr, b2.y * fr), v2);
-  v2 = fmaf(w3, fmaf(a3.y, ofr, b3.y * fr), v2);
+  float p1 = w0 * fmaf(a0.x, ofr, b0.x * fr);
+  p1 = fmaf(w1, fmaf(a1.x, ofr, b1.x * fr), p1);
+  p1 = fmaf(w2, fmaf(a2.x, ofr, b2.x * fr), p1);
+  p1 = fmaf(w3, fmaf(a3.x, ofr, b3.x * fr), p1);
+  float p2 = w0 * fmaf(a0.y, ofr, b0.y * fr);
+  p2 = fmaf(w1, fmaf(a1.y, ofr, b1.y * fr), p2);
+  p2 = fmaf(w2, fmaf(a2.y, ofr, b2.y * fr), p2);
+  p2 = fmaf(w3, fmaf(a3.y, ofr, b3.y * fr), p2);
+  v1 = H.w1 * p1;
+  v2 = H.w2 * p2;
+  return true;
+}
+
+template <int ACC>
+__device__ __forceinline__ void deposit_mixed(const PaintParams &P, const HotHalo &H,
+                                              long long slot, int ir, float fr,
+                                              const SweepBuffers *W) {
   float vals[P2M_MAXMAPS];
 #pragma unroll
   for (int m = 0; m < P2M_MAXMAPS; m++) vals[m] = 0.0f;
-  vals[0] = H.w1 * v1;
-  vals[1] = H.w2 * v2;
+  if (!paired_values(P, H, ir, fr, vals[0], vals[1])) {
+    deposit_maps<ACC>(P, H, W->acc, slot, ir, fr, W);
+    return;
+  }
   accumulate_vals<ACC>(P, W->acc, slot, vals, W);
+}
+
+/* A compensated deposit of the paired maps split in two: the atomic adds are issued at
+   once, the TwoSum of their returned old values is finished one candidate later, so the
+   atomics' round trip overlaps the next candidate's decision and table reads. */
+struct PendingDeposit {
+  long long slot; /* -1: none */
+  float v0, v1, o0, o1;
+};
+
+__device__ __forceinline__ void finish_pending(const SweepBuffers &W, PendingDeposit &d) {
+  if (d.slot < 0) return;
+  bool any = false;
+  if (d.v0 != 0.0f) {
+    const float sm = __fadd_rn(d.o0, d.v0), bb = __fsub_rn(sm, d.o0);
+    const float err = __fadd_rn(__fsub_rn(d.o0, __fsub_rn(sm, bb)), __fsub_rn(d.v0, bb));
+    if (err != 0.0f) {
+      atomicAdd(W.lo + d.slot, err);
+      any = true;
+    }
+  }
+  if (d.v1 != 0.0f) {
+    const float sm = __fadd_rn(d.o1, d.v1), bb = __fsub_rn(sm, d.o1);
+    const float err = __fadd_rn(__fsub_rn(d.o1, __fsub_rn(sm, bb)), __fsub_rn(d.v1, bb));
+    if (err != 0.0f) {
+      atomicAdd(W.lo + W.npix + d.slot, err);
+      any = true;
+    }
+  }
+  if (any) W.tiles[d.slot >> P2M_TILE_SHIFT] = 1;
+  d.slot = -1;
 }
 
 /* haloproject.f90:136-152: one warp per (halo, row); every operation is the
@@ -851,7 +889,7 @@ template <int EXACT, int ACC>
 __device__ __forceinline__ void paint_pixel(const PaintParams &P, const SweepBuffers &W,
                                             const RingItem &it, const HotHalo &H, int k,
                                             long long pix, unsigned int &nupd,
-                                            unsigned int &nrc) {
+                                            unsigned int &nrc, PendingDeposit *pend = nullptr) {
   int ir = 0;
   float fr = 0.0f, u = 0.0f;
   bool zero_val = H.zero;
@@ -885,8 +923,22 @@ __device__ __forceinline__ void paint_pixel(const PaintParams &P, const SweepBuf
   if (P.flags & 1)
     record_set(W.set_rec, W.set_pix, W.set_cap, &W.ctr->n_sets, W.halos[it.halo].rec, pix);
   if (zero_val || H.zero) return;
-  if (EXACT) deposit_maps<ACC>(P, H, W.acc, pix, ir, fr, &W);
-  else deposit_mixed<ACC>(P, H, pix, ir, fr, &W);
+  if (EXACT) {
+    deposit_maps<ACC>(P, H, W.acc, pix, ir, fr, &W);
+  } else if (ACC == 2 && pend) {
+    float v0, v1;
+    if (paired_values(P, H, ir, fr, v0, v1)) {
+      pend->slot = pix;
+      pend->v0 = v0;
+      pend->v1 = v1;
+      pend->o0 = v0 != 0.0f ? atomicAdd(W.out[0] + pix, v0) : 0.0f;
+      pend->o1 = v1 != 0.0f ? atomicAdd(W.out[1] + pix, v1) : 0.0f;
+    } else {
+      deposit_mixed<ACC>(P, H, pix, ir, fr, &W);
+    }
+  } else {
+    deposit_mixed<ACC>(P, H, pix, ir, fr, &W);
+  }
 }
 
 /* loads items g0..g0+31 (below ihi) and their halos' hot fields into the warp's cache */
@@ -1013,7 +1065,7 @@ __device__ __forceinline__ int warp_find(int key, int t) {
 }
 
 #ifndef P2M_HALOS_MINBLOCKS
-#define P2M_HALOS_MINBLOCKS 4 /* resident blocks per SM the register budget must allow */
+#define P2M_HALOS_MINBLOCKS 3 /* resident blocks per SM the register budget must allow */
 #endif
 
 /* per-warp shared-memory stage of the fused painter: the disc geometry and
@@ -1044,6 +1096,9 @@ __global__ void __launch_bounds__(256, P2M_HALOS_MINBLOCKS) k_paint_halos(PaintP
   const long long nh = W.n_halos;
   unsigned int nupd = 0, nrc = 0;
   unsigned long long ncand = 0;
+  PendingDeposit pend;
+  pend.slot = -1;
+  pend.v0 = pend.v1 = pend.o0 = pend.o1 = 0.0f;
   for (;;) {
     long long h0 = 0;
     if (lane == 0) h0 = 32LL * (long long)atomicAdd(&W.ctr->next_unit, 1u);
@@ -1108,6 +1163,9 @@ __global__ void __launch_bounds__(256, P2M_HALOS_MINBLOCKS) k_paint_halos(PaintP
         const int c = c0 + lane;
         const int i = warp_find(cex, c);
         const int k = c - __shfl_sync(FULL, cex, i);
+        PendingDeposit nd;
+        nd.slot = -1;
+        nd.v0 = nd.v1 = nd.o0 = nd.o1 = 0.0f;
         if (c < ctot) {
           RingItem ci;
           const int jj = S.ij[i];
@@ -1123,12 +1181,18 @@ __global__ void __launch_bounds__(256, P2M_HALOS_MINBLOCKS) k_paint_halos(PaintP
           int iphi = ci.lo + k;
           if (iphi < 0) iphi += np;
           if (iphi >= np) iphi -= np;
-          paint_pixel<EXACT, ACC>(P, W, ci, S.hot[jj], k, S.irb[i] + iphi, nupd, nrc);
+          paint_pixel<EXACT, ACC>(P, W, ci, S.hot[jj], k, S.irb[i] + iphi, nupd, nrc,
+                                  ACC == 2 ? &nd : nullptr);
+        }
+        if (ACC == 2) {
+          finish_pending(W, pend); /* the previous candidate's adds have returned by now */
+          pend = nd;
         }
       }
       if (lane == 0) ncand += (unsigned long long)ctot;
     }
   }
+  if (ACC == 2) finish_pending(W, pend);
   warp_count(&W.ctr->hp_updates, nupd);
   warp_count(&W.ctr->n_recheck, nrc);
   warp_count(&W.ctr->n_cand, ncand);
