@@ -126,6 +126,45 @@ __global__ void __launch_bounds__(256) k_cut(PaintParams P, IngestBuffers B, lon
 
 /* -------------------------------------------------------------- ingest: set-up ----- */
 
+/* float-float numbers (hi + lo, |lo| <= ulp(hi)/2) built with error-free transformations
+   (Dekker / Knuth two-product and two-sum through fmaf); ~44-bit precision at FP32 cost */
+struct ffloat {
+  float h, l;
+};
+
+__device__ __forceinline__ ffloat ff_sq(float a) {
+  const float p = __fmul_rn(a, a);
+  return {p, __fmaf_rn(a, a, -p)};
+}
+
+__device__ __forceinline__ ffloat ff_norm(float s, float e) {
+  const float h = __fadd_rn(s, e);
+  return {h, __fsub_rn(e, __fsub_rn(h, s))};
+}
+
+__device__ __forceinline__ ffloat ff_add(ffloat x, ffloat y) {
+  const float s = __fadd_rn(x.h, y.h);
+  const float bb = __fsub_rn(s, x.h);
+  float e = __fadd_rn(__fsub_rn(x.h, __fsub_rn(s, bb)), __fsub_rn(y.h, bb));
+  e = __fadd_rn(e, __fadd_rn(x.l, y.l));
+  return ff_norm(s, e);
+}
+
+/* sqrt with one Newton correction of the correctly rounded FP32 root */
+__device__ __forceinline__ ffloat ff_sqrt(ffloat x) {
+  const float y = __fsqrt_rn(x.h);
+  const float r = __fadd_rn(__fmaf_rn(-y, y, x.h), x.l);
+  return ff_norm(y, __fdiv_rn(r, __fmul_rn(2.0f, y)));
+}
+
+/* x / y with one correction of the FP32 quotient (exact remainder through fmaf) */
+__device__ __forceinline__ ffloat ff_div(ffloat x, ffloat y) {
+  const float q = __fdiv_rn(x.h, y.h);
+  float r = __fmaf_rn(-q, y.h, x.h);
+  r = __fsub_rn(__fadd_rn(r, x.l), __fmul_rn(q, y.l));
+  return ff_norm(q, __fdiv_rn(r, y.h));
+}
+
 /* geometry, thresholds and interpolation constants of one halo from its loop
    quantities (pks2map.f90:284-298 outputs) */
 __device__ void halo_geometry(const PaintParams &P, float xh, float yh, float zh, float rh,
@@ -195,16 +234,23 @@ __device__ void halo_geometry(const PaintParams &P, float xh, float yh, float zh
     if ((double)T > P2M_HP_PI || !(T >= 0.0f)) {
       atomicOr(err, (unsigned)P2M_DEVERR_RADIUS); /* query_disc aborts on radius > pi */
     } else {
-      double a = (double)H.hv[0], b = (double)H.hv[1], c = (double)H.hv[2];
-      double rxy = DSQRT(DADD(DMUL(a, a), DMUL(b, b)));
-      double nrm = DSQRT(DADD(DADD(DMUL(a, a), DMUL(b, b)), DMUL(c, c)));
-      double z0 = DDIV(c, nrm), s0 = DDIV(rxy, nrm);
-      double phi0 = (a != 0.0 || b != 0.0) ? atan2(b, a) : 0.0;
-      double pf = phi0 / P2M_HP_TWOPI;
-      H.z0h = (float)z0;
-      H.z0l = (float)(z0 - (double)H.z0h);
-      H.s0h = (float)s0;
-      H.s0l = (float)(s0 - (double)H.s0h);
+      /* unit centre z = c / |v|, sin(theta) = sqrt(a^2 + b^2) / |v| in float-float (the
+         squares of the float components are exact as float-float pairs); phi / 2pi from
+         the FP64 atan2 */
+      const float a = H.hv[0], b = H.hv[1], c = H.hv[2];
+      const ffloat ss = ff_add(ff_sq(a), ff_sq(b));
+      const ffloat nn = ff_add(ss, ff_sq(c));
+      if (nn.h > 0.0f) {
+        const ffloat nrm = ff_sqrt(nn);
+        const ffloat z0 = ff_div({c, 0.0f}, nrm);
+        const ffloat s0 = ss.h > 0.0f ? ff_div(ff_sqrt(ss), nrm) : ffloat{0.0f, 0.0f};
+        H.z0h = z0.h;
+        H.z0l = z0.l;
+        H.s0h = s0.h;
+        H.s0l = s0.l;
+      }
+      double phi0 = (a != 0.0f || b != 0.0f) ? atan2((double)b, (double)a) : 0.0;
+      double pf = phi0 * (1.0 / P2M_HP_TWOPI);
       H.p0h = (float)pf;
       H.p0l = (float)(pf - (double)H.p0h);
       H.C_in = chord2(T * (1.0f - 2e-6f));
