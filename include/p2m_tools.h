@@ -28,7 +28,8 @@ int32_t p2m_generate_catalogue(uint64_t seed, int64_t first, int64_t n, int32_t 
 void p2m_philox4x32(const uint32_t c[4], const uint32_t k[2], uint32_t out[4]);
 
 /* Device time (ms) of each phase of the last paint call and of the last map read-out,
-   for a context created with P2M_FLAG_TIMING: [0] cut, [1] per-halo set-up, [2] ring
+   for a context created with P2M_FLAG_TIMING: [0] cut with the per-halo set-up of
+   catalogue records (one kernel), [1] set-up of p2m_project_halo batches, [2] ring
    offsets of the large halos, [3] their ring spans, [4] flat sky, [5] their candidate
    offsets, [6] HEALPix paint (both painting kernels, which run concurrently), [7] the
    large halos' painting kernel alone, [8] read-out.  Diagnostics only (the reference prints no

@@ -60,8 +60,6 @@ struct p2m_ctx {
   /* per-call buffers */
   float *d_records = nullptr;
   long long cap_rec_floats = 0;
-  int *d_surv = nullptr;
-  long long cap_surv = 0;
   unsigned int *d_nring = nullptr;
   long long cap_nring = 0;
   long long *d_ioff = nullptr;
@@ -215,7 +213,6 @@ IngestBuffers ingest_buffers(const p2m_ctx *ctx, const float *records) {
   memset(&B, 0, sizeof(B));
   B.records = records;
   B.rec_base = ctx->rec_count;
-  B.surv = ctx->d_surv;
   B.halos = ctx->d_halos + ctx->n_halos;
   B.halo_base = ctx->n_halos;
   B.nring = ctx->d_nring;
@@ -318,7 +315,6 @@ p2m_status wait_zero(p2m_ctx *ctx, cudaStream_t s) {
 
 p2m_status begin_call(p2m_ctx *ctx, long long n, cudaStream_t s) {
   ST(zero_outputs(ctx, s));
-  CK(grow(&ctx->d_surv, &ctx->cap_surv, std::max(n, 1LL)));
   CK(grow(&ctx->d_nring, &ctx->cap_nring, std::max(n, 1LL)));
   CK(grow(&ctx->d_ioff, &ctx->cap_ioff, std::max(n, 1LL)));
   CK(grow(&ctx->d_halos, &ctx->cap_halos, ctx->n_halos + std::max(n, 1LL), ctx->n_halos, s));
@@ -364,11 +360,8 @@ p2m_status ingest_device(p2m_ctx *ctx, const float *d_rec, long long nrec, int n
   PaintParams P = make_params(ctx, nfloat);
   IngestBuffers B = ingest_buffers(ctx, d_rec);
   TB(PH_CUT);
-  p2m_launch_cut(P, B, nrec, s, ctx->nsm);
+  p2m_launch_cut_setup(P, B, nrec, s, ctx->nsm);
   TE(PH_CUT);
-  TB(PH_SETUP);
-  p2m_launch_setup(P, B, nrec, s, ctx->nsm);
-  TE(PH_SETUP);
   p2m_status st = ingest_tail(ctx, P, nrec, s);
   join_out(ctx, s);
   if (st) return st;
@@ -568,7 +561,6 @@ p2m_status p2m_create(const p2m_config *cfg, p2m_ctx **out) {
     CK(cudaMalloc((void **)&ctx->d_set_pix, sizeof(long long) * (size_t)ctx->cap_set));
   }
   long long nrec = std::max<long long>(cfg->max_records, 1024);
-  CK(grow(&ctx->d_surv, &ctx->cap_surv, nrec));
   CK(grow(&ctx->d_nring, &ctx->cap_nring, nrec));
   CK(grow(&ctx->d_ioff, &ctx->cap_ioff, nrec));
   CK(grow(&ctx->d_halos, &ctx->cap_halos, nrec / 4 + 1024));
@@ -583,7 +575,7 @@ void p2m_destroy(p2m_ctx *ctx) {
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   if (ctx->zstream) cudaStreamSynchronize(ctx->zstream);
   void *ptrs[] = {ctx->d_rofz, ctx->d_zofr, ctx->d_ringtab, ctx->d_acc64, ctx->d_fs_acc,
-                  ctx->d_fs_out, ctx->d_halos, ctx->d_items_raw, ctx->d_records, ctx->d_surv,
+                  ctx->d_fs_out, ctx->d_halos, ctx->d_items_raw, ctx->d_records,
                   ctx->d_nring, ctx->d_ioff, ctx->d_fs_items, ctx->d_scan_tmp, ctx->d_counts,
                   ctx->d_pix_off, ctx->d_nitems, ctx->d_sums, ctx->d_set_rec, ctx->d_set_pix,
                   ctx->d_ctr, ctx->d_prep, ctx->d_lo, ctx->d_tiles};

@@ -3,10 +3,10 @@
  *
  * A paint call ingests catalogue records; the HEALPix maps are produced by a sweep when
  * they are read.  Ingest (one stream, one host round trip to size the item buffer):
- *   k_cut      records -> halos inside the radial cut with mass >= mmin whose table
- *              value is not identically zero (block-aggregated compaction)
- *   k_setup    per halo: the loop quantities of pks2map.f90:284-298, disc radius and
- *              centre, interpolation constants, candidate ring range, flat-sky box
+ *   k_cut_setup  records -> halos inside the radial cut with mass >= mmin whose table
+ *              value is not identically zero, queued in shared memory, and per queued
+ *              halo the loop quantities of pks2map.f90:284-298, disc radius and centre,
+ *              interpolation constants, candidate ring range, flat-sky box
  *   scan       rings of the large halos (more than big_rings rings) -> item offsets
  *   k_items    per (large halo, ring) item: FP32 superset of the ring's pixel span and
  *              the ring constants of the disc test
@@ -110,7 +110,6 @@ struct PaintParams {
 struct IngestBuffers {
   const float *records;
   long long rec_base;   /* record index of records[0] */
-  int *surv;            /* record indices of enumerated halos (call-local) */
   HaloRec *halos;       /* halos[0..n_surv) of this call */
   long long halo_base;  /* global index of halos[0] */
   unsigned int *nring;  /* rings per large halo, 0 for the others */
@@ -143,10 +142,8 @@ struct SweepBuffers {
 };
 
 /* launchers (p2m_kernels.cu) */
-void p2m_launch_cut(const PaintParams &P, const IngestBuffers &B, long long n, cudaStream_t s,
-                    int nsm);
-void p2m_launch_setup(const PaintParams &P, const IngestBuffers &B, long long n_max,
-                      cudaStream_t s, int nsm);
+void p2m_launch_cut_setup(const PaintParams &P, const IngestBuffers &B, long long n,
+                          cudaStream_t s, int nsm);
 void p2m_launch_setup_prepared(const PaintParams &P, const IngestBuffers &B, const float *prep,
                                long long n, cudaStream_t s, int nsm);
 void p2m_launch_scan_u32(const unsigned int *in, const unsigned long long *n_ptr, long long *out,

@@ -12,6 +12,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
+
 #include "../../include/p2m_tools.h"
 #include "p2m_internal.h"
 
@@ -64,64 +66,26 @@ __device__ __forceinline__ p2m_hinterp halo_hinterp(const HaloRec &H) {
 #define CUT_PER_THREAD 8
 
 /* radial cut (pks2map.f90:144-160), mass cut (:264, :296), and the table's chi bound
-   (maptable.f90:184,188: chi = rofz(zofr(chi)) > chimaxt paints zeros) */
-__global__ void __launch_bounds__(256) k_cut(PaintParams P, IngestBuffers B, long long n) {
-  __shared__ int wsum[8];
-  __shared__ long long base_s;
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  unsigned long long nshell = 0, nmass = 0, nkeep = 0;
-  const long long tile = (long long)blockDim.x * CUT_PER_THREAD;
-  for (long long t0 = (long long)blockIdx.x * tile; t0 < n; t0 += (long long)gridDim.x * tile) {
-    unsigned keepbits = 0;
-#pragma unroll
-    for (int k = 0; k < CUT_PER_THREAD; k++) {
-      long long i = t0 + (long long)k * blockDim.x + threadIdx.x;
-      if (i >= n) continue;
-      const float *r = B.records + i * P.nfloat;
-      float p0 = __ldg(r + 0), p1 = __ldg(r + 1), p2 = __ldg(r + 2), rth = __ldg(r + 6);
-      if (!(p2m_isfinite(p0) && p2m_isfinite(p1) && p2m_isfinite(p2) && p2m_isfinite(rth))) continue;
-      float xh = FSUB(p2, P.chihview), yh = p1, zh = p0;
-      float chih = FSQRT(FADD(FADD(FMUL(xh, xh), FMUL(yh, yh)), FMUL(zh, zh)));
-      bool shell = !(chih > P.cut_high || chih < P.cut_low);
-      float mass = FMUL(P.mass_fac, FMUL(FMUL(rth, rth), rth));
-      bool massive = shell && !(mass < 1e13f);
-      bool keep = massive;
-      if (massive && !(P.flags & 2)) {
-        float chi0 = FSQRT(FADD(FADD(FMUL(p2, p2), FMUL(p1, p1)), FMUL(p0, p0)));
-        float z = p2m_lookup(P.zofr, P.cosmo.dzofr, chi0);
-        keep = !(p2m_lookup(P.rofz, P.cosmo.drofz, z) > P.th.chimaxt);
-      }
-      nshell += shell;
-      nmass += massive;
-      if (keep) keepbits |= 1u << k;
-    }
-    int cnt = __popc(keepbits);
-    nkeep += cnt;
-    int x = cnt;
-    for (int o = 1; o < 32; o <<= 1) {
-      int y = __shfl_up_sync(FULL, x, o);
-      if (lane >= o) x += y;
-    }
-    if (lane == 31) wsum[wid] = x;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      int tot = 0;
-      for (int w = 0; w < 8; w++) {
-        int v = wsum[w];
-        wsum[w] = tot;
-        tot += v;
-      }
-      base_s = tot ? (long long)atomicAdd(&B.ctr->n_surv, (unsigned long long)tot) : 0;
-    }
-    __syncthreads();
-    long long pos = base_s + wsum[wid] + (x - cnt);
-    for (int k = 0; k < CUT_PER_THREAD; k++)
-      if (keepbits & (1u << k)) B.surv[pos++] = (int)(t0 + (long long)k * blockDim.x + threadIdx.x);
-    __syncthreads();
+   (maptable.f90:184,188: chi = rofz(zofr(chi)) > chimaxt paints zeros) of one record;
+   true if the record is enumerated */
+__device__ __forceinline__ bool cut_record(const PaintParams &P, const float *r, bool &shell,
+                                           bool &massive) {
+  shell = massive = false;
+  float p0 = __ldg(r + 0), p1 = __ldg(r + 1), p2 = __ldg(r + 2), rth = __ldg(r + 6);
+  if (!(p2m_isfinite(p0) && p2m_isfinite(p1) && p2m_isfinite(p2) && p2m_isfinite(rth)))
+    return false;
+  float xh = FSUB(p2, P.chihview), yh = p1, zh = p0;
+  float chih = FSQRT(FADD(FADD(FMUL(xh, xh), FMUL(yh, yh)), FMUL(zh, zh)));
+  shell = !(chih > P.cut_high || chih < P.cut_low);
+  float mass = FMUL(P.mass_fac, FMUL(FMUL(rth, rth), rth));
+  massive = shell && !(mass < 1e13f);
+  bool keep = massive;
+  if (massive && !(P.flags & 2)) {
+    float chi0 = FSQRT(FADD(FADD(FMUL(p2, p2), FMUL(p1, p1)), FMUL(p0, p0)));
+    float z = p2m_lookup(P.zofr, P.cosmo.dzofr, chi0);
+    keep = !(p2m_lookup(P.rofz, P.cosmo.drofz, z) > P.th.chimaxt);
   }
-  block_count(&B.ctr->n_shell, nshell);
-  block_count(&B.ctr->n_massive, nmass);
-  block_count(&B.ctr->n_enum, nkeep);
+  return keep;
 }
 
 /* -------------------------------------------------------------- ingest: set-up ----- */
@@ -278,13 +242,10 @@ __device__ __forceinline__ void store_halo(const PaintParams &P, const IngestBuf
   if (H.jmin <= H.jmax && H.kmin <= H.kmax) fsrows += (unsigned long long)(H.kmax - H.kmin + 1);
 }
 
-/* per-halo set-up from a catalogue record (pks2map.f90:264, :284-298) */
-__global__ void __launch_bounds__(256) k_setup(PaintParams P, IngestBuffers B) {
-  long long n = (long long)B.ctr->n_surv;
-  unsigned long long fsrows = 0;
-  for (long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x; s < n;
-       s += (long long)gridDim.x * blockDim.x) {
-    int i = B.surv[s];
+/* per-halo set-up of record i as halo s (pks2map.f90:264, :284-298) */
+__device__ __forceinline__ void setup_record(const PaintParams &P, const IngestBuffers &B,
+                                             long long s, int i, unsigned long long &fsrows) {
+  {
     const float *r = B.records + (long long)i * P.nfloat;
     float p0 = r[0], p1 = r[1], p2 = r[2], rth = r[6];
     float mass = FMUL(P.mass_fac, FMUL(FMUL(rth, rth), rth));
@@ -311,6 +272,77 @@ __global__ void __launch_bounds__(256) k_setup(PaintParams P, IngestBuffers B) {
     halo_geometry(P, xh, yh, zh, rh, chih, mh, redshift, H, &B.ctr->err);
     store_halo(P, B, s, H, fsrows);
   }
+}
+
+#define CS_QCAP (256 + 256 * CUT_PER_THREAD)
+
+/* The cut and the set-up in one pass: each block cuts tiles of 2048 records into a
+   shared-memory queue of survivors and sets up 256 of them (one per thread) whenever the
+   queue holds that many, so the FP64-heavy set-up of some warps overlaps the catalogue
+   stream of others and the survivor list never goes through global memory.  Halo slots
+   are reserved 256 at a time. */
+__global__ void __launch_bounds__(256) k_cut_setup(PaintParams P, IngestBuffers B, long long n) {
+  __shared__ int q[CS_QCAP];
+  __shared__ int wsum[8];
+  __shared__ int qn, tile_n;
+  __shared__ long long base_s;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  unsigned long long nshell = 0, nmass = 0, nkeep = 0, fsrows = 0;
+  if (threadIdx.x == 0) qn = 0;
+  const long long tile = (long long)blockDim.x * CUT_PER_THREAD;
+  for (long long t0 = (long long)blockIdx.x * tile; t0 < n; t0 += (long long)gridDim.x * tile) {
+    unsigned keepbits = 0;
+#pragma unroll
+    for (int k = 0; k < CUT_PER_THREAD; k++) {
+      long long i = t0 + (long long)k * blockDim.x + threadIdx.x;
+      if (i >= n) continue;
+      bool shell, massive;
+      if (cut_record(P, B.records + i * P.nfloat, shell, massive)) keepbits |= 1u << k;
+      nshell += shell;
+      nmass += massive;
+    }
+    int cnt = __popc(keepbits);
+    nkeep += cnt;
+    int x = cnt;
+    for (int o = 1; o < 32; o <<= 1) {
+      int y = __shfl_up_sync(FULL, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) wsum[wid] = x;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int tot = 0;
+      for (int w = 0; w < 8; w++) {
+        int v = wsum[w];
+        wsum[w] = tot;
+        tot += v;
+      }
+      tile_n = tot;
+    }
+    __syncthreads();
+    int pos = qn + wsum[wid] + (x - cnt);
+    for (int k = 0; k < CUT_PER_THREAD; k++)
+      if (keepbits & (1u << k)) q[pos++] = (int)(t0 + (long long)k * blockDim.x + threadIdx.x);
+    __syncthreads();
+    if (threadIdx.x == 0) qn += tile_n;
+    __syncthreads();
+    while (qn >= 256) {
+      if (threadIdx.x == 0) base_s = (long long)atomicAdd(&B.ctr->n_surv, 256ull);
+      __syncthreads();
+      setup_record(P, B, base_s + threadIdx.x, q[qn - 256 + threadIdx.x], fsrows);
+      __syncthreads();
+      if (threadIdx.x == 0) qn -= 256;
+      __syncthreads();
+    }
+  }
+  if (qn > 0) {
+    if (threadIdx.x == 0) base_s = (long long)atomicAdd(&B.ctr->n_surv, (unsigned long long)qn);
+    __syncthreads();
+    if ((int)threadIdx.x < qn) setup_record(P, B, base_s + threadIdx.x, q[threadIdx.x], fsrows);
+  }
+  block_count(&B.ctr->n_shell, nshell);
+  block_count(&B.ctr->n_massive, nmass);
+  block_count(&B.ctr->n_enum, nkeep);
   block_count(&B.ctr->n_fs_rows, fsrows);
 }
 
@@ -1540,13 +1572,17 @@ static inline int grid_for(long long n, int block, int nsm, int per_sm) {
   return (int)g;
 }
 
-void p2m_launch_cut(const PaintParams &P, const IngestBuffers &B, long long n, cudaStream_t s,
-                    int nsm) {
-  k_cut<<<grid_for((n + CUT_PER_THREAD - 1) / CUT_PER_THREAD, 256, nsm, 8), 256, 0, s>>>(P, B, n);
-}
-void p2m_launch_setup(const PaintParams &P, const IngestBuffers &B, long long n_max,
-                      cudaStream_t s, int nsm) {
-  k_setup<<<grid_for(n_max, 256, nsm, 8), 256, 0, s>>>(P, B);
+void p2m_launch_cut_setup(const PaintParams &P, const IngestBuffers &B, long long n,
+                          cudaStream_t s, int nsm) {
+  /* one resident wave: each block streams its tiles and sets up its own survivors */
+  static int per_sm = 0;
+  if (!per_sm &&
+      (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cut_setup, 256, 0) != cudaSuccess ||
+       per_sm < 1))
+    per_sm = 1;
+  long long tiles = (n + 256LL * CUT_PER_THREAD - 1) / (256LL * CUT_PER_THREAD);
+  long long g = std::min<long long>(tiles, (long long)nsm * per_sm);
+  k_cut_setup<<<(int)std::max<long long>(g, 1), 256, 0, s>>>(P, B, n);
 }
 void p2m_launch_setup_prepared(const PaintParams &P, const IngestBuffers &B, const float *prep,
                                long long n, cudaStream_t s, int nsm) {
