@@ -33,6 +33,7 @@ struct p2m_ctx {
   std::vector<float> rofz_host, zofr_host;
   float *d_rofz = nullptr, *d_zofr = nullptr;
   float4 *d_ringtab = nullptr;
+  float4 *d_phitab = nullptr;
   p2m_tabhdr th;
   bool th_set = false;
   float *d_tab[P2M_MAXTABLES] = {};
@@ -195,6 +196,7 @@ PaintParams make_params(const p2m_ctx *ctx, int nfloat) {
   P.rofz = ctx->d_rofz;
   P.zofr = ctx->d_zofr;
   P.ringtab = ctx->d_ringtab;
+  P.phitab = ctx->d_phitab;
   P.band_u = ctx->band_u;
   P.inv_drt = ctx->th_set ? 1.0f / ctx->th.drt : 0.0f;
   P.big_rings = ctx->big_rings;
@@ -527,6 +529,15 @@ p2m_status p2m_create(const p2m_config *cfg, p2m_ctx **out) {
     }
     CK(cudaMalloc((void **)&ctx->d_ringtab, sizeof(float4) * (size_t)nr));
     CK(cudaMemcpy(ctx->d_ringtab, rt.data(), sizeof(float4) * (size_t)nr, cudaMemcpyHostToDevice));
+    /* cos and sin of the grid angles 2 pi k / M as (hi, lo) float pairs */
+    std::vector<float4> pt(P2M_PHITAB);
+    for (int k = 0; k < P2M_PHITAB; k++) {
+      double t = P2M_HP_TWOPI * (double)k / (double)P2M_PHITAB, c = cos(t), sn = sin(t);
+      float ch = (float)c, sh = (float)sn;
+      pt[(size_t)k] = make_float4(ch, (float)(c - (double)ch), sh, (float)(sn - (double)sh));
+    }
+    CK(cudaMalloc((void **)&ctx->d_phitab, sizeof(float4) * P2M_PHITAB));
+    CK(cudaMemcpy(ctx->d_phitab, pt.data(), sizeof(float4) * P2M_PHITAB, cudaMemcpyHostToDevice));
     ctx->hp_npix = 12LL * cfg->nside * cfg->nside;
     for (int m = 0; m < cfg->nmaps; m++) {
       CK(cudaMalloc((void **)&ctx->d_out_own[m], sizeof(float) * (size_t)ctx->hp_npix));
@@ -574,7 +585,7 @@ void p2m_destroy(p2m_ctx *ctx) {
   cudaSetDevice(ctx->cfg.device);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   if (ctx->zstream) cudaStreamSynchronize(ctx->zstream);
-  void *ptrs[] = {ctx->d_rofz, ctx->d_zofr, ctx->d_ringtab, ctx->d_acc64, ctx->d_fs_acc,
+  void *ptrs[] = {ctx->d_rofz, ctx->d_zofr, ctx->d_ringtab, ctx->d_phitab, ctx->d_acc64, ctx->d_fs_acc,
                   ctx->d_fs_out, ctx->d_halos, ctx->d_items_raw, ctx->d_records,
                   ctx->d_nring, ctx->d_ioff, ctx->d_fs_items, ctx->d_scan_tmp, ctx->d_counts,
                   ctx->d_pix_off, ctx->d_nitems, ctx->d_sums, ctx->d_set_rec, ctx->d_set_pix,

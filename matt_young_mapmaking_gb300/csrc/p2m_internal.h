@@ -29,6 +29,7 @@
 #define P2M_BIG_RINGS 64      /* default: halos spanning more rings go through the item buffer */
 #define P2M_TILE_SHIFT 5      /* compensated path: a flagged tile is 32 pixels (128 bytes) */
 #define P2M_TILE_PIX (1 << P2M_TILE_SHIFT)
+#define P2M_PHITAB 4096       /* grid angles 2 pi k / P2M_PHITAB of the disc-centre phi reduction */
 
 struct DevCounters {
   /* per call (cleared before every ingest call and every sweep) */
@@ -104,6 +105,7 @@ struct PaintParams {
   const float *tables[P2M_MAXTABLES];
   const float *rofz, *zofr;
   const float4 *ringtab; /* (z hi, z lo, sin theta hi, sin theta lo) of ring i at index i */
+  const float4 *phitab;  /* (cos hi, cos lo, sin hi, sin lo) of 2 pi k / P2M_PHITAB */
 };
 
 /* buffers of one ingest call */

@@ -121,6 +121,18 @@ __device__ __forceinline__ ffloat ff_sqrt(ffloat x) {
   return ff_norm(y, __fdiv_rn(r, __fmul_rn(2.0f, y)));
 }
 
+__device__ __forceinline__ ffloat ff_mul_f(ffloat x, float y) {
+  const float p = __fmul_rn(x.h, y);
+  return ff_norm(p, __fmaf_rn(x.l, y, __fmaf_rn(x.h, y, -p)));
+}
+
+__device__ __forceinline__ ffloat ff_mul(ffloat x, ffloat y) {
+  const float p = __fmul_rn(x.h, y.h);
+  float e = __fmaf_rn(x.h, y.h, -p);
+  e = __fmaf_rn(x.h, y.l, __fmaf_rn(x.l, y.h, e));
+  return ff_norm(p, e);
+}
+
 /* x / y with one correction of the FP32 quotient (exact remainder through fmaf) */
 __device__ __forceinline__ ffloat ff_div(ffloat x, ffloat y) {
   const float q = __fdiv_rn(x.h, y.h);
@@ -213,10 +225,26 @@ __device__ void halo_geometry(const PaintParams &P, float xh, float yh, float zh
         H.s0h = s0.h;
         H.s0l = s0.l;
       }
-      double phi0 = (a != 0.0f || b != 0.0f) ? atan2((double)b, (double)a) : 0.0;
-      double pf = phi0 * (1.0 / P2M_HP_TWOPI);
-      H.p0h = (float)pf;
-      H.p0l = (float)(pf - (double)H.p0h);
+      /* phi / 2pi by table-based reduction (Tang's method) in float-float: k = the grid
+         angle 2 pi k / M nearest the FP32 atan2; (a, b) rotated by -2 pi k / M leaves an
+         angle |d| < 8e-4 = atan(t) = t - t^3/3 (next term < 1e-16); phi / 2pi =
+         k / M (exact) + d / 2pi, good to ~1e-15 */
+      if (a != 0.0f || b != 0.0f) {
+        const float phi1 = atan2f(b, a);
+        const int k = __float2int_rn(phi1 * ((float)P2M_PHITAB / 6.28318531f));
+        const float4 cs = P.phitab[k & (P2M_PHITAB - 1)];
+        const ffloat cz = {cs.x, cs.y}, sz = {cs.z, cs.w};
+        const ffloat ap = ff_add(ff_mul_f(cz, a), ff_mul_f(sz, b));
+        const ffloat bp = ff_add(ff_mul_f(cz, b), ff_mul_f({-sz.h, -sz.l}, a));
+        const ffloat t = ff_div(bp, ap);
+        const float t3 = __fdiv_rn(__fmul_rn(__fmul_rn(t.h, t.h), t.h), 3.0f);
+        const ffloat d = ff_add(t, {-t3, 0.0f});
+        constexpr double kInv2pi = 1.0 / P2M_HP_TWOPI; /* folded at compile time */
+        const ffloat inv2pi = {(float)kInv2pi, (float)(kInv2pi - (double)(float)kInv2pi)};
+        const ffloat pf = ff_add({(float)k * (1.0f / (float)P2M_PHITAB), 0.0f}, ff_mul(d, inv2pi));
+        H.p0h = pf.h;
+        H.p0l = pf.l;
+      }
       H.C_in = chord2(T * (1.0f - 2e-6f));
       H.C_out = chord2(T * (1.0f + 2e-6f));
       float tspan = T * (1.0f + 2e-5f) + 1e-6f;
