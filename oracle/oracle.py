@@ -92,6 +92,12 @@ def lib():
         L.orc_paint.restype = I32
         L.orc_paint_threads.argtypes = [VP, VP, I32, VP, I64, VP, VP, I32, VP, VP]
         L.orc_paint_threads.restype = I32
+        L.orc_paint_ranks.argtypes = [VP, VP, I32, VP, I64, VP, I32, VP]
+        L.orc_paint_ranks.restype = I32
+        L.orc_reduce_ranks.argtypes = [VP, I32, I64, VP, I32]
+        L.orc_reduce_ranks.restype = None
+        L.orc_zero_ranks.argtypes = [VP, I32, I64]
+        L.orc_zero_ranks.restype = None
         L.orc_make_maptable.argtypes = [I32, F, F, I32, I32, I32, VP, I32]
         L.orc_make_maptable.restype = I64
         L.orc_halo_setup.argtypes = [VP, VP, VP, VP]
@@ -242,6 +248,33 @@ def paint_threads(p, tables, records, nthreads):
     if rc:
         raise RuntimeError("oracle paint failed (%d)" % rc)
     return hp, fs, {k: getattr(st, k) for k, _ in OrcStats._fields_}, tuple(t)
+
+
+class RankMaps:
+    """Private HEALPix float maps of nranks threads-as-ranks, allocated and written once
+    (the reference's per-rank `hpmapl = 0`), for painting repeated samples into them."""
+
+    def __init__(self, p, nranks):
+        self.n = p.nmaps * 12 * p.nside * p.nside
+        self.maps = [np.empty(self.n, dtype=np.float32) for _ in range(nranks)]
+        self.ptrs = (ctypes.c_void_p * nranks)(*[m.ctypes.data for m in self.maps])
+        # every rank writes its own map now (in parallel), not while painting
+        lib().orc_zero_ranks(self.ptrs, nranks, self.n)
+
+    def paint(self, p, tables, records):
+        rec = np.ascontiguousarray(records, dtype=np.float32)
+        tabs = (OrcTable * len(tables))(*[t.t for t in tables])
+        st = OrcStats()
+        rc = lib().orc_paint_ranks(ctypes.byref(p), tabs, len(tables), _p(rec), rec.shape[0],
+                                   self.ptrs, len(self.maps), ctypes.byref(st))
+        if rc:
+            raise RuntimeError("oracle paint failed (%d)" % rc)
+        return {k: getattr(st, k) for k, _ in OrcStats._fields_}
+
+    def reduce(self, nthreads):
+        out = np.empty(self.n, dtype=np.float32)
+        lib().orc_reduce_ranks(self.ptrs, len(self.maps), self.n, _p(out), nthreads)
+        return out
 
 
 def fmath(fn, x, y=None):

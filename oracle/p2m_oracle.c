@@ -665,6 +665,11 @@ int orc_paint_threads(const orc_params *p, const orc_table *tables, int ntables,
 #endif
     hpl[tid] = (float *)calloc((size_t)(hp_n > 0 ? hp_n : 1), sizeof(float));
     fsl[tid] = (float *)calloc((size_t)(fs_n > 0 ? fs_n : 1), sizeof(float));
+    /* `fsmapl = 0; hpmapl = 0` (pks2map.f90:278-279) writes every page of the rank's maps
+       before the halo loop: done here too, so that the set-up time carries the page
+       faults and the painting time is painting only */
+    if (hpl[tid]) memset(hpl[tid], 0, sizeof(float) * (size_t)(hp_n > 0 ? hp_n : 1));
+    if (fsl[tid]) memset(fsl[tid], 0, sizeof(float) * (size_t)(fs_n > 0 ? fs_n : 1));
   }
   double t1 = now_s();
   /* pksc.f90:51-52: nhalol = (N-1)/ntasks + 1 per rank */
@@ -729,6 +734,73 @@ int orc_paint_threads(const orc_params *p, const orc_table *tables, int ntables,
     t[2] = t3 - t2;
   }
   return rc;
+}
+
+/* The halo loop of every "rank" over records [0, nhalo), split as pksc.f90:51-52 splits
+   them, painting into caller-owned private HEALPix float maps (hp_maps[r]: nmaps * 12 *
+   nside^2 floats), without allocating, zeroing or reducing them: for timing the painting
+   alone over repeated samples.  HEALPix only (npix_fs must be 0). */
+int orc_paint_ranks(const orc_params *p, const orc_table *tables, int ntables,
+                    const float *records, int64_t nhalo, float **hp_maps, int nthreads,
+                    orc_stats *stats) {
+  int rc = check_params(p, ntables);
+  if (rc) return rc;
+  if (p->npix_fs > 0 || p->nside <= 0 || nthreads < 1) return -1;
+  orc_cosmo *c = (orc_cosmo *)malloc(sizeof(orc_cosmo));
+  orc_cosmo_init(c);
+  orc_stats *sts = (orc_stats *)calloc((size_t)nthreads, sizeof(orc_stats));
+  int *rcs = (int *)calloc((size_t)nthreads, sizeof(int));
+  int64_t per = (nhalo - 1) / nthreads + 1;
+#pragma omp parallel num_threads(nthreads)
+  {
+#ifdef _OPENMP
+    int tid = omp_get_thread_num();
+#else
+    int tid = 0;
+#endif
+    int64_t h0 = per * tid, h1 = h0 + per;
+    if (h1 > nhalo) h1 = nhalo;
+    if (h0 < h1) {
+      paint_out o;
+      memset(&o, 0, sizeof(o));
+      o.fp32 = 1;
+      o.hp32 = hp_maps[tid];
+      o.hp_npix = 12 * (int64_t)p->nside * p->nside;
+      rcs[tid] = paint_range(c, p, tables, records, h0, h1, &o, &sts[tid], NULL, NULL, 0, NULL);
+    }
+  }
+  orc_stats st;
+  memset(&st, 0, sizeof(st));
+  for (int r = 0; r < nthreads; r++) {
+    st.n_in += sts[r].n_in;
+    st.n_cut += sts[r].n_cut;
+    st.n_painted += sts[r].n_painted;
+    st.hp_updates += sts[r].hp_updates;
+    st.hp_candidates += sts[r].hp_candidates;
+    st.ring_gaps += sts[r].ring_gaps;
+    if (rcs[r]) rc = rcs[r];
+  }
+  free(sts);
+  free(rcs);
+  free(c);
+  if (stats) *stats = st;
+  return rc;
+}
+
+/* `hpmapl = 0` (pks2map.f90:279) of every rank, each rank writing its own map */
+void orc_zero_ranks(float **maps, int nranks, int64_t n) {
+#pragma omp parallel for num_threads(nranks) schedule(static, 1)
+  for (int r = 0; r < nranks; r++) memset(maps[r], 0, sizeof(float) * (size_t)n);
+}
+
+/* MPI_Allreduce(SUM) of the ranks' float maps in rank order (pks2map.f90:313-314) */
+void orc_reduce_ranks(float **maps, int nranks, int64_t n, float *out, int nthreads) {
+#pragma omp parallel for num_threads(nthreads) schedule(static)
+  for (int64_t k = 0; k < n; k++) {
+    float s = 0.0f;
+    for (int r = 0; r < nranks; r++) s = s + maps[r][k];
+    out[k] = s;
+  }
 }
 
 /* host evaluation of the shared float math (p2m_fmath.h) for tests:

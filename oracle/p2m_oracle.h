@@ -99,6 +99,11 @@ int orc_paint(const orc_params *p, const orc_table *tables, int ntables, const f
    map, summed at the end: the reference's MPI decomposition (pksc.f90:51-66,
    pks2map.f90:313-314) with threads as ranks.  Float output only.  Times (seconds)
    of the map set-up, paint and reduction phases are returned in t[3]. */
+int orc_paint_ranks(const orc_params *p, const orc_table *tables, int ntables,
+                    const float *records, int64_t nhalo, float **hp_maps, int nthreads,
+                    orc_stats *stats);
+void orc_reduce_ranks(float **maps, int nranks, int64_t n, float *out, int nthreads);
+void orc_zero_ranks(float **maps, int nranks, int64_t n);
 int orc_paint_threads(const orc_params *p, const orc_table *tables, int ntables,
                       const float *records, int64_t nhalo, float *hp_out, float *fs_out,
                       int nthreads, orc_stats *stats, double t[3]);
