@@ -52,6 +52,22 @@ int32_t p2m_get_timings(struct p2m_ctx *ctx, double *ms, int32_t n);
 int32_t p2m_map_sums_noalloc(const float *const *d_maps, int32_t nmaps, int64_t npix,
                              double *sums, void *stream);
 
+/* Output files of the pks2map command line (host code, no GPU).  Each returns 0 or a
+   status (P2M_ERR_BADARG, P2M_ERR_IO). */
+#define P2M_NDPDY 10000
+/* P(<y) of a HEALPix map, pks2map.f90:340-357: pixel counts in P2M_NDPDY bins of width
+   1e-4 / P2M_NDPDY (bin int(y / width) + 1, counted in float as the reference counts, so
+   a bin stops at 2^24), divided by npix and cumulated. */
+int32_t p2m_dpdy(const float *map, int64_t npix, float *dpdy);
+/* <out>_dp.bin: int32 P2M_NDPDY, float32 1e-4, float32 dpdy[P2M_NDPDY] (pks2map.f90:370-373) */
+int32_t p2m_write_dpdy(const char *path, const float *dpdy);
+/* <out>_fs.map: int32 npix, npix, float32 fov, fov (radians), float32 map[npix*npix]
+   (pks2map.f90:375-379) */
+int32_t p2m_write_flatsky(const char *path, const float *map, int32_t npix, float fov_rad);
+/* <out>_hp.fits: empty primary HDU + BINTABLE, one column of 1024-float rows in RING
+   order, NSIDE and ORDERING = 'RING' cards (pks2map.f90:381-385, HEALPix output_map) */
+int32_t p2m_write_healpix_fits(const char *path, const float *map, int32_t nside);
+
 /* Self-test of the single-precision math the kernels use (fn: 0 log, 1 exp, 2 pow,
    3 asin, 4 atan, 5 sin, 6 cos, 7 tan) evaluated on the GPU over n device floats;
    d_y is read only for pow.  Synchronous.  Returns 0 or a CUDA error code. */

@@ -26,7 +26,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",
               "-I" + CSRC, "-I" + INCLUDE]
 CU_SOURCES = ["p2m_kernels.cu", "p2m_capi.cu", "p2m_noalloc.cu"]
-CPP_SOURCES = ["p2m_tools.cpp"]
+CPP_SOURCES = ["p2m_tools.cpp", "p2m_outputs.cpp"]
 
 
 def _nvcc():
@@ -85,7 +85,7 @@ def build_lib(force=False, verbose=False):
 
 def build_cli(force=False):
     """The pks2map and make_maptable executables (link against the library)."""
-    deps = [os.path.join(CSRC, "pks2map_cli.cpp"), os.path.join(CSRC, "p2m_io.h"), LIB]
+    deps = [LIB] + _headers()
     for src, exe in (("pks2map_cli.cpp", CLI), ("make_maptable_cli.cpp", MAPTABLE_CLI)):
         path = os.path.join(CSRC, src)
         if not os.path.exists(path):

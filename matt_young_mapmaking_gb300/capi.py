@@ -108,6 +108,10 @@ def load_library():
         "p2m_fmath_eval_device": (I32, [I32, I32, VP, VP, VP, I64]),
         "p2m_get_timings": (I32, [VP, VP, I32]),
         "p2m_map_sums_noalloc": (I32, [VP, I32, I64, VP, VP]),
+        "p2m_dpdy": (I32, [VP, I64, VP]),
+        "p2m_write_dpdy": (I32, [ctypes.c_char_p, VP]),
+        "p2m_write_flatsky": (I32, [ctypes.c_char_p, VP, I32, F]),
+        "p2m_write_healpix_fits": (I32, [ctypes.c_char_p, VP, I32]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -125,7 +129,8 @@ def exported_symbols():
             "p2m_bind_healpix_device", "p2m_get_stats",
             "p2m_synchronize", "p2m_get_pixel_sets", "p2m_make_maptable",
             "p2m_generate_catalogue", "p2m_philox4x32", "p2m_fmath_eval_device",
-            "p2m_get_timings", "p2m_map_sums_noalloc"]
+            "p2m_get_timings", "p2m_map_sums_noalloc", "p2m_dpdy", "p2m_write_dpdy",
+            "p2m_write_flatsky", "p2m_write_healpix_fits"]
 
 
 PHASES = ["cut", "setup", "big_scan", "big_items", "flatsky", "big_offsets", "paint", "paint_big",
@@ -307,3 +312,35 @@ def generate_catalogue(seed, n, nfloat=10, r=(100.0, 3000.0), m=(1e12, 1e15), sl
     if st:
         raise P2MError(1, "generate_catalogue: bad arguments")
     return out
+
+
+NDPDY = 10000
+
+
+def _status(st, what):
+    if st:
+        raise P2MError(st, what)
+
+
+def dpdy(hp_map):
+    """P(<y) of a HEALPix map as pks2map computes it (pks2map.f90:340-357)."""
+    m = np.ascontiguousarray(hp_map, dtype=np.float32)
+    out = np.empty(NDPDY, dtype=np.float32)
+    _status(load_library().p2m_dpdy(_ptr(m), m.size, _ptr(out)), "p2m_dpdy")
+    return out
+
+
+def write_outputs(fileout, hp_map=None, nside=0, fs_map=None, npix_fs=0, fov_rad=0.0):
+    """The files pks2map writes: <fileout>_dp.bin and _hp.fits from the HEALPix map,
+    <fileout>_fs.map from the flat-sky map."""
+    lib = load_library()
+    if hp_map is not None:
+        m = np.ascontiguousarray(hp_map, dtype=np.float32)
+        d = dpdy(m)
+        _status(lib.p2m_write_dpdy((fileout + "_dp.bin").encode(), _ptr(d)), "_dp.bin")
+        _status(lib.p2m_write_healpix_fits((fileout + "_hp.fits").encode(), _ptr(m), nside),
+                "_hp.fits")
+    if fs_map is not None:
+        f = np.ascontiguousarray(fs_map, dtype=np.float32)
+        _status(lib.p2m_write_flatsky((fileout + "_fs.map").encode(), _ptr(f), npix_fs,
+                                      float(fov_rad)), "_fs.map")

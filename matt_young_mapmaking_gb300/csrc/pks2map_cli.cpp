@@ -1,0 +1,215 @@
+/*
+ * pks2map_cli.cpp -- the pks2map command line on one GB300 (pks2map.f90:58-385).
+ *
+ *   pks2map <filein> <fileout> <tablefile> [<zmin> <nside> <scramble> <center> <npix>
+ *           <fov> <zmax> <chihview> <model> <profile>]
+ *
+ * Same positional arguments and defaults as the reference (pks2map.f90:62-82; an
+ * argument that is a single dot, or does not parse, takes its default, textlib.f90:33-86),
+ * the same report lines, and the same output files: <fileout>_dp.bin, _fs.map, _hp.fits.
+ * The halo loop runs on the GPU through the C ABI (include/p2m.h).  The environment
+ * selects the precision (P2M_PRECISION = mixed | fp64 | mixed64, default mixed) and the
+ * device (P2M_DEVICE, default 0).  scramble and center are not implemented: non-zero
+ * values are rejected.
+ */
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/p2m.h"
+#include "../../include/p2m_tools.h"
+#include "p2m_fmath.h"
+#include "p2m_scalar.h"
+
+namespace {
+
+bool is_dot(const char *s) { return std::strcmp(s, ".") == 0; }
+
+/* textlib.f90 i4arg / r4arg: default when absent, a single dot, or unparsable */
+int i4arg(int argc, char **argv, int k, int def) {
+  if (k >= argc || is_dot(argv[k])) return def;
+  char *end = nullptr;
+  long v = std::strtol(argv[k], &end, 10);
+  if (end == argv[k] || *end) return def;
+  return (int)v;
+}
+float r4arg(int argc, char **argv, int k, float def) {
+  if (k >= argc || is_dot(argv[k])) return def;
+  char *end = nullptr;
+  double v = std::strtod(argv[k], &end);
+  if (end == argv[k] || *end) return def;
+  return (float)v;
+}
+
+bool read_file(const char *path, std::vector<char> &out) {
+  FILE *f = std::fopen(path, "rb");
+  if (!f) return false;
+  std::fseek(f, 0, SEEK_END);
+  long n = std::ftell(f);
+  std::fseek(f, 0, SEEK_SET);
+  out.resize((size_t)(n > 0 ? n : 0));
+  bool ok = n <= 0 || std::fread(out.data(), 1, (size_t)n, f) == (size_t)n;
+  std::fclose(f);
+  return ok;
+}
+
+int fail(const char *what, p2m_ctx *ctx = nullptr, int status = 0) {
+  std::fprintf(stderr, "pks2map: %s", what);
+  if (ctx) std::fprintf(stderr, ": %s", p2m_last_error(ctx));
+  if (status) std::fprintf(stderr, " (status %d)", status);
+  std::fprintf(stderr, "\n");
+  if (ctx) p2m_destroy(ctx);
+  return 1;
+}
+
+/* Fortran `1pe<w>.<d>` of a finite value: one digit before the point */
+std::string fe(double v, int d) {
+  char b[64];
+  std::snprintf(b, sizeof b, "%.*E", d, v);
+  return b;
+}
+
+}  // namespace
+
+int main(int argc, char **argv) {
+  if (argc - 1 < 3) {
+    std::printf("Usage: pks2map <filein> <fileout> <tablefile> [<zmin> <nside> <scramble> "
+                "<center> <npix> <fov> <zmax> <chihview> <model> <profile>]\n");
+    return 0;
+  }
+  const char *filein = argv[1], *fileout = argv[2], *tablefile = argv[3];
+  const float zmin = r4arg(argc, argv, 4, 0.0f);
+  const int nside = i4arg(argc, argv, 5, 4096);
+  const int scramble = i4arg(argc, argv, 6, 0);
+  const int centre = i4arg(argc, argv, 7, 0);
+  const int npix = i4arg(argc, argv, 8, 16);
+  const float fov_deg = r4arg(argc, argv, 9, 10.0f);
+  const float zmax = r4arg(argc, argv, 10, 1.25f);
+  const float chihview = r4arg(argc, argv, 11, 0.0f);
+  const int model = i4arg(argc, argv, 12, 1);
+  const int profile = i4arg(argc, argv, 13, 1);
+  if (scramble != 0 || centre != 0) return fail("scramble and center are not implemented");
+  if (profile != 1 && profile != 2) return fail("profile must be 1 or 2");
+
+  /* pks2map.f90:88-105 (fov to radians, dpix) and its report */
+  const float mypi = 4.0f * p2m_atanf(1.0f);
+  const float fov = ((fov_deg / 360.0f) * 2.0f) * mypi;
+  const float dpix = npix > 0 ? fov / (float)npix : 0.0f;
+  const long long hpnpix = 12LL * nside * nside;
+  std::printf("\n\nResolution:         %d x %d pixels (%s radians)\n", npix, npix,
+              fe(dpix, 2).c_str());
+  std::printf("Field of view:      %s degrees\n", fe(fov / 2.0f / mypi * 360.0f, 2).c_str());
+  std::printf("Healpix Nside:      %d\nNumber of pixels:   %lld\n", nside, hpnpix);
+  {
+    /* pks2map.f90:134-137: cut distances from the r(z) table, printed as f4.2 Gpc */
+    p2m_cosmo cosmo;
+    std::vector<float> rofz(P2M_NZTAB), zofr(P2M_NZTAB);
+    p2m_cosmo_build(&cosmo, rofz.data(), zofr.data());
+    auto f42 = [](float v) {
+      char b[16];
+      if (!(v > -0.995f && v < 9.995f)) return std::string("****");
+      std::snprintf(b, sizeof b, "%4.2f", v);
+      return std::string(b);
+    };
+    std::printf("cut_low, cut_high:  %s %s Gpc\n",
+                f42(p2m_lookup(rofz.data(), cosmo.drofz, zmin) / 1e3f).c_str(),
+                f42(p2m_lookup(rofz.data(), cosmo.drofz, zmax) / 1e3f).c_str());
+  }
+
+  std::vector<char> table, cat;
+  if (!read_file(tablefile, table)) return fail("cannot read the table file");
+  if (!read_file(filein, cat) || cat.size() < 8) return fail("cannot read the catalogue");
+  int32_t nhalo = 0;
+  std::memcpy(&nhalo, cat.data(), 4);
+  /* 7 floats after a 2-word header (pksc.f90:46-66) or 10 after a 3-word header */
+  int nfloat = 0, hdr = 0;
+  if (nhalo >= 0 && cat.size() == 8 + 28ull * (size_t)nhalo) nfloat = 7, hdr = 8;
+  else if (nhalo >= 0 && cat.size() == 12 + 40ull * (size_t)nhalo) nfloat = 10, hdr = 12;
+  if (!nfloat) return fail("catalogue size matches neither 8+28N nor 12+40N bytes");
+
+  p2m_config cfg;
+  std::memset(&cfg, 0, sizeof cfg);
+  cfg.nside = nside;
+  cfg.npix_fs = npix;
+  cfg.fov_deg = fov_deg;
+  cfg.zmin = zmin;
+  cfg.zmax = zmax;
+  cfg.chihview = chihview;
+  cfg.model = model;
+  cfg.precision = P2M_PREC_MIXED;
+  if (const char *e = std::getenv("P2M_PRECISION")) {
+    if (!std::strcmp(e, "fp64")) cfg.precision = P2M_PREC_FP64;
+    else if (!std::strcmp(e, "mixed64")) cfg.precision = P2M_PREC_MIXED_F64;
+  }
+  cfg.nmaps = 1;
+  cfg.map_table[0] = 0;
+  cfg.map_profile[0] = profile;
+  cfg.max_records = nhalo < (1 << 22) ? (nhalo > 0 ? nhalo : 1) : (1 << 22);
+  cfg.device = std::getenv("P2M_DEVICE") ? std::atoi(std::getenv("P2M_DEVICE")) : 0;
+  p2m_ctx *ctx = nullptr;
+  int st = p2m_create(&cfg, &ctx);
+  if (st) return fail("p2m_create", ctx, st);
+
+  st = p2m_load_table(ctx, 0, table.data(), (int64_t)table.size());
+  if (st) return fail("p2m_load_table", ctx, st);
+  st = p2m_paint_records(ctx, (const float *)(cat.data() + hdr), nhalo, nfloat);
+  if (st) return fail("p2m_paint_records", ctx, st);
+
+  std::vector<float> hp((size_t)(nside > 0 ? hpnpix : 0)), fs((size_t)npix * (size_t)npix);
+  if (nside > 0 && (st = p2m_get_healpix(ctx, 0, hp.data()))) return fail("p2m_get_healpix", ctx, st);
+  if (npix > 0 && (st = p2m_get_flatsky(ctx, 0, fs.data()))) return fail("p2m_get_flatsky", ctx, st);
+  p2m_stats stats;
+  if ((st = p2m_get_stats(ctx, &stats))) return fail("p2m_get_stats", ctx, st);
+  p2m_destroy(ctx);
+
+  /* pks2map.f90:318-338: halo count, moments, RMS and mean */
+  std::printf("Number of halos in map:    %lld\n", (long long)stats.n_painted);
+  double fm[3] = {0, 0, 0}, hm[3] = {0, 0, 0};
+  for (float v : fs) {
+    double x = v;
+    fm[0] += x;
+    fm[1] += x * x;
+    fm[2] += x * x * x;
+  }
+  for (float v : hp) {
+    double x = v;
+    hm[0] += x;
+    hm[1] += x * x;
+    hm[2] += x * x * x;
+  }
+  const double nfs = fs.empty() ? 1.0 : (double)fs.size(), nhp = hp.empty() ? 1.0 : (double)hp.size();
+  for (int k = 0; k < 3; k++) {
+    fm[k] /= nfs;
+    hm[k] /= nhp;
+  }
+  std::printf("Flatsky moments:    %s %s %s \n", fe(fm[0], 3).c_str(), fe(fm[1], 3).c_str(),
+              fe(fm[2], 3).c_str());
+  std::printf("Healpix moments:    %s %s %s \n", fe(hm[0], 3).c_str(), fe(hm[1], 3).c_str(),
+              fe(hm[2], 3).c_str());
+  double fv = 0, hv = 0;
+  for (float v : fs) fv += ((double)v - fm[0]) * ((double)v - fm[0]);
+  for (float v : hp) hv += ((double)v - hm[0]) * ((double)v - hm[0]);
+  std::printf("Flatsky RMS:                %s\nFlatsky Mean:               %s\n",
+              fe(std::sqrt(fv / nfs), 3).c_str(), fe(fm[0], 2).c_str());
+  std::printf("Healpix RMS:                %s\nHealpix Mean:               %s\n\n",
+              fe(std::sqrt(hv / nhp), 3).c_str(), fe(hm[0], 2).c_str());
+
+  /* pks2map.f90:340-385: P(<y), then the three files */
+  const std::string out = fileout;
+  if (nside > 0) {
+    std::vector<float> dpdy(P2M_NDPDY);
+    if ((st = p2m_dpdy(hp.data(), hpnpix, dpdy.data()))) return fail("p2m_dpdy", nullptr, st);
+    if ((st = p2m_write_dpdy((out + "_dp.bin").c_str(), dpdy.data())))
+      return fail("cannot write _dp.bin", nullptr, st);
+  }
+  if ((st = p2m_write_flatsky((out + "_fs.map").c_str(), fs.data(), npix, fov)))
+    return fail("cannot write _fs.map", nullptr, st);
+  if (nside > 0 && (st = p2m_write_healpix_fits((out + "_hp.fits").c_str(), hp.data(), nside)))
+    return fail("cannot write _hp.fits", nullptr, st);
+  std::printf("\n");
+  return 0;
+}

@@ -7,7 +7,9 @@ Patch catalogues carry a 3-word header (+ float32 zbox) and 10 float32 per halo
 
 Profile tables (maptable.f90:94,142,156-162): int32 nchit, nmht, nrt, float32 chimint,
 chimaxt, mhmint, mhmaxt, rmint, rmaxt, then float32 table(2, nrt, nmht, nchit) in
-Fortran order.  Output maps (pks2map.f90:366-381): _dp.bin, _fs.map, _hp.fits.
+Fortran order.  Output maps (pks2map.f90:366-385): _dp.bin (int32 ndpdy, float32 dpdy_max, float32
+P(<y)[ndpdy]), _fs.map (int32 npix, npix, float32 fov, fov, float32 map), _hp.fits (FITS
+BINTABLE, one column of 1024-float rows, RING order).
 """
 import os
 import struct
@@ -87,3 +89,54 @@ def read_table(path):
 def write_table(path, image):
     with open(path, "wb") as f:
         f.write(bytes(image))
+
+
+def read_dpdy(path):
+    """<out>_dp.bin -> (dpdy_max, P(<y) float32 array)."""
+    with open(path, "rb") as f:
+        raw = f.read()
+    n, mx = struct.unpack("<if", raw[:8])
+    return mx, np.frombuffer(raw, dtype="<f4", count=n, offset=8).copy()
+
+
+def read_flatsky(path):
+    """<out>_fs.map -> (fov in radians, (npix, npix) float32 map, index [k, j], j fastest)."""
+    with open(path, "rb") as f:
+        raw = f.read()
+    n1, n2, fov, _ = struct.unpack("<iiff", raw[:16])
+    return fov, np.frombuffer(raw, dtype="<f4", count=n1 * n2, offset=16).reshape(n2, n1).copy()
+
+
+def read_healpix_fits(path):
+    """<out>_hp.fits -> (header cards of the BINTABLE as a dict, RING-ordered float32 map).
+    Reads the layout the HEALPix writer produces: an empty primary HDU, then a BINTABLE
+    whose single column holds TFORM1 = '<repeat>E' floats per row (big endian)."""
+    with open(path, "rb") as f:
+        raw = f.read()
+
+    def header(at):
+        cards = {}
+        pos = at
+        while True:
+            block = raw[pos:pos + 2880]
+            if len(block) < 2880:
+                raise ValueError("truncated FITS header")
+            pos += 2880
+            for k in range(36):
+                c = block[80 * k:80 * k + 80].decode("ascii")
+                key = c[:8].strip()
+                if key == "END":
+                    return cards, pos
+                if c[8:10] == "= ":
+                    v = c[10:].split(" /")[0].strip()
+                    cards[key] = v.strip("'").strip() if v.startswith("'") else v
+
+    prim, pos = header(0)
+    if prim.get("SIMPLE") != "T":
+        raise ValueError("not a FITS file")
+    ext, pos = header(pos)
+    if ext.get("XTENSION") != "BINTABLE":
+        raise ValueError("second HDU is not a BINTABLE")
+    rows, width = int(ext["NAXIS2"]), int(ext["NAXIS1"])
+    data = np.frombuffer(raw, dtype=">f4", count=rows * width // 4, offset=pos)
+    return ext, data.astype(np.float32)
