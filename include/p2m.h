@@ -116,6 +116,14 @@ p2m_status p2m_reset_maps(p2m_ctx *ctx);
    held in host memory: radial cut, mass, per-halo set-up and both projections, exactly
    the halo loop of pks2map.f90:134-303.  Accumulates into the context's maps. */
 p2m_status p2m_paint_records(p2m_ctx *ctx, const float *records, int64_t nrec, int32_t nfloat);
+/* The pks2map command-line flags scramble and center (pks2map.f90:75-76, :162-262): 1
+   gives every halo that survives the radial cut a random direction from the reference's
+   ranf stream (seed 13579*(rank+1), two draws per halo in catalogue order), resp. flips
+   and rotates all positions so that the largest-RTH halo lies on the z axis.  ntasks
+   (1..25) is the MPI rank count whose halo blocks and streams are reproduced.  Call
+   right after p2m_create or p2m_reset_maps; the whole catalogue must then come in one
+   paint call. */
+p2m_status p2m_set_preprocess(p2m_ctx *ctx, int32_t scramble, int32_t centre, int32_t ntasks);
 /* Same with the records already in device memory (on ctx's device), ordered on the
    given cudaStream_t (NULL = the context's stream). */
 p2m_status p2m_paint_records_device(p2m_ctx *ctx, const float *d_records, int64_t nrec,

@@ -52,6 +52,10 @@ int32_t p2m_get_timings(struct p2m_ctx *ctx, double *ms, int32_t n);
 int32_t p2m_map_sums_noalloc(const float *const *d_maps, int32_t nmaps, int64_t npix,
                              double *sums, void *stream);
 
+/* With center: RTHmax, then the distance and x, y, z of the largest halo before and after
+   the rotation (the report of pks2map.f90:205-209, :250-254); zeros otherwise. */
+int32_t p2m_get_centre(struct p2m_ctx *ctx, float *out9);
+
 /* Output files of the pks2map command line (host code, no GPU).  Each returns 0 or a
    status (P2M_ERR_BADARG, P2M_ERR_IO). */
 #define P2M_NDPDY 10000

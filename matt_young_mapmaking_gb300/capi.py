@@ -108,6 +108,8 @@ def load_library():
         "p2m_fmath_eval_device": (I32, [I32, I32, VP, VP, VP, I64]),
         "p2m_get_timings": (I32, [VP, VP, I32]),
         "p2m_map_sums_noalloc": (I32, [VP, I32, I64, VP, VP]),
+        "p2m_set_preprocess": (I32, [VP, I32, I32, I32]),
+        "p2m_get_centre": (I32, [VP, VP]),
         "p2m_dpdy": (I32, [VP, I64, VP]),
         "p2m_write_dpdy": (I32, [ctypes.c_char_p, VP]),
         "p2m_write_flatsky": (I32, [ctypes.c_char_p, VP, I32, F]),
@@ -129,7 +131,8 @@ def exported_symbols():
             "p2m_bind_healpix_device", "p2m_get_stats",
             "p2m_synchronize", "p2m_get_pixel_sets", "p2m_make_maptable",
             "p2m_generate_catalogue", "p2m_philox4x32", "p2m_fmath_eval_device",
-            "p2m_get_timings", "p2m_map_sums_noalloc", "p2m_dpdy", "p2m_write_dpdy",
+            "p2m_get_timings", "p2m_map_sums_noalloc", "p2m_set_preprocess", "p2m_get_centre",
+            "p2m_dpdy", "p2m_write_dpdy",
             "p2m_write_flatsky", "p2m_write_healpix_fits"]
 
 
@@ -205,6 +208,16 @@ class Painter:
         return self._h
 
     # -- the reference's interface ---------------------------------------------------
+    def set_preprocess(self, scramble=0, centre=0, ntasks=1):
+        """pks2map's scramble / center flags (call right after creation or reset)."""
+        self._check(self._lib.p2m_set_preprocess(self._h, scramble, centre, ntasks))
+
+    def centre_info(self):
+        """RTHmax, then distance, x, y, z of the largest halo before and after the rotation."""
+        v = np.zeros(9, dtype=np.float32)
+        self._check(self._lib.p2m_get_centre(self._h, _ptr(v)))
+        return v
+
     def load_table(self, slot, image):
         """loadmaptable: `image` is the table file's bytes (header + table)."""
         buf = np.frombuffer(bytes(image) if not isinstance(image, np.ndarray) else image.tobytes(),

@@ -34,6 +34,12 @@ struct p2m_ctx {
   float *d_rofz = nullptr, *d_zofr = nullptr;
   float4 *d_ringtab = nullptr;
   float4 *d_phitab = nullptr;
+  /* scramble / centre of the catalogue (pks2map.f90:162-262) */
+  p2m_pre pre = {};
+  unsigned int *d_pre_flags = nullptr, *d_pre_bits = nullptr;
+  long long *d_pre_ord = nullptr, *d_pre_last = nullptr;
+  long long cap_pre_flags = 0, cap_pre_ord = 0, cap_pre_last = 0;
+  float centre_info[9] = {};
   p2m_tabhdr th;
   bool th_set = false;
   float *d_tab[P2M_MAXTABLES] = {};
@@ -197,6 +203,8 @@ PaintParams make_params(const p2m_ctx *ctx, int nfloat) {
   P.zofr = ctx->d_zofr;
   P.ringtab = ctx->d_ringtab;
   P.phitab = ctx->d_phitab;
+  P.pre = ctx->pre;
+  P.pre_ord = ctx->d_pre_ord;
   P.band_u = ctx->band_u;
   P.inv_drt = ctx->th_set ? 1.0f / ctx->th.drt : 0.0f;
   P.big_rings = ctx->big_rings;
@@ -349,6 +357,94 @@ p2m_status flush_prepared(p2m_ctx *ctx) {
   return P2M_OK;
 }
 
+/* scramble / centre (pks2map.f90:162-262) of the whole catalogue in d_rec: survivor
+   ordinals for the rank streams, and the flips and angles that put the largest-RTH
+   halo on the z axis (computed on the host with the kernels' own arithmetic) */
+p2m_status preprocess(p2m_ctx *ctx, const float *d_rec, long long nrec, int nfloat,
+                      cudaStream_t s) {
+  p2m_pre &q = ctx->pre;
+  const int ntasks = q.ntasks > 1 ? q.ntasks : 1;
+  q.per_rank = nrec > 0 ? (nrec - 1) / ntasks + 1 : 1;
+  q.flip[0] = q.flip[1] = q.flip[2] = 0;
+  q.ct = q.cp = 1.0f;
+  q.st = q.sp = 0.0f;
+  const int centre = q.centre;
+  q.centre = 0; /* the flags, ordinals and search see the positions before rotation */
+  PaintParams P = make_params(ctx, nfloat);
+  CK(grow(&ctx->d_pre_flags, &ctx->cap_pre_flags, nrec));
+  CK(grow(&ctx->d_pre_ord, &ctx->cap_pre_ord, nrec));
+  p2m_launch_pre_flags(P, d_rec, nrec, ctx->d_pre_flags, s, ctx->nsm);
+  unsigned long long nn = (unsigned long long)nrec;
+  CK(cudaMemcpyAsync(ctx->d_nitems, &nn, sizeof(nn), cudaMemcpyHostToDevice, s));
+  p2m_launch_scan_u32(ctx->d_pre_flags, ctx->d_nitems, ctx->d_pre_ord, nullptr, ctx->d_scan_tmp, s);
+  for (int k = 0; k < 9; k++) ctx->centre_info[k] = 0.0f;
+  if (centre) {
+    CK(grow(&ctx->d_pre_last, &ctx->cap_pre_last, ntasks));
+    CK(cudaMemsetAsync(ctx->d_pre_last, 0xff, sizeof(long long) * (size_t)ntasks, s));
+    CK(cudaMemsetAsync(ctx->d_pre_bits, 0, sizeof(unsigned int), s));
+    P.pre_ord = ctx->d_pre_ord;
+    p2m_launch_pre_centre(P, d_rec, nrec, ctx->d_pre_flags, ctx->d_pre_bits, ctx->d_pre_last, s,
+                          ctx->nsm);
+    CK(cudaGetLastError());
+    std::vector<long long> last((size_t)ntasks);
+    unsigned int bits = 0;
+    CK(cudaMemcpyAsync(last.data(), ctx->d_pre_last, sizeof(long long) * (size_t)ntasks,
+                       cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(&bits, ctx->d_pre_bits, sizeof(bits), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    float rthmax;
+    memcpy(&rthmax, &bits, 4);
+    /* per rank the last survivor holding RTHmax, then MAX over ranks per coordinate */
+    float xm = -1e5f, ym = -1e5f, zm = -1e5f;
+    for (int r = 0; r < ntasks; r++) {
+      if (last[(size_t)r] < 0) continue;
+      const long long i = last[(size_t)r];
+      float pos[3];
+      CK(cudaMemcpy(pos, d_rec + i * nfloat, sizeof(pos), cudaMemcpyDeviceToHost));
+      if (q.scramble) {
+        long long oi = 0, ob = 0;
+        CK(cudaMemcpy(&oi, ctx->d_pre_ord + i, sizeof(oi), cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(&ob, ctx->d_pre_ord + (long long)r * q.per_rank, sizeof(ob),
+                      cudaMemcpyDeviceToHost));
+        p2m_scramble_pos(13579LL * (r + 1), oi - ob, pos);
+      }
+      xm = std::max(xm, pos[2]);
+      ym = std::max(ym, pos[1]);
+      zm = std::max(zm, pos[0]);
+    }
+    float *info = ctx->centre_info;
+    info[0] = rthmax;
+    info[1] = FSQRT(FADD(FADD(FMUL(xm, xm), FMUL(ym, ym)), FMUL(zm, zm)));
+    info[2] = xm;
+    info[3] = ym;
+    info[4] = zm;
+    q.flip[2] = xm < 0.0f;
+    q.flip[1] = ym < 0.0f;
+    q.flip[0] = zm < 0.0f;
+    xm = std::fabs(xm);
+    ym = std::fabs(ym);
+    zm = std::fabs(zm);
+    const float theta = p2m_asinf(FDIV(zm, FSQRT(FADD(FMUL(xm, xm), FMUL(zm, zm)))));
+    const float xml = FMUL(FDIV(xm, std::fabs(xm)), FSQRT(FADD(FMUL(xm, xm), FMUL(zm, zm))));
+    const float phi = p2m_asinf(FDIV(ym, FSQRT(FADD(FMUL(ym, ym), FMUL(xml, xml)))));
+    q.ct = p2m_cosf(theta);
+    q.st = p2m_sinf(theta);
+    q.cp = p2m_cosf(phi);
+    q.sp = p2m_sinf(phi);
+    q.centre = 1;
+    /* the largest halo after the flips and rotation (pks2map.f90:245-257) */
+    float after[3] = {info[4], info[3], info[2]}; /* posxyz(1..3) before them */
+    p2m_rotate_pos(&q, after);
+    info[5] = FSQRT(FADD(FADD(FMUL(after[2], after[2]), FMUL(after[1], after[1])),
+                         FMUL(after[0], after[0])));
+    info[6] = after[2];
+    info[7] = after[1];
+    info[8] = after[0];
+  }
+  CK(cudaGetLastError());
+  return P2M_OK;
+}
+
 p2m_status ingest_device(p2m_ctx *ctx, const float *d_rec, long long nrec, int nfloat,
                          cudaStream_t s) {
   if (nfloat != 7 && nfloat != 10) return fail(ctx, P2M_ERR_BADARG, "nfloat must be 7 or 10");
@@ -358,7 +454,12 @@ p2m_status ingest_device(p2m_ctx *ctx, const float *d_rec, long long nrec, int n
   ST(flush_prepared(ctx));
   if (nrec == 0) return P2M_OK;
   join_in(ctx, s);
+  const bool pre = ctx->pre.scramble || ctx->pre.centre;
+  if (pre && ctx->rec_count > 0)
+    return fail(ctx, P2M_ERR_STATE,
+                "with scramble or centre the catalogue must be painted in one call after a reset");
   ST(begin_call(ctx, nrec, s));
+  if (pre) ST(preprocess(ctx, d_rec, nrec, nfloat, s));
   PaintParams P = make_params(ctx, nfloat);
   IngestBuffers B = ingest_buffers(ctx, d_rec);
   TB(PH_CUT);
@@ -565,6 +666,7 @@ p2m_status p2m_create(const p2m_config *cfg, p2m_ctx **out) {
   CK(cudaMalloc((void **)&ctx->d_ctr, sizeof(DevCounters)));
   CK(cudaMallocHost((void **)&ctx->h_ctr, sizeof(DevCounters)));
   CK(cudaMalloc((void **)&ctx->d_nitems, sizeof(unsigned long long)));
+  CK(cudaMalloc((void **)&ctx->d_pre_bits, sizeof(unsigned int)));
   CK(cudaMalloc((void **)&ctx->d_sums, sizeof(double) * 2 * P2M_MAXMAPS));
   if (cfg->flags & P2M_FLAG_RECORD_SETS) {
     ctx->cap_set = 1LL << 24;
@@ -589,7 +691,8 @@ void p2m_destroy(p2m_ctx *ctx) {
                   ctx->d_fs_out, ctx->d_halos, ctx->d_items_raw, ctx->d_records,
                   ctx->d_nring, ctx->d_ioff, ctx->d_fs_items, ctx->d_scan_tmp, ctx->d_counts,
                   ctx->d_pix_off, ctx->d_nitems, ctx->d_sums, ctx->d_set_rec, ctx->d_set_pix,
-                  ctx->d_ctr, ctx->d_prep, ctx->d_lo, ctx->d_tiles};
+                  ctx->d_ctr, ctx->d_prep, ctx->d_lo, ctx->d_tiles,
+                  ctx->d_pre_flags, ctx->d_pre_bits, ctx->d_pre_ord, ctx->d_pre_last};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   for (int m = 0; m < P2M_MAXMAPS; m++)
@@ -676,6 +779,19 @@ p2m_status p2m_reset_maps(p2m_ctx *ctx) {
     CK(cudaMemsetAsync(ctx->d_fs_acc, 0, 8 * (size_t)ctx->cfg.nmaps * (size_t)ctx->fs_npix, s));
   CK(cudaMemsetAsync(ctx->d_ctr, 0, sizeof(DevCounters), s));
   CK(cudaMemsetAsync(ctx->d_sums, 0, sizeof(double) * 2 * P2M_MAXMAPS, s));
+  return P2M_OK;
+}
+
+p2m_status p2m_set_preprocess(p2m_ctx *ctx, int32_t scramble, int32_t centre, int32_t ntasks) {
+  if (!ctx) return P2M_ERR_BADARG;
+  if ((scramble != 0 && scramble != 1) || (centre != 0 && centre != 1) || ntasks < 1 ||
+      ntasks > 25)
+    return fail(ctx, P2M_ERR_BADARG, "scramble and centre must be 0 or 1, ntasks 1..25");
+  if (ctx->dirty || ctx->rec_count > 0 || !ctx->prep.empty())
+    return fail(ctx, P2M_ERR_STATE, "set the pre-processing right after p2m_reset_maps");
+  ctx->pre.scramble = scramble;
+  ctx->pre.centre = centre;
+  ctx->pre.ntasks = ntasks;
   return P2M_OK;
 }
 
@@ -846,6 +962,12 @@ p2m_status p2m_get_pixel_sets(p2m_ctx *ctx, int64_t *rec, int64_t *pix, int64_t 
     CK(cudaMemcpy(rec, ctx->d_set_rec, sizeof(long long) * (size_t)k, cudaMemcpyDeviceToHost));
     CK(cudaMemcpy(pix, ctx->d_set_pix, sizeof(long long) * (size_t)k, cudaMemcpyDeviceToHost));
   }
+  return P2M_OK;
+}
+
+int32_t p2m_get_centre(p2m_ctx *ctx, float *out9) {
+  if (!ctx || !out9) return P2M_ERR_BADARG;
+  for (int k = 0; k < 9; k++) out9[k] = ctx->centre_info[k];
   return P2M_OK;
 }
 

@@ -106,6 +106,8 @@ struct PaintParams {
   const float *rofz, *zofr;
   const float4 *ringtab; /* (z hi, z lo, sin theta hi, sin theta lo) of ring i at index i */
   const float4 *phitab;  /* (cos hi, cos lo, sin hi, sin lo) of 2 pi k / P2M_PHITAB */
+  p2m_pre pre;           /* scramble / centre of the catalogue (pks2map.f90:162-262) */
+  const long long *pre_ord; /* with pre: radial-cut survivors before each record */
 };
 
 /* buffers of one ingest call */
@@ -146,6 +148,11 @@ struct SweepBuffers {
 /* launchers (p2m_kernels.cu) */
 void p2m_launch_cut_setup(const PaintParams &P, const IngestBuffers &B, long long n,
                           cudaStream_t s, int nsm);
+void p2m_launch_pre_flags(const PaintParams &P, const float *records, long long n,
+                          unsigned int *flags, cudaStream_t s, int nsm);
+void p2m_launch_pre_centre(const PaintParams &P, const float *records, long long n,
+                           const unsigned int *flags, unsigned int *rthmax_bits,
+                           long long *last, cudaStream_t s, int nsm);
 void p2m_launch_setup_prepared(const PaintParams &P, const IngestBuffers &B, const float *prep,
                                long long n, cudaStream_t s, int nsm);
 void p2m_launch_scan_u32(const unsigned int *in, const unsigned long long *n_ptr, long long *out,

@@ -68,8 +68,35 @@ __device__ __forceinline__ p2m_hinterp halo_hinterp(const HaloRec &H) {
 /* radial cut (pks2map.f90:144-160), mass cut (:264, :296), and the table's chi bound
    (maptable.f90:184,188: chi = rofz(zofr(chi)) > chimaxt paints zeros) of one record;
    true if the record is enumerated */
-__device__ __forceinline__ bool cut_record(const PaintParams &P, const float *r, bool &shell,
-                                           bool &massive) {
+/* radial cut of pks2map.f90:144-160 on a record as read */
+__device__ __forceinline__ bool in_shell(const PaintParams &P, const float *r) {
+  float p0 = __ldg(r + 0), p1 = __ldg(r + 1), p2 = __ldg(r + 2), rth = __ldg(r + 6);
+  if (!(p2m_isfinite(p0) && p2m_isfinite(p1) && p2m_isfinite(p2) && p2m_isfinite(rth)))
+    return false;
+  float xh = FSUB(p2, P.chihview), yh = p1, zh = p0;
+  float chih = FSQRT(FADD(FADD(FMUL(xh, xh), FMUL(yh, yh)), FMUL(zh, zh)));
+  return !(chih > P.cut_high || chih < P.cut_low);
+}
+
+/* posxyz(1..3) of record i as the halo loop sees it: as read, or scrambled in its
+   rank's stream and / or rotated (pks2map.f90:162-262) */
+__device__ __forceinline__ void halo_position(const PaintParams &P, const float *records, long long i,
+                                              float pos[3]) {
+  const float *r = records + i * P.nfloat;
+  pos[0] = r[0];
+  pos[1] = r[1];
+  pos[2] = r[2];
+  if (P.pre.scramble) {
+    const long long rank = i / P.pre.per_rank;
+    const long long k = P.pre_ord[i] - P.pre_ord[rank * P.pre.per_rank];
+    p2m_scramble_pos(13579LL * (rank + 1), k, pos);
+  }
+  if (P.pre.centre) p2m_rotate_pos(&P.pre, pos);
+}
+
+__device__ __forceinline__ bool cut_record(const PaintParams &P, const float *records, long long i,
+                                           bool &shell, bool &massive) {
+  const float *r = records + i * P.nfloat;
   shell = massive = false;
   float p0 = __ldg(r + 0), p1 = __ldg(r + 1), p2 = __ldg(r + 2), rth = __ldg(r + 6);
   if (!(p2m_isfinite(p0) && p2m_isfinite(p1) && p2m_isfinite(p2) && p2m_isfinite(rth)))
@@ -77,6 +104,20 @@ __device__ __forceinline__ bool cut_record(const PaintParams &P, const float *r,
   float xh = FSUB(p2, P.chihview), yh = p1, zh = p0;
   float chih = FSQRT(FADD(FADD(FMUL(xh, xh), FMUL(yh, yh)), FMUL(zh, zh)));
   shell = !(chih > P.cut_high || chih < P.cut_low);
+  if (shell && (P.pre.scramble || P.pre.centre)) {
+    /* the halo loop sees the scrambled / rotated position */
+    float pos[3];
+    halo_position(P, records, i, pos);
+    p0 = pos[0];
+    p1 = pos[1];
+    p2 = pos[2];
+    if (!(p2m_isfinite(p0) && p2m_isfinite(p1) && p2m_isfinite(p2))) {
+      /* each rank's first scrambled halo: the seed's unreduced digits give a first draw
+         above 1 and a NaN position; it counts in the mass cut and paints nothing */
+      massive = !(FMUL(P.mass_fac, FMUL(FMUL(rth, rth), rth)) < 1e13f);
+      return false;
+    }
+  }
   float mass = FMUL(P.mass_fac, FMUL(FMUL(rth, rth), rth));
   massive = shell && !(mass < 1e13f);
   bool keep = massive;
@@ -275,7 +316,9 @@ __device__ __forceinline__ void setup_record(const PaintParams &P, const IngestB
                                              long long s, int i, unsigned long long &fsrows) {
   {
     const float *r = B.records + (long long)i * P.nfloat;
-    float p0 = r[0], p1 = r[1], p2 = r[2], rth = r[6];
+    float pos[3];
+    halo_position(P, B.records, i, pos);
+    float p0 = pos[0], p1 = pos[1], p2 = pos[2], rth = r[6];
     float mass = FMUL(P.mass_fac, FMUL(FMUL(rth, rth), rth));
     float xh = p2, yh = p1, zh = p0;
     float chih = FSQRT(FADD(FADD(FMUL(xh, xh), FMUL(yh, yh)), FMUL(zh, zh)));
@@ -291,7 +334,10 @@ __device__ __forceinline__ void setup_record(const PaintParams &P, const IngestB
     H.w1 = 1.0f;
     H.w2 = 1.0f;
     if (P.any_ksz) {
-      /* intended per-halo -v_los/c of pksc.f90:70-74 */
+      /* intended per-halo -v_los/c of pksc.f90:70-74, from the record as read */
+      p0 = r[0];
+      p1 = r[1];
+      p2 = r[2];
       float v0 = r[3], v1 = r[4], v2 = r[5];
       float dot = FADD(FADD(FMUL(p0, v0), FMUL(p1, v1)), FMUL(p2, v2));
       float nrm = FSQRT(FADD(FADD(FMUL(p0, p0), FMUL(p1, p1)), FMUL(p2, p2)));
@@ -325,7 +371,7 @@ __global__ void __launch_bounds__(256) k_cut_setup(PaintParams P, IngestBuffers 
       long long i = t0 + (long long)k * blockDim.x + threadIdx.x;
       if (i >= n) continue;
       bool shell, massive;
-      if (cut_record(P, B.records + i * P.nfloat, shell, massive)) keepbits |= 1u << k;
+      if (cut_record(P, B.records, i, shell, massive)) keepbits |= 1u << k;
       nshell += shell;
       nmass += massive;
     }
@@ -439,7 +485,7 @@ __global__ void __launch_bounds__(1024) k_scan_top(long long *bsum, unsigned lon
     __syncthreads();
   }
   bsum[t] = t > 0 ? sh[t - 1] : 0;
-  if (t == SCAN_BLOCKS - 1) *total = (unsigned long long)sh[t];
+  if (total && t == SCAN_BLOCKS - 1) *total = (unsigned long long)sh[t];
 }
 
 __global__ void __launch_bounds__(256) k_scan_apply(const unsigned int *in,
@@ -1598,6 +1644,47 @@ static inline int grid_for(long long n, int block, int nsm, int per_sm) {
   if (g > cap) g = cap;
   if (g < 1) g = 1;
   return (int)g;
+}
+
+/* radial-cut flags of the records (input of the survivor-ordinal scan) */
+__global__ void __launch_bounds__(256) k_pre_flags(PaintParams P, const float *records, long long n,
+                                                   unsigned int *flags) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    flags[i] = in_shell(P, records + i * P.nfloat) ? 1u : 0u;
+}
+
+/* centre (pks2map.f90:191-210): the largest RTH among the survivors, then per rank the
+   last survivor holding it */
+__global__ void __launch_bounds__(256) k_pre_rthmax(PaintParams P, const float *records, long long n,
+                                                    const unsigned int *flags, unsigned int *bits) {
+  unsigned int mx = 0u;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const float rth = records[i * P.nfloat + 6];
+    if (flags[i] && rth > 0.0f) mx = max(mx, __float_as_uint(rth));
+  }
+  for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(FULL, mx, o));
+  if ((threadIdx.x & 31) == 0 && mx) atomicMax(bits, mx);
+}
+__global__ void __launch_bounds__(256) k_pre_last(PaintParams P, const float *records, long long n,
+                                                  const unsigned int *flags,
+                                                  const unsigned int *bits, long long *last) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    if (flags[i] && __float_as_uint(records[i * P.nfloat + 6]) == *bits)
+      atomicMax(&last[i / P.pre.per_rank], i); /* signed: the slots start at -1 */
+}
+
+void p2m_launch_pre_flags(const PaintParams &P, const float *records, long long n,
+                          unsigned int *flags, cudaStream_t s, int nsm) {
+  k_pre_flags<<<grid_for(n, 256, nsm, 8), 256, 0, s>>>(P, records, n, flags);
+}
+void p2m_launch_pre_centre(const PaintParams &P, const float *records, long long n,
+                           const unsigned int *flags, unsigned int *rthmax_bits,
+                           long long *last, cudaStream_t s, int nsm) {
+  k_pre_rthmax<<<grid_for(n, 256, nsm, 8), 256, 0, s>>>(P, records, n, flags, rthmax_bits);
+  k_pre_last<<<grid_for(n, 256, nsm, 8), 256, 0, s>>>(P, records, n, flags, rthmax_bits, last);
 }
 
 void p2m_launch_cut_setup(const PaintParams &P, const IngestBuffers &B, long long n,

@@ -287,4 +287,78 @@ P2M_HD float p2m_ring_coord(int nside, float theta) {
   return fn * (2.0f - 1.5f * z);
 }
 
+/* ------------------------------------------------- scramble and centre -------------- */
+
+/* Pre-processing of pks2map.f90:162-262 (off unless set): scramble gives every halo that
+   survives the radial cut a random direction; centre flips and rotates all positions so
+   that the largest-RTH halo lands on the z axis.  Positions are posxyz(1..3), the first
+   three floats of a record. */
+typedef struct p2m_pre {
+  int32_t scramble, centre;
+  int32_t ntasks;        /* MPI ranks emulated: each scrambles its block (pksc.f90:51-52) */
+  int32_t flip[3];       /* negate posxyz(1), posxyz(2), posxyz(3) */
+  long long per_rank;    /* records per rank block */
+  float ct, st, cp, sp;  /* cos, sin of rmaxtheta and rmaxphi */
+} p2m_pre;
+
+#define P2M_RANF_MASK ((1ULL << 48) - 1ULL)
+/* random.f90:28-29 multiplier (373, 3707, 1442, 647) as one 48-bit number */
+#define P2M_RANF_MULT (373ULL + (3707ULL << 12) + (1442ULL << 24) + (647ULL << 36))
+
+/* low 48 bits of a * b: exact under 64-bit wrap-around */
+P2M_HD unsigned long long p2m_ranf_mul(unsigned long long a, unsigned long long b) {
+  return (a * b) & P2M_RANF_MASK;
+}
+
+/* Output n of the ranf stream whose seed has every digit d (pks2map.f90:164 broadcasts
+   13579*(rank+1) to the four digits).  ranf (random.f90:40-57) returns the value of the
+   current seed, then multiplies it by the multiplier modulo 2^48 (random.f90:264-286).
+   Output 0 reads the unreduced digits; output n >= 1 is state_n / 2^48 with
+   state_n = mult^n * seed (mod 2^48), found by jump-ahead. */
+P2M_HD double p2m_ranf_nth(long long d, long long n) {
+  if (n == 0) {
+    const double fd = (double)(float)d;
+    return DADD(DADD(DADD(DDIV(fd, 4096.0), DDIV(fd, 16777216.0)), DDIV(fd, 68719476736.0)),
+                DDIV(fd, 281474976710656.0));
+  }
+  const unsigned long long ud = (unsigned long long)d;
+  unsigned long long s = (ud + (ud << 12) + (ud << 24) + (ud << 36)) & P2M_RANF_MASK;
+  unsigned long long a = P2M_RANF_MULT, e = (unsigned long long)n;
+  while (e) { /* s = mult^n * s */
+    if (e & 1ULL) s = p2m_ranf_mul(s, a);
+    a = p2m_ranf_mul(a, a);
+    e >>= 1;
+  }
+  const double s4 = (double)(s >> 36), s3 = (double)((s >> 24) & 4095ULL),
+               s2 = (double)((s >> 12) & 4095ULL), s1 = (double)(s & 4095ULL);
+  return DADD(DADD(DADD(DDIV(s4, 4096.0), DDIV(s3, 16777216.0)), DDIV(s2, 68719476736.0)),
+              DDIV(s1, 281474976710656.0));
+}
+
+/* pks2map.f90:166-184 for the k-th surviving halo of its rank (k from 0), seed digits d */
+P2M_HD void p2m_scramble_pos(long long d, long long k, float pos[3]) {
+  const float xh = pos[0], yh = pos[1], zh = pos[2];
+  const float chih = FSQRT(FADD(FADD(FMUL(xh, xh), FMUL(yh, yh)), FMUL(zh, zh)));
+  const float muran = (float)DSUB(DMUL(2.0, p2m_ranf_nth(d, 2 * k)), 1.0);
+  const float phiran = (float)DMUL((double)FMUL(2.0f, 3.14159f), p2m_ranf_nth(d, 2 * k + 1));
+  const float rh = FMUL(FSQRT(FSUB(1.0f, FMUL(muran, muran))), chih);
+  pos[0] = FMUL(rh, p2m_cosf(phiran));
+  pos[1] = FMUL(rh, p2m_sinf(phiran));
+  pos[2] = FMUL(muran, chih);
+}
+
+/* pks2map.f90:216-241: the flips, then the rotations by rmaxtheta and rmaxphi */
+P2M_HD void p2m_rotate_pos(const p2m_pre *q, float pos[3]) {
+  const float p1 = q->flip[0] ? -pos[0] : pos[0];
+  const float p2 = q->flip[1] ? -pos[1] : pos[1];
+  const float p3 = q->flip[2] ? -pos[2] : pos[2];
+  float xh = FADD(FMUL(p3, q->ct), FMUL(p1, q->st));
+  const float zh = FADD(FMUL(-p3, q->st), FMUL(p1, q->ct));
+  const float yh = FADD(FMUL(-xh, q->sp), FMUL(p2, q->cp));
+  xh = FADD(FMUL(xh, q->cp), FMUL(p2, q->sp));
+  pos[2] = zh;
+  pos[1] = yh;
+  pos[0] = xh;
+}
+
 #endif /* P2M_SCALAR_H */

@@ -9,8 +9,9 @@
  * the same report lines, and the same output files: <fileout>_dp.bin, _fs.map, _hp.fits.
  * The halo loop runs on the GPU through the C ABI (include/p2m.h).  The environment
  * selects the precision (P2M_PRECISION = mixed | fp64 | mixed64, default mixed) and the
- * device (P2M_DEVICE, default 0).  scramble and center are not implemented: non-zero
- * values are rejected.
+ * device (P2M_DEVICE, default 0).  scramble and center follow the reference's random
+ * stream and rotation; P2M_RANKS (default 1, at most 25) is the MPI rank count whose
+ * halo blocks and streams they reproduce (`mpirun -np <ranks> pks2map ...`).
  */
 #include <cmath>
 #include <cstdint>
@@ -73,6 +74,25 @@ std::string fe(double v, int d) {
   return b;
 }
 
+/* Fortran `e10.3`: 0.ddd mantissa, right-justified in 10 columns */
+std::string e103(double v) {
+  char b[64];
+  if (v == 0.0) {
+    std::snprintf(b, sizeof b, "%10s", "0.000E+00");
+    return b;
+  }
+  int ex = (int)std::floor(std::log10(std::fabs(v))) + 1;
+  double m = std::fabs(v) / std::pow(10.0, ex);
+  if (m >= 0.9995) { /* rounding to three digits carries into the exponent */
+    m /= 10.0;
+    ex += 1;
+  }
+  char body[32];
+  std::snprintf(body, sizeof body, "%s0.%03dE%+03d", v < 0 ? "-" : "", (int)std::lround(m * 1000.0), ex);
+  std::snprintf(b, sizeof b, "%10s", body);
+  return b;
+}
+
 }  // namespace
 
 int main(int argc, char **argv) {
@@ -92,8 +112,10 @@ int main(int argc, char **argv) {
   const float chihview = r4arg(argc, argv, 11, 0.0f);
   const int model = i4arg(argc, argv, 12, 1);
   const int profile = i4arg(argc, argv, 13, 1);
-  if (scramble != 0 || centre != 0) return fail("scramble and center are not implemented");
+  if ((scramble != 0 && scramble != 1) || (centre != 0 && centre != 1))
+    return fail("scramble and center must be 0 or 1");
   if (profile != 1 && profile != 2) return fail("profile must be 1 or 2");
+  const int ranks = std::getenv("P2M_RANKS") ? std::atoi(std::getenv("P2M_RANKS")) : 1;
 
   /* pks2map.f90:88-105 (fov to radians, dpix) and its report */
   const float mypi = 4.0f * p2m_atanf(1.0f);
@@ -149,6 +171,7 @@ int main(int argc, char **argv) {
   cfg.map_table[0] = 0;
   cfg.map_profile[0] = profile;
   cfg.max_records = nhalo < (1 << 22) ? (nhalo > 0 ? nhalo : 1) : (1 << 22);
+  if (scramble || centre) cfg.max_records = nhalo > 0 ? nhalo : 1; /* one pass: one catalogue */
   cfg.device = std::getenv("P2M_DEVICE") ? std::atoi(std::getenv("P2M_DEVICE")) : 0;
   p2m_ctx *ctx = nullptr;
   int st = p2m_create(&cfg, &ctx);
@@ -156,8 +179,20 @@ int main(int argc, char **argv) {
 
   st = p2m_load_table(ctx, 0, table.data(), (int64_t)table.size());
   if (st) return fail("p2m_load_table", ctx, st);
+  if ((st = p2m_set_preprocess(ctx, scramble, centre, ranks))) return fail("p2m_set_preprocess", ctx, st);
   st = p2m_paint_records(ctx, (const float *)(cat.data() + hdr), nhalo, nfloat);
   if (st) return fail("p2m_paint_records", ctx, st);
+  if (centre) {
+    /* pks2map.f90:205-209 and :250-254 */
+    float c[9];
+    p2m_get_centre(ctx, c);
+    std::printf("\nBefore rotation largest halo is at\nRTH, distance:    %s %s \nx, y, z:          %s %s %s \n\n",
+                fe(c[0], 3).c_str(), fe(c[1], 3).c_str(), e103(c[2]).c_str(), e103(c[3]).c_str(),
+                e103(c[4]).c_str());
+    std::printf("\nAfter rotation largest halo is at\nRTH, distance:    %s %s \nx, y, z:          %s %s %s \n\n",
+                fe(c[0], 3).c_str(), fe(c[5], 3).c_str(), e103(c[6]).c_str(), e103(c[7]).c_str(),
+                e103(c[8]).c_str());
+  }
 
   std::vector<float> hp((size_t)(nside > 0 ? hpnpix : 0)), fs((size_t)npix * (size_t)npix);
   if (nside > 0 && (st = p2m_get_healpix(ctx, 0, hp.data()))) return fail("p2m_get_healpix", ctx, st);

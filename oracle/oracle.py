@@ -29,14 +29,16 @@ class OrcParams(ctypes.Structure):
                 ("zmax", ctypes.c_float), ("chihview", ctypes.c_float),
                 ("model", ctypes.c_int32), ("nmaps", ctypes.c_int32),
                 ("profile", ctypes.c_int32 * MAXMAPS), ("table_id", ctypes.c_int32 * MAXMAPS),
-                ("fp32_accumulate", ctypes.c_int32), ("nfloat", ctypes.c_int32)]
+                ("fp32_accumulate", ctypes.c_int32), ("nfloat", ctypes.c_int32),
+                ("scramble", ctypes.c_int32), ("centre", ctypes.c_int32),
+                ("ntasks", ctypes.c_int32)]
 
 
 class OrcStats(ctypes.Structure):
     _fields_ = [("n_in", ctypes.c_int64), ("n_cut", ctypes.c_int64),
                 ("n_painted", ctypes.c_int64), ("hp_updates", ctypes.c_int64),
                 ("fs_updates", ctypes.c_int64), ("hp_candidates", ctypes.c_int64),
-                ("ring_gaps", ctypes.c_int64)]
+                ("ring_gaps", ctypes.c_int64), ("centre", ctypes.c_float * 9)]
 
 
 class OrcCosmo(ctypes.Structure):
@@ -104,6 +106,11 @@ def lib():
         L.orc_halo_setup.restype = I32
         _lib = L
     return _lib
+
+
+def _stats_dict(st):
+    return {k: (list(getattr(st, k)) if k == "centre" else getattr(st, k))
+            for k, _ in OrcStats._fields_}
 
 
 def _p(a):
@@ -191,7 +198,7 @@ def query_disc(nside, vec, radius):
 
 
 def params(nside=512, npix_fs=0, fov_deg=10.0, zmin=0.0, zmax=1.25, chihview=0.0, model=1,
-           maps=((0, 1),), fp32=False, nfloat=10):
+           maps=((0, 1),), fp32=False, nfloat=10, scramble=0, centre=0, ntasks=1):
     p = OrcParams()
     p.nside, p.npix_fs, p.fov_deg = nside, npix_fs, fov_deg
     p.zmin, p.zmax, p.chihview, p.model = zmin, zmax, chihview, model
@@ -200,6 +207,7 @@ def params(nside=512, npix_fs=0, fov_deg=10.0, zmin=0.0, zmax=1.25, chihview=0.0
         p.table_id[i], p.profile[i] = t, pr
     p.fp32_accumulate = 1 if fp32 else 0
     p.nfloat = nfloat
+    p.scramble, p.centre, p.ntasks = scramble, centre, ntasks
     return p
 
 
@@ -225,7 +233,7 @@ def paint(p, tables, records, record_sets=False, set_cap=1 << 24):
                          ctypes.byref(nset))
     if rc:
         raise RuntimeError("oracle paint failed (%d)" % rc)
-    stats = {k: getattr(st, k) for k, _ in OrcStats._fields_}
+    stats = _stats_dict(st)
     sets = None
     if record_sets:
         k = min(nset.value, set_cap)
@@ -247,7 +255,7 @@ def paint_threads(p, tables, records, nthreads):
                                  _p(t))
     if rc:
         raise RuntimeError("oracle paint failed (%d)" % rc)
-    return hp, fs, {k: getattr(st, k) for k, _ in OrcStats._fields_}, tuple(t)
+    return hp, fs, _stats_dict(st), tuple(t)
 
 
 class RankMaps:
@@ -269,7 +277,7 @@ class RankMaps:
                                    self.ptrs, len(self.maps), ctypes.byref(st))
         if rc:
             raise RuntimeError("oracle paint failed (%d)" % rc)
-        return {k: getattr(st, k) for k, _ in OrcStats._fields_}
+        return _stats_dict(st)
 
     def reduce(self, nthreads):
         out = np.empty(self.n, dtype=np.float32)

@@ -568,11 +568,130 @@ static int check_params(const orc_params *p, int ntables) {
   return 0;
 }
 
-/* halo loop over records [h0, h1): pks2map.f90:134-303 */
+/* ------------------------------------------------------- scramble and centre -------- */
+
+/* random.f90:264-286: c = a * b on four 12-bit digits, carries propagated, truncated to
+   four digits (the digits of b may exceed 4095: pks2map seeds every digit with
+   13579 * (rank + 1)) */
+static void ranf_modmult(const int64_t a[4], const int64_t b[4], int64_t c[4]) {
+  int64_t j1 = a[0] * b[0];
+  int64_t j2 = a[0] * b[1] + a[1] * b[0];
+  int64_t j3 = a[0] * b[2] + a[1] * b[1] + a[2] * b[0];
+  int64_t j4 = a[0] * b[3] + a[1] * b[2] + a[2] * b[1] + a[3] * b[0];
+  int64_t k1 = j1, k2 = j2 + k1 / 4096, k3 = j3 + k2 / 4096, k4 = j4 + k3 / 4096;
+  c[0] = k1 % 4096;
+  c[1] = k2 % 4096;
+  c[2] = k3 % 4096;
+  c[3] = k4 % 4096;
+}
+
+/* random.f90:40-57: the output from the current seed, then seed = multiplier * seed */
+static double ranf(int64_t seed[4]) {
+  static const int64_t mult[4] = {373, 3707, 1442, 647};
+  double r = (((double)(float)seed[3] / 4096.0 + (double)(float)seed[2] / 16777216.0) +
+              (double)(float)seed[1] / 68719476736.0) +
+             (double)(float)seed[0] / 281474976710656.0;
+  int64_t out[4];
+  ranf_modmult(mult, seed, out);
+  memcpy(seed, out, sizeof(out));
+  return r;
+}
+
+/* pks2map.f90:144-262 before the halo loop: the radial cut (surv), then with scramble a
+   random direction per surviving halo from its rank's ranf stream (seed 13579*(rank+1)
+   in every digit, two draws per halo in rank order; :162-187), then with centre the
+   flips and two rotations that put the largest-RTH halo on the z axis (:189-262).
+   trec: the records with the new positions (fields 0..2 = posxyz(1..3)). */
+static void preprocess(const orc_params *p, const float *recs, int64_t n, float cut_low,
+                       float cut_high, float *trec, unsigned char *surv, float info[9]) {
+  const int nf = p->nfloat;
+  const int ntasks = p->ntasks > 1 ? p->ntasks : 1;
+  const int64_t per = n > 0 ? (n - 1) / ntasks + 1 : 1;
+  memcpy(trec, recs, sizeof(float) * (size_t)(n * nf));
+  for (int64_t i = 0; i < n; i++)
+    surv[i] = (unsigned char)halo_in_shell(recs + i * nf, p->chihview, cut_low, cut_high);
+  if (p->scramble) {
+    for (int r = 0; r < ntasks; r++) {
+      int64_t seed[4];
+      for (int k = 0; k < 4; k++) seed[k] = 13579LL * (r + 1);
+      for (int64_t i = r * per; i < n && i < (r + 1) * per; i++) {
+        if (!surv[i]) continue;
+        float *q = trec + i * nf;
+        float xh = q[0], yh = q[1], zh = q[2];
+        float chih = sqrtf(((xh * xh) + (yh * yh)) + (zh * zh));
+        double rnd = ranf(seed);
+        float muran = (float)(2.0 * rnd - 1.0);
+        rnd = ranf(seed);
+        float phiran = (float)((double)(2.0f * 3.14159f) * rnd);
+        float rh = sqrtf(1.0f - muran * muran) * chih;
+        q[0] = rh * p2m_cosf(phiran);
+        q[1] = rh * p2m_sinf(phiran);
+        q[2] = muran * chih;
+      }
+    }
+  }
+  for (int k = 0; k < 9; k++) info[k] = 0.0f;
+  if (!p->centre) return;
+  float rthmax = -1.0f;
+  for (int64_t i = 0; i < n; i++)
+    if (surv[i] && recs[i * nf + 6] > rthmax) rthmax = recs[i * nf + 6];
+  /* per rank: the last survivor with rth == RTHmax; then MAX over ranks per coordinate */
+  float xm = -1e5f, ym = -1e5f, zm = -1e5f;
+  for (int r = 0; r < ntasks; r++) {
+    float xl = -1e5f, yl = -1e5f, zl = -1e5f;
+    for (int64_t i = r * per; i < n && i < (r + 1) * per; i++) {
+      if (!surv[i] || recs[i * nf + 6] != rthmax) continue;
+      xl = trec[i * nf + 2];
+      yl = trec[i * nf + 1];
+      zl = trec[i * nf + 0];
+    }
+    if (xl > xm) xm = xl;
+    if (yl > ym) ym = yl;
+    if (zl > zm) zm = zl;
+  }
+  info[0] = rthmax;
+  info[1] = sqrtf(((xm * xm) + (ym * ym)) + (zm * zm));
+  info[2] = xm;
+  info[3] = ym;
+  info[4] = zm;
+  const int f3 = xm < 0.0f, f2 = ym < 0.0f, f1 = zm < 0.0f;
+  xm = fabsf(xm);
+  ym = fabsf(ym);
+  zm = fabsf(zm);
+  float theta = p2m_asinf(zm / sqrtf((xm * xm) + (zm * zm)));
+  float xml = (xm / fabsf(xm)) * sqrtf((xm * xm) + (zm * zm));
+  float phi = p2m_asinf(ym / sqrtf((ym * ym) + (xml * xml)));
+  float ct = p2m_cosf(theta), st = p2m_sinf(theta), cp = p2m_cosf(phi), sp = p2m_sinf(phi);
+  for (int64_t i = 0; i < n; i++) {
+    if (!surv[i]) continue;
+    float *q = trec + i * nf;
+    float p1 = f1 ? -q[0] : q[0], p2 = f2 ? -q[1] : q[1], p3 = f3 ? -q[2] : q[2];
+    float xh = (p3 * ct) + (p1 * st);
+    float zh = ((-p3) * st) + (p1 * ct);
+    float yh = ((-xh) * sp) + (p2 * cp);
+    xh = (xh * cp) + (p2 * sp);
+    q[2] = zh;
+    q[1] = yh;
+    q[0] = xh;
+  }
+  for (int r = 0; r < ntasks; r++)
+    for (int64_t i = r * per; i < n && i < (r + 1) * per; i++) {
+      if (!surv[i] || recs[i * nf + 6] != rthmax) continue;
+      const float *q = trec + i * nf;
+      info[5] = sqrtf(((q[2] * q[2]) + (q[1] * q[1])) + (q[0] * q[0]));
+      info[6] = q[2];
+      info[7] = q[1];
+      info[8] = q[0];
+    }
+}
+
+/* halo loop over records [h0, h1): pks2map.f90:134-303.  With surv, the radial cut has
+   been made (surv[i]) and records holds the scrambled / rotated positions, while orig
+   holds the records as read (for the line-of-sight velocity). */
 static int paint_range(const orc_cosmo *c, const orc_params *p, const orc_table *tabs,
                        const float *records, int64_t h0, int64_t h1, const paint_out *o,
                        orc_stats *st, int64_t *set_halo, int64_t *set_pix, int64_t set_cap,
-                       int64_t *set_n) {
+                       int64_t *set_n, const unsigned char *surv, const float *orig) {
   float cut_low = orc_rofz(c, p->zmin), cut_high = orc_rofz(c, p->zmax);
   /* pks2map.f90:92-93: fov to radians, dpix */
   float fov = ((p->fov_deg / 360.0f) * 2.0f) * c->mypi;
@@ -584,13 +703,17 @@ static int paint_range(const orc_cosmo *c, const orc_params *p, const orc_table 
   for (int64_t i = h0; i < h1; i++) {
     const float *rec = records + i * p->nfloat;
     st->n_in++;
-    if (!halo_in_shell(rec, p->chihview, cut_low, cut_high)) continue;
+    if (surv ? !surv[i] : !halo_in_shell(rec, p->chihview, cut_low, cut_high)) continue;
     st->n_cut++;
     halo_state hs;
     if (!halo_prepare(c, p, rec, &hs)) continue;
     st->n_painted++;
+    /* a scrambled halo with a NaN position (each rank's first: its seed's unreduced
+       digits give a first draw above 1) counts and paints nothing */
+    if (!isfinite(hs.xh) || !isfinite(hs.yh) || !isfinite(hs.zh)) continue;
     float vmap[ORC_MAXMAPS];
-    for (int m = 0; m < p->nmaps; m++) vmap[m] = halo_vrad(rec, p->profile[m]);
+    const float *vrec = surv ? orig + i * p->nfloat : rec;
+    for (int m = 0; m < p->nmaps; m++) vmap[m] = halo_vrad(vrec, p->profile[m]);
     projecthalo_flatsky(c, p, tabs, &hs, vmap, fov, dpix, o, st);
     if (p->nside > 0) {
       rc = projecthalo_healpix(c, p, tabs, &hs, vmap, list, listcap, o, st, i, set_halo,
@@ -628,7 +751,25 @@ int orc_paint(const orc_params *p, const orc_table *tables, int ntables, const f
   orc_stats st;
   memset(&st, 0, sizeof(st));
   if (set_n) *set_n = 0;
-  rc = paint_range(c, p, tables, records, 0, nhalo, &o, &st, set_halo, set_pix, set_cap, set_n);
+  if (p->scramble || p->centre) {
+    float *trec = (float *)malloc(sizeof(float) * (size_t)(nhalo * p->nfloat + 1));
+    unsigned char *surv = (unsigned char *)malloc((size_t)nhalo + 1);
+    if (!trec || !surv) {
+      free(trec);
+      free(surv);
+      free(c);
+      return -20;
+    }
+    preprocess(p, records, nhalo, orc_rofz(c, p->zmin), orc_rofz(c, p->zmax), trec, surv,
+               st.centre);
+    rc = paint_range(c, p, tables, trec, 0, nhalo, &o, &st, set_halo, set_pix, set_cap, set_n,
+                     surv, records);
+    free(trec);
+    free(surv);
+  } else {
+    rc = paint_range(c, p, tables, records, 0, nhalo, &o, &st, set_halo, set_pix, set_cap,
+                     set_n, NULL, NULL);
+  }
   if (stats) *stats = st;
   free(c);
   return rc;
@@ -691,7 +832,8 @@ int orc_paint_threads(const orc_params *p, const orc_table *tables, int ntables,
       o.fs32 = fsl[tid];
       o.hp_npix = 12 * (int64_t)p->nside * p->nside;
       o.fs_npix2 = (int64_t)p->npix_fs * p->npix_fs;
-      rcs[tid] = paint_range(c, p, tables, records, h0, h1, &o, &sts[tid], NULL, NULL, 0, NULL);
+      rcs[tid] = paint_range(c, p, tables, records, h0, h1, &o, &sts[tid], NULL, NULL, 0, NULL,
+                             NULL, NULL);
     }
   }
   double t2 = now_s();
@@ -766,7 +908,8 @@ int orc_paint_ranks(const orc_params *p, const orc_table *tables, int ntables,
       o.fp32 = 1;
       o.hp32 = hp_maps[tid];
       o.hp_npix = 12 * (int64_t)p->nside * p->nside;
-      rcs[tid] = paint_range(c, p, tables, records, h0, h1, &o, &sts[tid], NULL, NULL, 0, NULL);
+      rcs[tid] = paint_range(c, p, tables, records, h0, h1, &o, &sts[tid], NULL, NULL, 0, NULL,
+                             NULL, NULL);
     }
   }
   orc_stats st;

@@ -55,6 +55,9 @@ typedef struct orc_params {
   int32_t table_id[ORC_MAXMAPS];
   int32_t fp32_accumulate;       /* 1: literal float accumulation (hpmapl += curval) */
   int32_t nfloat;                /* 7 or 10 floats per catalogue record */
+  int32_t scramble, centre;      /* command-line flags of pks2map.f90:75-76 */
+  int32_t ntasks;                /* MPI ranks whose streams and blocks scramble and centre
+                                    follow (pksc.f90:51-52; 0 or 1: one rank) */
 } orc_params;
 
 typedef struct orc_stats {
@@ -62,6 +65,8 @@ typedef struct orc_stats {
   int64_t hp_updates, fs_updates;   /* (halo, pixel) pairs passing the disc test */
   int64_t hp_candidates;            /* pixels returned by query_disc */
   int64_t ring_gaps;                /* discs whose non-empty rings are not contiguous */
+  float centre[9];                  /* with centre: RTHmax, then distance, x, y, z of the
+                                       largest halo before and after the rotation */
 } orc_stats;
 
 /* cosmology of pks2map.f90:118-132 and cosmology.f90:269-323 */

@@ -24,8 +24,9 @@ def masked_rel(a, b):
     return (np.abs(a[m] - b[m]) / np.abs(b[m])).max()
 
 
-@pytest.mark.parametrize("nfloat,profile", [(10, 1), (7, 2)])
-def test_pks2map_command_line(tmp_path, nfloat, profile):
+@pytest.mark.parametrize("nfloat,profile,scramble,centre", [(10, 1, 0, 0), (7, 2, 0, 0),
+                                                             (10, 1, 1, 1)])
+def test_pks2map_command_line(tmp_path, nfloat, profile, scramble, centre):
     exe = os.path.join(PKG, "pks2map")
     rec = catalogs.shell(41, 30_000, nfloat=nfloat)
     cat = str(tmp_path / "halos.pksc")
@@ -35,7 +36,7 @@ def test_pks2map_command_line(tmp_path, nfloat, profile):
     p2m.write_table(tabfile, tab)
     out = str(tmp_path / "map")
     nside, npix, fov, zmax = 256, 64, 10.0, 1.25
-    args = [exe, cat, out, tabfile, "0.0", str(nside), "0", "0", str(npix), str(fov),
+    args = [exe, cat, out, tabfile, "0.0", str(nside), str(scramble), str(centre), str(npix), str(fov),
             str(zmax), "0.0", "1", str(profile)]
     r = subprocess.run(args, capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stderr
@@ -48,6 +49,7 @@ def test_pks2map_command_line(tmp_path, nfloat, profile):
     # the same painting through the C ABI
     with p2m.Painter(nside=nside, npix_fs=npix, fov_deg=fov, zmax=zmax, maps=((0, profile),),
                      max_records=len(rec)) as pt:
+        pt.set_preprocess(scramble, centre, 1)
         pt.load_table(0, tab)
         pt.paint_records(rec)
         api_hp, api_fs, st = pt.healpix(0), pt.flatsky(0), pt.stats()
@@ -57,8 +59,9 @@ def test_pks2map_command_line(tmp_path, nfloat, profile):
 
     # and against the oracle
     p = oracle.params(nside=nside, npix_fs=npix, fov_deg=fov, zmax=zmax, maps=((0, profile),),
-                      nfloat=nfloat)
+                      nfloat=nfloat, scramble=scramble, centre=centre)
     ohp, ofs, ost, _ = oracle.paint(p, [oracle.Table(tab)], rec)
     assert masked_rel(hp, ohp[0]) <= 1e-5
     assert masked_rel(fs.ravel(), ofs[0]) <= 1e-6
     assert ost["n_painted"] == st["n_painted"]
+    assert ("After rotation largest halo is at" in r.stdout) == bool(centre)

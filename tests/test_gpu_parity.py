@@ -141,6 +141,43 @@ def test_stored_item_and_fused_paths(precision, big_rings, monkeypatch):
                           sum_tol=SUM_TOL if precision == "fp64" else SUM_TOL_MIXED_FEW)
 
 
+@pytest.mark.parametrize("scramble,centre,ntasks", [(1, 0, 1), (0, 1, 1), (1, 1, 1), (1, 1, 3)])
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_scramble_and_centre(scramble, centre, ntasks, precision):
+    """pks2map's scramble (the reference's ranf stream per rank, jumped ahead on the GPU)
+    and center (flips and rotations about the largest halo): pixel sets bit-exact against
+    the oracle, which runs the generator sequentially."""
+    rec = catalogs.shell(23, 20_000)
+    tab = catalogs.table()
+    maps = ((0, 1), (0, 2))
+    with p2m.Painter(nside=256, precision=precision, maps=maps, flags=FLAGS,
+                     max_records=len(rec)) as pt:
+        pt.set_preprocess(scramble, centre, ntasks)
+        pt.load_table(0, tab)
+        pt.paint_records(rec)
+        hp = np.stack([pt.healpix(m) for m in range(2)])
+        st, sets, info = pt.stats(), pt.pixel_sets(), pt.centre_info()
+    p = oracle.params(nside=256, maps=maps, nfloat=10, scramble=scramble, centre=centre,
+                      ntasks=ntasks)
+    rhp, _, rst, rsets = oracle.paint(p, [oracle.Table(tab)], rec, record_sets=True)
+    assert_sets_equal(sets, rsets)
+    assert st["n_painted"] == rst["n_painted"]
+    for m in range(2):
+        assert_maps_close(hp[m], rhp[m], what="map %d" % m,
+                          sum_tol=SUM_TOL if precision == "fp64" else SUM_TOL_MIXED_FEW)
+    if centre:
+        assert np.array_equal(info, np.array(rst["centre"], dtype=np.float32))
+
+
+def test_preprocess_needs_one_call():
+    rec = catalogs.shell(24, 4000)
+    with p2m.Painter(nside=64, max_records=2000) as pt:
+        pt.set_preprocess(1, 0, 1)
+        pt.load_table(0, catalogs.table())
+        with pytest.raises(p2m.P2MError):
+            pt.paint_records(rec)  # two chunks of 2000 records
+
+
 def test_layout7_chihview_and_bad_records():
     rec = catalogs.shell(5, 20_000, nfloat=7).copy()
     rec[::997, 0] = np.nan
