@@ -127,6 +127,24 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def max_over_ranks(x, device=None):
+    """The largest of x over the ranks of the default process group (x itself without
+    one): every replica's time enters the whole-job throughput through the slowest."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(x)
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_throughput(units_per_rank, world_size, ms_max):
+    """Whole-job units/s of replicas that each process units_per_rank, timed by the
+    slowest rank (weak scaling: the work per replica is fixed)."""
+    return units_per_rank * world_size / (ms_max * 1e-3)
+
+
 def catalogue(n):
     import matt_young_mapmaking_gb300 as p2m
     return p2m.generate_catalogue(SEED, n, 10, r=SHELL, m=MASS)
@@ -262,11 +280,7 @@ def run_ours(args):
         ev1.record(stream)
         barrier()
         clocks = sampler.stop() if sampler else None
-        ms = ev0.elapsed_time(ev1) / steps
-        if ws > 1:
-            t = torch.tensor([ms], device=dev)
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            ms = float(t.item())
+        ms = max_over_ranks(ev0.elapsed_time(ev1) / steps, dev)
         return ms, clocks
 
     pt = make(args.precision)
@@ -291,7 +305,7 @@ def run_ours(args):
     for _ in range(args.steps):
         e2e_step()
     barrier()
-    e2e_ms = 1e3 * (time.perf_counter() - t0) / args.steps
+    e2e_ms = max_over_ranks(1e3 * (time.perf_counter() - t0) / args.steps, dev)
     pt.close()
     # the host link alone: the same copies without the painting
     d_tmp = torch.empty_like(h_rec, device=dev)
@@ -310,7 +324,7 @@ def run_ours(args):
     del d_tmp
 
     total_halos = N * ws
-    value = total_halos / (ms * 1e-3)
+    value = job_throughput(N, ws, ms)
     upd = st["hp_updates"] * len(MAPS)
     peaks = {}
     try:
