@@ -1388,14 +1388,34 @@ __global__ void __launch_bounds__(256) k_finalize_full(double *acc, long long np
       }
     }
   } else {
-    for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < npix; p += stride) {
-      for (int m = 0; m < nmaps; m++) {
-        double *ad = acc + p * nmaps + m;
-        float v = (float)__ldcs(ad);
-        __stcs(ad, 0.0);
-        if (accumulate) v = __fadd_rn(outs[m][p], v);
-        __stcs(outs[m] + p, v);
-      }
+    /* any other map count: the block moves 256 pixels' interleaved accumulators at a time
+       through shared memory, so that the reads and the clearing stores are linear over
+       whole sectors (a per-pixel loop at a stride of nmaps doubles leaves partial-sector
+       writes behind) and every thread has up to P2M_MAXMAPS loads in flight */
+    __shared__ float sv[256 * P2M_MAXMAPS];
+    const int t = threadIdx.x;
+    for (long long base = (long long)blockIdx.x * 256; base < npix; base += (long long)gridDim.x * 256) {
+      const int np = (int)(npix - base < 256 ? npix - base : 256);
+      const int n = np * nmaps;
+      double *a = acc + base * nmaps;
+      double r[P2M_MAXMAPS];
+#pragma unroll
+      for (int k = 0; k < P2M_MAXMAPS; k++)
+        if (t + k * 256 < n) r[k] = __ldcs(a + t + k * 256);
+#pragma unroll
+      for (int k = 0; k < P2M_MAXMAPS; k++)
+        if (t + k * 256 < n) {
+          sv[t + k * 256] = (float)r[k];
+          __stcs(a + t + k * 256, 0.0);
+        }
+      __syncthreads();
+      if (t < np)
+        for (int m = 0; m < nmaps; m++) {
+          float v = sv[t * nmaps + m];
+          if (accumulate) v = __fadd_rn(outs[m][base + t], v);
+          __stcs(outs[m] + base + t, v);
+        }
+      __syncthreads();
     }
   }
 }
