@@ -397,9 +397,10 @@ def run_ours(args):
         pp = make("fp64")
         ms64, _ = timed(pp, max(2, args.steps // 2), 1)
         ref_maps = [o.cpu().numpy() for o in outs]
+        phases64 = pp.timings()
         pp.close()
         out["plain_fp64"] = {"value": total_halos / (ms64 * 1e-3), "ms_per_step": ms64,
-                             "speedup_of_mixed": ms64 / ms}
+                             "speedup_of_mixed": ms64 / ms, "phases_ms": phases64}
         errs = {}
         for m, name in enumerate(("tsz", "ksz")):
             a = maps_main[m].astype(np.float64)

@@ -546,9 +546,11 @@ p2m_status sweep(p2m_ctx *ctx, cudaStream_t s) {
     /* fold the sparse low words into the maps and clear them */
     p2m_launch_fold_lo(P, W, s, ctx->nsm);
   } else {
-    /* the read-out also clears the accumulator for the next paint */
+    /* the read-out reads the accumulator; a memset then clears it for the next paint */
     p2m_launch_finalize_full(P, ctx->d_acc64, ctx->hp_npix, ctx->d_out, ctx->swept ? 1 : 0, s,
                              ctx->nsm);
+    CK(cudaMemsetAsync(ctx->d_acc64, 0,
+                       sizeof(double) * (size_t)ctx->cfg.nmaps * (size_t)ctx->hp_npix, s));
   }
   TE(PH_READOUT);
   CK(cudaGetLastError());
