@@ -72,6 +72,32 @@ int32_t p2m_write_flatsky(const char *path, const float *map, int32_t npix, floa
    order, NSIDE and ORDERING = 'RING' cards (pks2map.f90:381-385, HEALPix output_map) */
 int32_t p2m_write_healpix_fits(const char *path, const float *map, int32_t nside);
 
+/* Angular power spectra of painted maps, for the precision report (validation only;
+   host maps in, spectra out, synchronous, device memory allocated for the call).
+
+   p2m_cl_healpix: the spectra of RING-ordered HEALPix maps up to lmax (<= 4 nside and
+   <= P2M_CL_LMAX_MAX), by the pixel-area quadrature of the HEALPix library that the
+   reference vendors: map2alm without iterations and with unit ring weights
+   (src/modules/External/alm_map_dd_inc.F90:2978-3224, ring_analysis and the lambda_lm
+   recursion of alm_tools.F90:394-650, 1022-1097), then alm2cl (alm_map_dd_inc.F90:5347-5423).
+   cl_aa[l], and with map_b, cl_ab[l] = sum_m Re a_lm conj(b_lm) / (2l+1) and cl_bb[l],
+   for l = 0 .. lmax.  map_b may be NULL (cl_ab and cl_bb are then not written).
+
+   p2m_cl_flatsky: binned periodogram of npix x npix flat-sky maps over fov_rad x fov_rad
+   (the layout of p2m_get_flatsky): nbins (<= P2M_CL_MAXBINS) linear bins of ell = 2 pi |k| / fov in
+   (0, ell_max], C = (fov^2 / npix^4) |FFT(map)(k)|^2 averaged over each bin's modes;
+   ell_mean is the bins' mean ell and nmodes their mode counts.  The mode k = 0 and the
+   Nyquist line are left out.  npix is a power of two up to 8192, or any size up to
+   2048.  The reference computes no flat-sky spectrum; this one stands beside the
+   HEALPix one for the 8192^2 map. */
+#define P2M_CL_LMAX_MAX 16384
+#define P2M_CL_MAXBINS 1024
+int32_t p2m_cl_healpix(int32_t device, const float *map_a, const float *map_b, int32_t nside,
+                       int32_t lmax, double *cl_aa, double *cl_ab, double *cl_bb);
+int32_t p2m_cl_flatsky(int32_t device, const float *map_a, const float *map_b, int32_t npix,
+                       float fov_rad, double ell_max, int32_t nbins, double *ell_mean,
+                       double *cl_aa, double *cl_ab, double *cl_bb, int64_t *nmodes);
+
 /* Self-test of the single-precision math the kernels use (fn: 0 log, 1 exp, 2 pow,
    3 asin, 4 atan, 5 sin, 6 cos, 7 tan) evaluated on the GPU over n device floats;
    d_y is read only for pow.  Synchronous.  Returns 0 or a CUDA error code. */

@@ -9,7 +9,7 @@ from .capi import (FLAG_ALL_HALOS, FLAG_RECORD_SETS, FLAG_TIMING, FLAG_VALIDATE,
                    PREC_FP64, PREC_MIXED,
                    P2MConfig, P2MError, Painter, exported_symbols, generate_catalogue,
                    load_library, make_maptable)
-from .capi import dpdy, write_outputs
+from .capi import cl_flatsky, cl_healpix, dpdy, write_outputs
 from .formats import (detect_layout, read_dpdy, read_flatsky, read_healpix_fits, read_pksc,
                       read_table, table_array, table_header, write_pksc, write_table)
 
@@ -18,4 +18,5 @@ __all__ = ["FLAG_ALL_HALOS", "FLAG_RECORD_SETS", "FLAG_TIMING", "FLAG_VALIDATE",
            "P2MConfig", "P2MError", "Painter", "exported_symbols", "generate_catalogue",
            "load_library", "make_maptable", "detect_layout", "read_pksc", "read_table",
            "table_array", "table_header", "write_pksc", "write_table", "dpdy", "write_outputs",
+           "cl_healpix", "cl_flatsky",
            "read_dpdy", "read_flatsky", "read_healpix_fits"]

@@ -25,7 +25,7 @@ MAPTABLE_CLI = os.path.join(PKG, "make_maptable")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",
               "-I" + CSRC, "-I" + INCLUDE]
-CU_SOURCES = ["p2m_kernels.cu", "p2m_capi.cu", "p2m_noalloc.cu"]
+CU_SOURCES = ["p2m_kernels.cu", "p2m_capi.cu", "p2m_noalloc.cu", "p2m_spectra.cu"]
 CPP_SOURCES = ["p2m_tools.cpp", "p2m_outputs.cpp"]
 
 

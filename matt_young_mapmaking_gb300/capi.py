@@ -114,6 +114,8 @@ def load_library():
         "p2m_write_dpdy": (I32, [ctypes.c_char_p, VP]),
         "p2m_write_flatsky": (I32, [ctypes.c_char_p, VP, I32, F]),
         "p2m_write_healpix_fits": (I32, [ctypes.c_char_p, VP, I32]),
+        "p2m_cl_healpix": (I32, [I32, VP, VP, I32, I32, VP, VP, VP]),
+        "p2m_cl_flatsky": (I32, [I32, VP, VP, I32, F, D, I32, VP, VP, VP, VP, VP]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -133,7 +135,7 @@ def exported_symbols():
             "p2m_generate_catalogue", "p2m_philox4x32", "p2m_fmath_eval_device",
             "p2m_get_timings", "p2m_map_sums_noalloc", "p2m_set_preprocess", "p2m_get_centre",
             "p2m_dpdy", "p2m_write_dpdy",
-            "p2m_write_flatsky", "p2m_write_healpix_fits"]
+            "p2m_write_flatsky", "p2m_write_healpix_fits", "p2m_cl_healpix", "p2m_cl_flatsky"]
 
 
 PHASES = ["cut", "setup", "big_scan", "big_items", "flatsky", "big_offsets", "paint", "paint_big",
@@ -313,6 +315,58 @@ def make_maptable(model=1, nu=0.0, alpha_cmb=0.0, nchit=0, nmht=0, nrt=0, device
     if st:
         raise P2MError(st, "make_maptable failed")
     return buf.tobytes()
+
+
+CL_LMAX_MAX = 16384
+CL_MAXBINS = 1024
+
+
+def cl_healpix(map_a, map_b=None, lmax=None, device=0):
+    """Angular power spectra of RING-ordered HEALPix maps on the GPU (include/p2m_tools.h
+    p2m_cl_healpix).  Returns {"aa": C_l of map_a} plus "ab" and "bb" when map_b is given,
+    each an array over l = 0 .. lmax (default 3 nside - 1)."""
+    lib = load_library()
+    a = np.ascontiguousarray(map_a, dtype=np.float32)
+    nside = int(round(np.sqrt(a.size / 12.0)))
+    if 12 * nside * nside != a.size:
+        raise P2MError(1, "map size %d is not 12 nside^2" % a.size)
+    if lmax is None:
+        lmax = 3 * nside - 1
+    b = None if map_b is None else np.ascontiguousarray(map_b, dtype=np.float32)
+    if b is not None and b.size != a.size:
+        raise P2MError(1, "maps differ in size")
+    out = {k: np.zeros(lmax + 1) for k in (("aa", "ab", "bb") if b is not None else ("aa",))}
+    st = lib.p2m_cl_healpix(device, _ptr(a), None if b is None else _ptr(b), nside, lmax,
+                            _ptr(out["aa"]), None if b is None else _ptr(out["ab"]),
+                            None if b is None else _ptr(out["bb"]))
+    if st:
+        raise P2MError(st, "p2m_cl_healpix failed")
+    return out
+
+
+def cl_flatsky(map_a, map_b=None, fov_rad=None, ell_max=8000.0, nbins=100, device=0):
+    """Binned angular power spectra of npix x npix flat-sky maps over fov_rad (include/
+    p2m_tools.h p2m_cl_flatsky).  Returns {"ell", "nmodes", "aa"} plus "ab" and "bb" when
+    map_b is given."""
+    lib = load_library()
+    a = np.ascontiguousarray(map_a, dtype=np.float32).ravel()
+    npix = int(round(np.sqrt(a.size)))
+    if npix * npix != a.size or fov_rad is None:
+        raise P2MError(1, "flat-sky maps are npix^2 floats with a field of view")
+    b = None if map_b is None else np.ascontiguousarray(map_b, dtype=np.float32).ravel()
+    if b is not None and b.size != a.size:
+        raise P2MError(1, "maps differ in size")
+    out = {"ell": np.zeros(nbins), "nmodes": np.zeros(nbins, dtype=np.int64),
+           "aa": np.zeros(nbins)}
+    if b is not None:
+        out["ab"], out["bb"] = np.zeros(nbins), np.zeros(nbins)
+    st = lib.p2m_cl_flatsky(device, _ptr(a), None if b is None else _ptr(b), npix, fov_rad,
+                            ell_max, nbins, _ptr(out["ell"]), _ptr(out["aa"]),
+                            None if b is None else _ptr(out["ab"]),
+                            None if b is None else _ptr(out["bb"]), _ptr(out["nmodes"]))
+    if st:
+        raise P2MError(st, "p2m_cl_flatsky failed")
+    return out
 
 
 def generate_catalogue(seed, n, nfloat=10, r=(100.0, 3000.0), m=(1e12, 1e15), slope=-0.9,
