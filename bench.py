@@ -57,6 +57,10 @@ def parse():
     ap.add_argument("--no-plain", action="store_true", help="skip the FP64 drop-in comparison")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--cpu-fraction", type=float, default=0.1)
+    ap.add_argument("--cl-lmax", type=int, default=2047,
+                    help="lmax of the C_l ratio of the Nside 4096 maps (0: skip)")
+    ap.add_argument("--no-precision-form", action="store_true",
+                    help="skip the precision-form report (1e5 halos, Nside 512 + 8192^2 flat sky)")
     return ap.parse_args()
 
 
@@ -143,6 +147,77 @@ def job_throughput(units_per_rank, world_size, ms_max):
     """Whole-job units/s of replicas that each process units_per_rank, timed by the
     slowest rank (weak scaling: the work per replica is fixed)."""
     return units_per_rank * world_size / (ms_max * 1e-3)
+
+
+def map_errors(a, b):
+    """Error of map a against the FP64 map b: per-pixel max-abs, relative L2, the largest
+    relative error where |b| > 1e-3 max|b|, and the total's error relative to the total
+    and to sum|b| (the two differ for the signed kSZ map)."""
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    mx = np.abs(b).max()
+    mask = np.abs(b) > 1e-3 * mx
+    rel = np.abs(a[mask] - b[mask]) / np.abs(b[mask])
+    return {"max_rel_masked": float(rel.max()) if rel.size else 0.0,
+            "max_abs": float(np.abs(a - b).max()),
+            "rel_l2": float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)),
+            "total_rel": float(abs(a.sum() - b.sum()) / max(abs(b.sum()), 1e-300)),
+            "total_rel_abs": float(abs(a.sum() - b.sum()) / max(np.abs(b).sum(), 1e-300))}
+
+
+def cl_ratio(spec, lmin=1):
+    """max and rms of |C(a) / C(b) - 1| over the multipoles (or bins) from lmin on where
+    C(b) is nonzero, from a spectra dict with "aa" (map a) and "bb" (the FP64 map b)."""
+    aa, bb = np.asarray(spec["aa"])[lmin:], np.asarray(spec["bb"])[lmin:]
+    sel = bb > 0
+    d = np.abs(aa[sel] / bb[sel] - 1.0)
+    return {"max": float(d.max()) if d.size else None,
+            "rms": float(np.sqrt(np.mean(d * d))) if d.size else None}
+
+
+def precision_form(device):
+    """The precision form of the path: the 1e5-halo catalogue (seed 1, shell 100-3000 Mpc,
+    masses 1e12-1e15) painted with the 148 GHz alpha = 0 table to a HEALPix Nside 512 tSZ
+    map and a flat-sky 8192^2 map over 10 degrees, by the mixed painter (FP32 profile
+    values, compensated FP32 accumulation) and by the FP64-accumulating painter.  Reports
+    the per-map errors of the mixed maps against the FP64 maps, the C_l ratio (l <= 1535 on
+    the sphere, 100 bins of ell <= 8000 on the flat sky) and the paint times."""
+    import torch
+
+    import matt_young_mapmaking_gb300 as p2m
+    n, nside, nfs, fov = 100_000, 512, 8192, 10.0
+    rec = p2m.generate_catalogue(1, n, 10, r=(100.0, 3000.0), m=(1e12, 1e15))
+    d_rec = torch.from_numpy(rec).to(torch.device("cuda", device))
+    table = p2m.make_maptable(1, 148.0, 0.0, device=device)
+    maps, times = {}, {}
+    for prec in ("mixed", "fp64"):
+        with p2m.Painter(nside=nside, npix_fs=nfs, fov_deg=fov, precision=prec,
+                         maps=((0, 1),), max_records=n, device=device) as pt:
+            pt.load_table(0, table)
+            ts = []
+            for _ in range(6):
+                pt.reset()
+                torch.cuda.synchronize(device)
+                t0 = time.perf_counter()
+                pt.paint_records_device(d_rec.data_ptr(), n, 10)
+                pt.flush()
+                pt.synchronize()
+                ts.append(time.perf_counter() - t0)
+            times[prec] = 1e3 * float(np.median(ts[1:]))
+            maps[prec] = (pt.healpix(0), pt.flatsky(0))
+    hp_cl = p2m.cl_healpix(maps["mixed"][0], maps["fp64"][0], lmax=3 * nside - 1,
+                           device=device)
+    fs_cl = p2m.cl_flatsky(maps["mixed"][1], maps["fp64"][1], fov_rad=np.radians(fov),
+                           ell_max=8000.0, nbins=100, device=device)
+    return {"workload": "%d halos (seed 1, 100-3000 Mpc, 1e12-1e15), 148 GHz table, "
+                        "HEALPix Nside %d + flat sky %d^2 over %g deg" % (n, nside, nfs, fov),
+            "ms_mixed": times["mixed"], "ms_fp64": times["fp64"],
+            "halos_per_s_mixed": n / (times["mixed"] * 1e-3),
+            "timing": "wall clock around paint + read-out, median of 5 after one warm-up",
+            "healpix": dict(map_errors(maps["mixed"][0], maps["fp64"][0]),
+                            cl_ratio=dict(cl_ratio(hp_cl), lmax=3 * nside - 1)),
+            "flatsky": dict(map_errors(maps["mixed"][1], maps["fp64"][1]),
+                            cl_ratio=dict(cl_ratio(fs_cl, lmin=0), ell_max=8000.0, bins=100))}
 
 
 def catalogue(n):
@@ -403,16 +478,14 @@ def run_ours(args):
                              "speedup_of_mixed": ms64 / ms, "phases_ms": phases64}
         errs = {}
         for m, name in enumerate(("tsz", "ksz")):
-            a = maps_main[m].astype(np.float64)
-            b = ref_maps[m].astype(np.float64)
-            mx = np.abs(b).max()
-            mask = np.abs(b) > 1e-3 * mx
-            rel = np.abs(a[mask] - b[mask]) / np.abs(b[mask])
-            errs[name] = {"max_rel_masked": float(rel.max()) if rel.size else 0.0,
-                          "max_abs": float(np.abs(a - b).max()),
-                          "rel_l2": float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)),
-                          "total_rel": float(abs(a.sum() - b.sum()) / max(abs(b.sum()), 1e-300))}
+            errs[name] = map_errors(maps_main[m], ref_maps[m])
+            if args.cl_lmax > 0:
+                spec = p2m.cl_healpix(maps_main[m], ref_maps[m], lmax=args.cl_lmax, device=local)
+                errs[name]["cl_ratio"] = dict(cl_ratio(spec), lmax=args.cl_lmax)
         out["error_vs_fp64"] = errs
+
+    if rank == 0 and not args.no_precision_form:
+        out["precision_form"] = precision_form(local)
 
     if rank == 0 and ws == 1 and not args.no_cpu:
         vals, info = cpu_reference(rec, nside, os.cpu_count() or 1, N * args.cpu_fraction)
