@@ -81,7 +81,13 @@ typedef struct p2m_config {
   int64_t max_records; /* largest record count of one paint call */
   int32_t device;      /* CUDA device ordinal */
   int32_t flags;       /* P2M_FLAG_* */
+  int32_t ncones;      /* 0 or 1: one sky.  2..P2M_MAXCONES: an ensemble of independent
+                          light-cones (p2m_paint_ensemble), each painted to its own copy
+                          of the nmaps HEALPix maps; HEALPix only (npix_fs = 0).  No
+                          counterpart in the reference, which paints one cone per run */
 } p2m_config;
+
+#define P2M_MAXCONES 4096
 
 typedef struct p2m_stats {
   int64_t n_records;   /* records read */
@@ -134,6 +140,21 @@ p2m_status p2m_paint_records_device(p2m_ctx *ctx, const float *d_records, int64_
    for projecthalo_flatsky + projecthalo_healpix.  Queued halos are painted on the next
    read of a map or by p2m_flush.  x, y, z are divided by chi in place, as
    projecthalo_flatsky does to its caller's variables (haloproject.f90:97-99). */
+/* Ensemble form (cfg.ncones > 1): ncones independent catalogues in one call, concatenated
+   in records, cone c owning records [offsets[c], offsets[c+1]) (offsets[0] = 0,
+   non-decreasing, ncones + 1 host values, ncones <= cfg.ncones).  Every cone goes through
+   the halo loop of pks2map.f90:134-303 exactly as a p2m_paint_records call of its own
+   would, into its own maps; all cones share one enumeration and one painting launch.
+   With an ensemble, map m is ncones x 12 nside^2 floats, cone-major: p2m_get_healpix and
+   the device read-outs move all cones, p2m_get_healpix_cone one.  Records painted by
+   p2m_paint_records or p2m_project_halo go to cone 0. */
+p2m_status p2m_paint_ensemble(p2m_ctx *ctx, const float *records, const int64_t *offsets,
+                              int32_t ncones, int32_t nfloat);
+p2m_status p2m_paint_ensemble_device(p2m_ctx *ctx, const float *d_records,
+                                     const int64_t *offsets, int32_t ncones, int32_t nfloat,
+                                     void *stream);
+p2m_status p2m_get_healpix_cone(p2m_ctx *ctx, int32_t cone, int32_t map, float *out);
+
 p2m_status p2m_project_halo(p2m_ctx *ctx, float *x, float *y, float *z, const float *r,
                             const float *chi, const float *m, const float *redshift,
                             const float *v, const int32_t *profile);
@@ -145,7 +166,8 @@ p2m_status p2m_get_healpix(p2m_ctx *ctx, int32_t map, float *out);
 p2m_status p2m_get_flatsky(p2m_ctx *ctx, int32_t map, float *out);
 /* ... or device memory, ordered on `stream` (NULL = the context's stream). */
 p2m_status p2m_get_healpix_device(p2m_ctx *ctx, int32_t map, float *d_out, void *stream);
-/* Make a caller-owned device buffer of 12*nside^2 floats the storage of HEALPix map `map`
+/* Make a caller-owned device buffer of 12*nside^2 floats (times ncones for an ensemble)
+   the storage of HEALPix map `map`
    (the reference's hpmap allocation, pks2map.f90:113): read-outs then write it in place
    and p2m_get_healpix_device with the same pointer copies nothing.  Call right after
    p2m_create or p2m_reset_maps; NULL restores the context's own buffer. */

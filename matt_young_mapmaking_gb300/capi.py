@@ -46,6 +46,7 @@ class P2MConfig(ctypes.Structure):
         ("max_records", ctypes.c_int64),
         ("device", ctypes.c_int32),
         ("flags", ctypes.c_int32),
+        ("ncones", ctypes.c_int32),
     ]
 
 
@@ -115,6 +116,9 @@ def load_library():
         "p2m_write_flatsky": (I32, [ctypes.c_char_p, VP, I32, F]),
         "p2m_write_healpix_fits": (I32, [ctypes.c_char_p, VP, I32]),
         "p2m_cl_healpix": (I32, [I32, VP, VP, I32, I32, VP, VP, VP]),
+        "p2m_paint_ensemble": (I32, [VP, VP, VP, I32, I32]),
+        "p2m_paint_ensemble_device": (I32, [VP, VP, VP, I32, I32, VP]),
+        "p2m_get_healpix_cone": (I32, [VP, I32, I32, VP]),
         "p2m_cl_flatsky": (I32, [I32, VP, VP, I32, F, D, I32, VP, VP, VP, VP, VP]),
     }
     for name, (res, args) in sig.items():
@@ -135,7 +139,8 @@ def exported_symbols():
             "p2m_generate_catalogue", "p2m_philox4x32", "p2m_fmath_eval_device",
             "p2m_get_timings", "p2m_map_sums_noalloc", "p2m_set_preprocess", "p2m_get_centre",
             "p2m_dpdy", "p2m_write_dpdy",
-            "p2m_write_flatsky", "p2m_write_healpix_fits", "p2m_cl_healpix", "p2m_cl_flatsky"]
+            "p2m_write_flatsky", "p2m_write_healpix_fits", "p2m_cl_healpix", "p2m_cl_flatsky",
+            "p2m_paint_ensemble", "p2m_paint_ensemble_device", "p2m_get_healpix_cone"]
 
 
 PHASES = ["cut", "setup", "big_scan", "big_items", "flatsky", "big_offsets", "paint", "paint_big",
@@ -155,7 +160,7 @@ class Painter:
 
     def __init__(self, nside=4096, npix_fs=0, fov_deg=10.0, zmin=0.0, zmax=1.25,
                  chihview=0.0, model=1, precision=PREC_MIXED, maps=((0, 1),),
-                 max_records=1 << 22, device=0, flags=0):
+                 max_records=1 << 22, device=0, flags=0, ncones=0):
         self._lib = load_library()
         cfg = P2MConfig()
         cfg.nside, cfg.npix_fs, cfg.fov_deg = nside, npix_fs, fov_deg
@@ -171,6 +176,8 @@ class Painter:
         for i, (t, p) in enumerate(maps):
             cfg.map_table[i], cfg.map_profile[i] = t, p
         cfg.max_records, cfg.device, cfg.flags = max_records, device, flags
+        cfg.ncones = ncones
+        self.ncones = max(ncones, 1)
         self.cfg = cfg
         self.nmaps = len(maps)
         self.nside, self.npix_fs = nside, npix_fs
@@ -240,6 +247,29 @@ class Painter:
         self._check(self._lib.p2m_paint_records_device(self._h, ctypes.c_void_p(dptr), n, nfloat,
                                                        ctypes.c_void_p(stream or 0)))
 
+    def paint_ensemble(self, records, offsets):
+        """Ensemble form: records of independent light-cones, concatenated; cone c owns
+        records[offsets[c]:offsets[c + 1]] and is painted to its own maps."""
+        rec = np.ascontiguousarray(records, dtype=np.float32)
+        off = np.ascontiguousarray(offsets, dtype=np.int64)
+        if rec.ndim != 2 or rec.shape[1] not in (7, 10):
+            raise P2MError(1, "records must be (n, 7) or (n, 10)")
+        if off.ndim != 1 or off.size < 2 or off[-1] != rec.shape[0]:
+            raise P2MError(1, "offsets must hold ncones + 1 values ending at the record count")
+        self._check(self._lib.p2m_paint_ensemble(self._h, _ptr(rec), _ptr(off), off.size - 1,
+                                                 rec.shape[1]))
+
+    def paint_ensemble_device(self, dptr, offsets, nfloat, stream=None):
+        off = np.ascontiguousarray(offsets, dtype=np.int64)
+        self._check(self._lib.p2m_paint_ensemble_device(self._h, ctypes.c_void_p(dptr), _ptr(off),
+                                                        off.size - 1, nfloat,
+                                                        ctypes.c_void_p(stream or 0)))
+
+    def healpix_cone(self, cone, m=0):
+        out = np.empty(12 * self.nside * self.nside, dtype=np.float32)
+        self._check(self._lib.p2m_get_healpix_cone(self._h, cone, m, _ptr(out)))
+        return out
+
     def project_halo(self, x, y, z, r, chi, m, redshift, v, profile):
         """Queue one halo with precomputed loop quantities; returns (x, y, z)/chi as the
         reference leaves them in its caller."""
@@ -253,7 +283,8 @@ class Painter:
         self._check(self._lib.p2m_flush(self._h))
 
     def healpix(self, m=0):
-        out = np.empty(12 * self.nside * self.nside, dtype=np.float32)
+        """Map m (with an ensemble: every cone's copy, cone-major)."""
+        out = np.empty(12 * self.nside * self.nside * self.ncones, dtype=np.float32)
         self._check(self._lib.p2m_get_healpix(self._h, m, _ptr(out)))
         return out
 
@@ -317,6 +348,7 @@ def make_maptable(model=1, nu=0.0, alpha_cmb=0.0, nchit=0, nmht=0, nrt=0, device
     return buf.tobytes()
 
 
+MAXCONES = 4096
 CL_LMAX_MAX = 16384
 CL_MAXBINS = 1024
 

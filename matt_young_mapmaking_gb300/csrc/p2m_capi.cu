@@ -45,8 +45,12 @@ struct p2m_ctx {
   float *d_tab[P2M_MAXTABLES] = {};
   float band_u = 2e-4f;
   int big_rings = P2M_BIG_RINGS;
-  /* outputs */
+  /* outputs: hp_npix counts every cone's pixels (ncones * cone_npix) */
   long long hp_npix = 0, fs_npix = 0;
+  long long cone_npix = 0;
+  int ncones = 1;
+  long long *d_cone_off = nullptr; /* first record of each cone of the current call */
+  std::vector<long long> cone_off_host;
   float *d_out_own[P2M_MAXMAPS] = {};
   float *d_out[P2M_MAXMAPS] = {};
   double *d_acc64 = nullptr; /* full-sky FP64 accumulator (plain and FP64-accumulating paths) */
@@ -208,6 +212,7 @@ PaintParams make_params(const p2m_ctx *ctx, int nfloat) {
   P.band_u = ctx->band_u;
   P.inv_drt = ctx->th_set ? 1.0f / ctx->th.drt : 0.0f;
   P.big_rings = ctx->big_rings;
+  P.cone_npix = ctx->cone_npix;
   if (ctx->th_set) {
     float fr;
     int ir;
@@ -446,7 +451,7 @@ p2m_status preprocess(p2m_ctx *ctx, const float *d_rec, long long nrec, int nflo
 }
 
 p2m_status ingest_device(p2m_ctx *ctx, const float *d_rec, long long nrec, int nfloat,
-                         cudaStream_t s) {
+                         cudaStream_t s, int ncones = 0) {
   if (nfloat != 7 && nfloat != 10) return fail(ctx, P2M_ERR_BADARG, "nfloat must be 7 or 10");
   if (nrec < 0) return fail(ctx, P2M_ERR_BADARG, "negative record count");
   if (nrec > (1LL << 31) - 1) return fail(ctx, P2M_ERR_BADARG, "more than 2^31-1 records per call");
@@ -462,6 +467,10 @@ p2m_status ingest_device(p2m_ctx *ctx, const float *d_rec, long long nrec, int n
   if (pre) ST(preprocess(ctx, d_rec, nrec, nfloat, s));
   PaintParams P = make_params(ctx, nfloat);
   IngestBuffers B = ingest_buffers(ctx, d_rec);
+  if (ncones > 1) {
+    B.cone_off = ctx->d_cone_off;
+    B.ncones = ncones;
+  }
   TB(PH_CUT);
   p2m_launch_cut_setup(P, B, nrec, s, ctx->nsm);
   TE(PH_CUT);
@@ -589,6 +598,8 @@ p2m_status p2m_create(const p2m_config *cfg, p2m_ctx **out) {
   if (cfg->model < 1 || cfg->model > 3) return P2M_ERR_BADARG;
   if (cfg->nmaps < 1 || cfg->nmaps > P2M_MAXMAPS) return P2M_ERR_BADARG;
   if (cfg->precision < P2M_PREC_FP64 || cfg->precision > P2M_PREC_MIXED_F64) return P2M_ERR_BADARG;
+  if (cfg->ncones < 0 || cfg->ncones > P2M_MAXCONES) return P2M_ERR_BADARG;
+  if (cfg->ncones > 1 && (cfg->nside == 0 || cfg->npix_fs != 0)) return P2M_ERR_BADARG;
   for (int m = 0; m < cfg->nmaps; m++) {
     if (cfg->map_table[m] < 0 || cfg->map_table[m] >= P2M_MAXTABLES) return P2M_ERR_BADARG;
     if (cfg->map_profile[m] != 1 && cfg->map_profile[m] != 2) return P2M_ERR_BADARG;
@@ -641,7 +652,11 @@ p2m_status p2m_create(const p2m_config *cfg, p2m_ctx **out) {
     }
     CK(cudaMalloc((void **)&ctx->d_phitab, sizeof(float4) * P2M_PHITAB));
     CK(cudaMemcpy(ctx->d_phitab, pt.data(), sizeof(float4) * P2M_PHITAB, cudaMemcpyHostToDevice));
-    ctx->hp_npix = 12LL * cfg->nside * cfg->nside;
+    ctx->ncones = cfg->ncones > 1 ? cfg->ncones : 1;
+    ctx->cone_npix = 12LL * cfg->nside * cfg->nside;
+    ctx->hp_npix = ctx->cone_npix * ctx->ncones;
+    if (ctx->ncones > 1)
+      CK(cudaMalloc((void **)&ctx->d_cone_off, sizeof(long long) * (size_t)(ctx->ncones + 1)));
     for (int m = 0; m < cfg->nmaps; m++) {
       CK(cudaMalloc((void **)&ctx->d_out_own[m], sizeof(float) * (size_t)ctx->hp_npix));
       ctx->d_out[m] = ctx->d_out_own[m];
@@ -694,7 +709,8 @@ void p2m_destroy(p2m_ctx *ctx) {
                   ctx->d_nring, ctx->d_ioff, ctx->d_fs_items, ctx->d_scan_tmp, ctx->d_counts,
                   ctx->d_pix_off, ctx->d_nitems, ctx->d_sums, ctx->d_set_rec, ctx->d_set_pix,
                   ctx->d_ctr, ctx->d_prep, ctx->d_lo, ctx->d_tiles,
-                  ctx->d_pre_flags, ctx->d_pre_bits, ctx->d_pre_ord, ctx->d_pre_last};
+                  ctx->d_pre_flags, ctx->d_pre_bits, ctx->d_pre_ord, ctx->d_pre_last,
+                  ctx->d_cone_off};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   for (int m = 0; m < P2M_MAXMAPS; m++)
@@ -791,6 +807,8 @@ p2m_status p2m_set_preprocess(p2m_ctx *ctx, int32_t scramble, int32_t centre, in
     return fail(ctx, P2M_ERR_BADARG, "scramble and centre must be 0 or 1, ntasks 1..25");
   if (ctx->dirty || ctx->rec_count > 0 || !ctx->prep.empty())
     return fail(ctx, P2M_ERR_STATE, "set the pre-processing right after p2m_reset_maps");
+  if ((scramble || centre) && ctx->ncones > 1)
+    return fail(ctx, P2M_ERR_BADARG, "scramble and centre act on one catalogue, not an ensemble");
   ctx->pre.scramble = scramble;
   ctx->pre.centre = centre;
   ctx->pre.ntasks = ntasks;
@@ -821,6 +839,84 @@ p2m_status p2m_paint_records_device(p2m_ctx *ctx, const float *d_records, int64_
   CK(cudaSetDevice(ctx->cfg.device));
   cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
   return ingest_device(ctx, d_records, nrec, nfloat, s);
+}
+
+namespace {
+
+p2m_status check_offsets(p2m_ctx *ctx, const int64_t *offsets, int32_t ncones) {
+  if (!offsets) return fail(ctx, P2M_ERR_BADARG, "null cone offsets");
+  if (ncones < 1 || ncones > ctx->ncones)
+    return fail(ctx, P2M_ERR_BADARG, "cone count outside 1.." + std::to_string(ctx->ncones));
+  if (offsets[0] != 0) return fail(ctx, P2M_ERR_BADARG, "offsets[0] must be 0");
+  for (int c = 0; c < ncones; c++)
+    if (offsets[c + 1] < offsets[c]) return fail(ctx, P2M_ERR_BADARG, "offsets must not decrease");
+  if (ctx->pre.scramble || ctx->pre.centre)
+    return fail(ctx, P2M_ERR_STATE, "scramble and centre act on one catalogue, not an ensemble");
+  return P2M_OK;
+}
+
+/* the cones' first records relative to call-local record `off`, clamped to [0, n] */
+p2m_status upload_offsets(p2m_ctx *ctx, const int64_t *offsets, int32_t ncones, long long off,
+                          long long n, cudaStream_t s) {
+  ctx->cone_off_host.resize((size_t)ncones + 1);
+  for (int c = 0; c <= ncones; c++)
+    ctx->cone_off_host[(size_t)c] = std::min(std::max((long long)offsets[c] - off, 0LL), n);
+  CK(cudaMemcpyAsync(ctx->d_cone_off, ctx->cone_off_host.data(),
+                     sizeof(long long) * ((size_t)ncones + 1), cudaMemcpyHostToDevice, s));
+  /* the host copy is reused by the next call: let this one finish reading it */
+  CK(cudaStreamSynchronize(s));
+  return P2M_OK;
+}
+
+}  // namespace
+
+p2m_status p2m_paint_ensemble(p2m_ctx *ctx, const float *records, const int64_t *offsets,
+                              int32_t ncones, int32_t nfloat) {
+  if (!ctx) return P2M_ERR_BADARG;
+  if (ctx->ncones < 2) return fail(ctx, P2M_ERR_STATE, "the context was not created for an ensemble");
+  ST(check_offsets(ctx, offsets, ncones));
+  const long long nrec = offsets[ncones];
+  if (nrec > 0 && !records) return fail(ctx, P2M_ERR_BADARG, "null records");
+  if (nfloat != 7 && nfloat != 10) return fail(ctx, P2M_ERR_BADARG, "nfloat must be 7 or 10");
+  CK(cudaSetDevice(ctx->cfg.device));
+  long long chunk = std::max<long long>(ctx->cfg.max_records, 1024);
+  for (long long off = 0; off < nrec; off += chunk) {
+    long long n = std::min(chunk, nrec - off);
+    long long need = n * nfloat;
+    CK(grow(&ctx->d_records, &ctx->cap_rec_floats, need));
+    CK(cudaMemcpyAsync(ctx->d_records, records + off * nfloat, sizeof(float) * (size_t)need,
+                       cudaMemcpyHostToDevice, ctx->stream));
+    ST(upload_offsets(ctx, offsets, ncones, off, n, ctx->stream));
+    ST(ingest_device(ctx, ctx->d_records, n, nfloat, ctx->stream, ncones));
+  }
+  return P2M_OK;
+}
+
+p2m_status p2m_paint_ensemble_device(p2m_ctx *ctx, const float *d_records,
+                                     const int64_t *offsets, int32_t ncones, int32_t nfloat,
+                                     void *stream) {
+  if (!ctx) return P2M_ERR_BADARG;
+  if (ctx->ncones < 2) return fail(ctx, P2M_ERR_STATE, "the context was not created for an ensemble");
+  ST(check_offsets(ctx, offsets, ncones));
+  const long long nrec = offsets[ncones];
+  if (nrec > 0 && !d_records) return fail(ctx, P2M_ERR_BADARG, "null records");
+  CK(cudaSetDevice(ctx->cfg.device));
+  cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
+  ST(upload_offsets(ctx, offsets, ncones, 0, nrec, s));
+  return ingest_device(ctx, d_records, nrec, nfloat, s, ncones);
+}
+
+p2m_status p2m_get_healpix_cone(p2m_ctx *ctx, int32_t cone, int32_t map, float *out) {
+  if (!ctx || !out) return P2M_ERR_BADARG;
+  if (map < 0 || map >= ctx->cfg.nmaps || ctx->cfg.nside <= 0)
+    return fail(ctx, P2M_ERR_BADARG, "map index out of range");
+  if (cone < 0 || cone >= ctx->ncones) return fail(ctx, P2M_ERR_BADARG, "cone index out of range");
+  CK(cudaSetDevice(ctx->cfg.device));
+  ST(sweep(ctx, ctx->stream));
+  CK(cudaMemcpyAsync(out, ctx->d_out[map] + (size_t)cone * (size_t)ctx->cone_npix,
+                     sizeof(float) * (size_t)ctx->cone_npix, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return P2M_OK;
 }
 
 p2m_status p2m_project_halo(p2m_ctx *ctx, float *x, float *y, float *z, const float *r,

@@ -59,6 +59,8 @@ struct HaloRec {
   float chi_t, fc, fm;    /* per-halo part of interpolate_table */
   int ichi, imh, zero;
   float w1, w2;           /* deposit weights of profile-1 and profile-2 maps */
+  int cone;               /* light-cone of an ensemble: the maps' slot offset is
+                             cone * 12 nside^2 (0 outside ensembles) */
   long long rec;          /* record index (over all paint calls since the reset) */
   int ir_lo, ir_hi;       /* candidate rings */
   int cbase[4];           /* table offsets of corners (imh,ichi),(imh+1,ichi),(imh,ichi+1),
@@ -68,6 +70,8 @@ struct HaloRec {
 };
 
 /* candidate span of one ring of one disc */
+static_assert(sizeof(HaloRec) == 144, "HaloRec layout");
+
 struct RingItem {
   int halo;
   int ring_n0;               /* ring << 16 | (n0 & 0xffff) */
@@ -108,12 +112,15 @@ struct PaintParams {
   const float4 *phitab;  /* (cos hi, cos lo, sin hi, sin lo) of 2 pi k / P2M_PHITAB */
   p2m_pre pre;           /* scramble / centre of the catalogue (pks2map.f90:162-262) */
   const long long *pre_ord; /* with pre: radial-cut survivors before each record */
+  long long cone_npix;   /* HEALPix pixels of one cone's map (12 nside^2) */
 };
 
 /* buffers of one ingest call */
 struct IngestBuffers {
   const float *records;
   long long rec_base;   /* record index of records[0] */
+  const long long *cone_off; /* ensemble: first record of each cone (call-local), ncones + 1 */
+  int ncones;           /* 0: every record belongs to cone 0 */
   HaloRec *halos;       /* halos[0..n_surv) of this call */
   long long halo_base;  /* global index of halos[0] */
   unsigned int *nring;  /* rings per large halo, 0 for the others */

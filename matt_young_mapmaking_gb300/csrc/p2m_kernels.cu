@@ -311,6 +311,18 @@ __device__ __forceinline__ void store_halo(const PaintParams &P, const IngestBuf
   if (H.jmin <= H.jmax && H.kmin <= H.kmax) fsrows += (unsigned long long)(H.kmax - H.kmin + 1);
 }
 
+/* light-cone of call-local record i: the last cone whose first record is <= i */
+__device__ __forceinline__ int cone_of(const IngestBuffers &B, long long i) {
+  if (B.ncones <= 1) return 0;
+  int lo = 0, hi = B.ncones - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (B.cone_off[mid] <= i) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
 /* per-halo set-up of record i as halo s (pks2map.f90:264, :284-298) */
 __device__ __forceinline__ void setup_record(const PaintParams &P, const IngestBuffers &B,
                                              long long s, int i, unsigned long long &fsrows) {
@@ -331,6 +343,7 @@ __device__ __forceinline__ void setup_record(const PaintParams &P, const IngestB
                         0.333333343f);
     HaloRec H;
     H.rec = B.rec_base + i;
+    H.cone = cone_of(B, i);
     H.w1 = 1.0f;
     H.w2 = 1.0f;
     if (P.any_ksz) {
@@ -431,6 +444,7 @@ __global__ void __launch_bounds__(256) k_setup_prepared(PaintParams P, IngestBuf
     int prof = (int)q[8];
     HaloRec H;
     H.rec = B.rec_base + s;
+    H.cone = 0;
     H.w1 = prof == 1 ? q[7] : 0.0f;
     H.w2 = prof == 2 ? q[7] : 0.0f;
     halo_geometry(P, q[0], q[1], q[2], q[3], q[4], q[5], q[6], H, &B.ctr->err);
@@ -673,9 +687,12 @@ __global__ void __launch_bounds__(256) k_fs_emit(PaintParams P, IngestBuffers B)
 /* the halo fields one candidate pixel needs */
 struct HotHalo {
   float C_in, C_out, chi_t, fc, fm, w1, w2;
-  int zero, ichi, imh;
+  int zc; /* bit 0: the table value is identically zero; bits 1..: the light-cone */
+  int ichi, imh;
   int cb[4];
 };
+__device__ __forceinline__ bool hot_zero(const HotHalo &h) { return h.zc & 1; }
+__device__ __forceinline__ int hot_cone(const HotHalo &h) { return h.zc >> 1; }
 
 __device__ __forceinline__ HotHalo hot_of(const HaloRec &H) {
   HotHalo h;
@@ -686,7 +703,7 @@ __device__ __forceinline__ HotHalo hot_of(const HaloRec &H) {
   h.fm = H.fm;
   h.w1 = H.w1;
   h.w2 = H.w2;
-  h.zero = H.zero;
+  h.zc = (H.zero ? 1 : 0) | (H.cone << 1);
   h.ichi = H.ichi;
   h.imh = H.imh;
   for (int c = 0; c < 4; c++) h.cb[c] = H.cbase[c];
@@ -787,7 +804,7 @@ __device__ __forceinline__ void deposit_maps(const PaintParams &P, const HotHalo
       hi.fm = H.fm;
       hi.ichi = H.ichi;
       hi.imh = H.imh;
-      hi.zero = H.zero;
+      hi.zero = hot_zero(H);
       v = p2m_blend8(tab, &P.th, &hi, prof, ir, fr);
     }
     vals[m] = FMUL(w, v);
@@ -1044,7 +1061,7 @@ __device__ __forceinline__ void paint_pixel(const PaintParams &P, const SweepBuf
                                             unsigned int &nrc, PendingDeposit *pend = nullptr) {
   int ir = 0;
   float fr = 0.0f, u = 0.0f;
-  bool zero_val = H.zero;
+  bool zero_val = hot_zero(H);
   int d;
   if (EXACT) {
     d = 2;
@@ -1074,22 +1091,24 @@ __device__ __forceinline__ void paint_pixel(const PaintParams &P, const SweepBuf
   nupd++;
   if (P.flags & 1)
     record_set(W.set_rec, W.set_pix, W.set_cap, &W.ctr->n_sets, W.halos[it.halo].rec, pix);
-  if (zero_val || H.zero) return;
+  if (zero_val || hot_zero(H)) return;
+  /* the halo's cone selects its copy of the maps (always 0 outside ensembles) */
+  const long long slot = pix + (long long)hot_cone(H) * P.cone_npix;
   if (EXACT) {
-    deposit_maps<ACC>(P, H, W.acc, pix, ir, fr, &W);
+    deposit_maps<ACC>(P, H, W.acc, slot, ir, fr, &W);
   } else if (ACC == 2 && pend) {
     float v0, v1;
     if (paired_values(P, H, ir, fr, v0, v1)) {
-      pend->slot = pix;
+      pend->slot = slot;
       pend->v0 = v0;
       pend->v1 = v1;
-      pend->o0 = v0 != 0.0f ? atomicAdd(W.out[0] + pix, v0) : 0.0f;
-      pend->o1 = v1 != 0.0f ? atomicAdd(W.out[1] + pix, v1) : 0.0f;
+      pend->o0 = v0 != 0.0f ? atomicAdd(W.out[0] + slot, v0) : 0.0f;
+      pend->o1 = v1 != 0.0f ? atomicAdd(W.out[1] + slot, v1) : 0.0f;
     } else {
-      deposit_mixed<ACC>(P, H, pix, ir, fr, &W);
+      deposit_mixed<ACC>(P, H, slot, ir, fr, &W);
     }
   } else {
-    deposit_mixed<ACC>(P, H, pix, ir, fr, &W);
+    deposit_mixed<ACC>(P, H, slot, ir, fr, &W);
   }
 }
 
