@@ -52,6 +52,29 @@ int32_t p2m_get_timings(struct p2m_ctx *ctx, double *ms, int32_t n);
 int32_t p2m_map_sums_noalloc(const float *const *d_maps, int32_t nmaps, int64_t npix,
                              double *sums, void *stream);
 
+/* Launch parameters of the sweep, chosen by p2m_autotune or set directly.  No counterpart
+   in the reference, whose halo loop has no launch parameters.  The defaults are the first
+   row of each field's range below; results do not depend on them (pixel sets are
+   identical, map values equal up to the order of the additions). */
+typedef struct p2m_tuning {
+  int32_t big_rings;  /* halos spanning more rings are painted from stored (halo, ring) items
+                         by the candidate-balanced kernel (0: every halo), 0..4096; 64 */
+  int32_t halos_grid; /* blocks per SM of the fused enumerate-and-paint kernel, 1..16; 8 */
+  int32_t full_grid;  /* blocks per SM of the stored-item kernel, 1..32; 8 */
+  int32_t full_chunk; /* candidates per warp chunk of the stored-item kernel, 32..65536; 1024 */
+  float ms;           /* p2m_autotune: device time of one paint call with the choice */
+} p2m_tuning;
+int32_t p2m_get_tuning(struct p2m_ctx *ctx, p2m_tuning *out);
+int32_t p2m_set_tuning(struct p2m_ctx *ctx, const p2m_tuning *t);
+/* Autotuner: paints the caller's catalogue (device records, as p2m_paint_records_device)
+   with candidate launch parameters and keeps the fastest.  The search is coordinate
+   descent: big_rings, then the fused kernel's grid, then the stored-item kernel's grid,
+   then its chunk.  Each candidate is timed by device events around the whole paint call
+   (reset, ingest, sweep), best of `reps`.  The maps are reset before the first and after
+   the last candidate.  Writes the choice to *out when out is not NULL. */
+int32_t p2m_autotune(struct p2m_ctx *ctx, const float *d_records, int64_t nrec, int32_t nfloat,
+                     int32_t reps, p2m_tuning *out);
+
 /* With center: RTHmax, then the distance and x, y, z of the largest halo before and after
    the rotation (the report of pks2map.f90:205-209, :250-254); zeros otherwise. */
 int32_t p2m_get_centre(struct p2m_ctx *ctx, float *out9);

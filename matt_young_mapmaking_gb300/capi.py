@@ -50,6 +50,12 @@ class P2MConfig(ctypes.Structure):
     ]
 
 
+class P2MTuning(ctypes.Structure):
+    _fields_ = [("big_rings", ctypes.c_int32), ("halos_grid", ctypes.c_int32),
+                ("full_grid", ctypes.c_int32), ("full_chunk", ctypes.c_int32),
+                ("ms", ctypes.c_float)]
+
+
 class P2MStats(ctypes.Structure):
     _fields_ = [
         ("n_records", ctypes.c_int64),
@@ -119,6 +125,9 @@ def load_library():
         "p2m_paint_ensemble": (I32, [VP, VP, VP, I32, I32]),
         "p2m_paint_ensemble_device": (I32, [VP, VP, VP, I32, I32, VP]),
         "p2m_get_healpix_cone": (I32, [VP, I32, I32, VP]),
+        "p2m_get_tuning": (I32, [VP, ctypes.POINTER(P2MTuning)]),
+        "p2m_set_tuning": (I32, [VP, ctypes.POINTER(P2MTuning)]),
+        "p2m_autotune": (I32, [VP, VP, I64, I32, I32, ctypes.POINTER(P2MTuning)]),
         "p2m_cl_flatsky": (I32, [I32, VP, VP, I32, F, D, I32, VP, VP, VP, VP, VP]),
     }
     for name, (res, args) in sig.items():
@@ -140,7 +149,8 @@ def exported_symbols():
             "p2m_get_timings", "p2m_map_sums_noalloc", "p2m_set_preprocess", "p2m_get_centre",
             "p2m_dpdy", "p2m_write_dpdy",
             "p2m_write_flatsky", "p2m_write_healpix_fits", "p2m_cl_healpix", "p2m_cl_flatsky",
-            "p2m_paint_ensemble", "p2m_paint_ensemble_device", "p2m_get_healpix_cone"]
+            "p2m_paint_ensemble", "p2m_paint_ensemble_device", "p2m_get_healpix_cone",
+            "p2m_get_tuning", "p2m_set_tuning", "p2m_autotune"]
 
 
 PHASES = ["cut", "setup", "big_scan", "big_items", "flatsky", "big_offsets", "paint", "paint_big",
@@ -264,6 +274,26 @@ class Painter:
         self._check(self._lib.p2m_paint_ensemble_device(self._h, ctypes.c_void_p(dptr), _ptr(off),
                                                         off.size - 1, nfloat,
                                                         ctypes.c_void_p(stream or 0)))
+
+    # -- launch parameters ---------------------------------------------------------
+    def tuning(self):
+        t = P2MTuning()
+        self._check(self._lib.p2m_get_tuning(self._h, ctypes.byref(t)))
+        return {k: getattr(t, k) for k, _ in P2MTuning._fields_}
+
+    def set_tuning(self, **kw):
+        t = P2MTuning(**{k: v for k, v in self.tuning().items()})
+        for k, v in kw.items():
+            setattr(t, k, v)
+        self._check(self._lib.p2m_set_tuning(self._h, ctypes.byref(t)))
+
+    def autotune(self, dptr, n, nfloat=10, reps=3):
+        """Times candidate launch parameters on device records and keeps the fastest
+        (include/p2m_tools.h p2m_autotune); returns the choice."""
+        t = P2MTuning()
+        self._check(self._lib.p2m_autotune(self._h, ctypes.c_void_p(dptr), n, nfloat, reps,
+                                           ctypes.byref(t)))
+        return {k: getattr(t, k) for k, _ in P2MTuning._fields_}
 
     def healpix_cone(self, cone, m=0):
         out = np.empty(12 * self.nside * self.nside, dtype=np.float32)

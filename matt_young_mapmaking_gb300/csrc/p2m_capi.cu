@@ -44,7 +44,7 @@ struct p2m_ctx {
   bool th_set = false;
   float *d_tab[P2M_MAXTABLES] = {};
   float band_u = 2e-4f;
-  int big_rings = P2M_BIG_RINGS;
+  p2m_tuning tune = {P2M_BIG_RINGS, 8, 8, 1024, 0.0f}; /* launch parameters of the sweep */
   /* outputs: hp_npix counts every cone's pixels (ncones * cone_npix) */
   long long hp_npix = 0, fs_npix = 0;
   long long cone_npix = 0;
@@ -211,7 +211,10 @@ PaintParams make_params(const p2m_ctx *ctx, int nfloat) {
   P.pre_ord = ctx->d_pre_ord;
   P.band_u = ctx->band_u;
   P.inv_drt = ctx->th_set ? 1.0f / ctx->th.drt : 0.0f;
-  P.big_rings = ctx->big_rings;
+  P.big_rings = ctx->tune.big_rings;
+  P.halos_grid = ctx->tune.halos_grid;
+  P.full_grid = ctx->tune.full_grid;
+  P.full_chunk = ctx->tune.full_chunk;
   P.cone_npix = ctx->cone_npix;
   if (ctx->th_set) {
     float fr;
@@ -612,8 +615,8 @@ p2m_status p2m_create(const p2m_config *cfg, p2m_ctx **out) {
   /* the plain FP64 path is fastest with every halo on the stored-item path, which balances
      its heavy per-candidate work over candidates; test hook: P2M_BIG_RINGS routes every
      halo through one painting path (0: stored items only) */
-  if (cfg->precision == P2M_PREC_FP64) ctx->big_rings = 0;
-  if (const char *e = getenv("P2M_BIG_RINGS")) ctx->big_rings = std::max(0, atoi(e));
+  if (cfg->precision == P2M_PREC_FP64) ctx->tune.big_rings = 0;
+  if (const char *e = getenv("P2M_BIG_RINGS")) ctx->tune.big_rings = std::max(0, atoi(e));
   CK(cudaSetDevice(cfg->device));
   CK(cudaDeviceGetAttribute(&ctx->nsm, cudaDevAttrMultiProcessorCount, cfg->device));
   CK(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
@@ -904,6 +907,92 @@ p2m_status p2m_paint_ensemble_device(p2m_ctx *ctx, const float *d_records,
   cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
   ST(upload_offsets(ctx, offsets, ncones, 0, nrec, s));
   return ingest_device(ctx, d_records, nrec, nfloat, s, ncones);
+}
+
+namespace {
+
+bool tuning_ok(const p2m_tuning &t) {
+  return t.big_rings >= 0 && t.big_rings <= 4096 && t.halos_grid >= 1 && t.halos_grid <= 16 &&
+         t.full_grid >= 1 && t.full_grid <= 32 && t.full_chunk >= 32 && t.full_chunk <= 65536;
+}
+
+struct EventPair {
+  cudaEvent_t a = nullptr, b = nullptr;
+  ~EventPair() {
+    if (a) cudaEventDestroy(a);
+    if (b) cudaEventDestroy(b);
+  }
+};
+
+}  // namespace
+
+int32_t p2m_get_tuning(p2m_ctx *ctx, p2m_tuning *out) {
+  if (!ctx || !out) return P2M_ERR_BADARG;
+  *out = ctx->tune;
+  return P2M_OK;
+}
+
+int32_t p2m_set_tuning(p2m_ctx *ctx, const p2m_tuning *t) {
+  if (!ctx || !t) return P2M_ERR_BADARG;
+  if (!tuning_ok(*t)) return fail(ctx, P2M_ERR_BADARG, "tuning parameter out of range");
+  if (ctx->dirty || !ctx->prep.empty())
+    return fail(ctx, P2M_ERR_STATE, "change the tuning before painting or after a read-out");
+  ctx->tune = *t;
+  return P2M_OK;
+}
+
+int32_t p2m_autotune(p2m_ctx *ctx, const float *d_records, int64_t nrec, int32_t nfloat,
+                     int32_t reps, p2m_tuning *out) {
+  if (!ctx) return P2M_ERR_BADARG;
+  if (!d_records || nrec < 1 || reps < 1 || reps > 100)
+    return fail(ctx, P2M_ERR_BADARG, "autotune needs device records and 1..100 repetitions");
+  CK(cudaSetDevice(ctx->cfg.device));
+  EventPair ev;
+  CK(cudaEventCreate(&ev.a));
+  CK(cudaEventCreate(&ev.b));
+  /* device time of one whole paint call with tuning t, best of reps */
+  auto trial = [&](const p2m_tuning &t, float *ms) -> p2m_status {
+    ctx->tune = t;
+    float best = 3.0e38f;
+    for (int r = 0; r < reps; r++) {
+      ST(p2m_reset_maps(ctx));
+      CK(cudaEventRecord(ev.a, ctx->stream));
+      ST(ingest_device(ctx, d_records, nrec, nfloat, ctx->stream));
+      ST(sweep(ctx, ctx->stream));
+      CK(cudaEventRecord(ev.b, ctx->stream));
+      CK(cudaEventSynchronize(ev.b));
+      float e = 0.0f;
+      CK(cudaEventElapsedTime(&e, ev.a, ev.b));
+      best = std::min(best, e);
+    }
+    *ms = best;
+    return P2M_OK;
+  };
+  static const int kBig[] = {0, 16, 32, 48, 64, 96, 128, 256};
+  static const int kHalos[] = {1, 2, 3, 4, 8};
+  static const int kFull[] = {2, 4, 8, 16};
+  static const int kChunk[] = {256, 512, 1024, 2048, 4096};
+  p2m_tuning best = ctx->tune;
+  ST(trial(best, &best.ms));
+  auto descend = [&](const int *vals, int n, int32_t p2m_tuning::*field) -> p2m_status {
+    for (int i = 0; i < n; i++) {
+      if (best.*field == vals[i]) continue;
+      p2m_tuning t = best;
+      t.*field = vals[i];
+      ST(trial(t, &t.ms));
+      if (t.ms < best.ms) best = t;
+    }
+    return P2M_OK;
+  };
+  p2m_status st = descend(kBig, 8, &p2m_tuning::big_rings);
+  if (!st) st = descend(kHalos, 5, &p2m_tuning::halos_grid);
+  if (!st) st = descend(kFull, 4, &p2m_tuning::full_grid);
+  if (!st) st = descend(kChunk, 5, &p2m_tuning::full_chunk);
+  ctx->tune = best;
+  if (st) return st;
+  ST(p2m_reset_maps(ctx));
+  if (out) *out = best;
+  return P2M_OK;
 }
 
 p2m_status p2m_get_healpix_cone(p2m_ctx *ctx, int32_t cone, int32_t map, float *out) {

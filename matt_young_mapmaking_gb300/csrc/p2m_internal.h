@@ -113,6 +113,9 @@ struct PaintParams {
   p2m_pre pre;           /* scramble / centre of the catalogue (pks2map.f90:162-262) */
   const long long *pre_ord; /* with pre: radial-cut survivors before each record */
   long long cone_npix;   /* HEALPix pixels of one cone's map (12 nside^2) */
+  int halos_grid;        /* blocks per SM of k_paint_halos */
+  int full_grid;         /* blocks per SM of k_paint_full */
+  int full_chunk;        /* candidates per warp chunk of k_paint_full */
 };
 
 /* buffers of one ingest call */

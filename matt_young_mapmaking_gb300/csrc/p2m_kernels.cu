@@ -1199,7 +1199,7 @@ __global__ void __launch_bounds__(256) k_paint_full(PaintParams P, SweepBuffers 
   if (npix_c == 0) return;
   const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
-  const long long chunk = 1024;
+  const long long chunk = P.full_chunk;
   CacheEnt *cache = s_cache[(threadIdx.x >> 5) & 7];
   unsigned int nupd = 0, nrc = 0;
   unsigned long long ncand = 0;
@@ -1757,9 +1757,10 @@ void p2m_launch_fs(const PaintParams &P, const IngestBuffers &B, long long n_max
   else k_paint_fs<0><<<nsm * 8, 256, 0, s>>>(P, B);
 }
 void p2m_launch_paint_full(const PaintParams &P, const SweepBuffers &W, cudaStream_t s, int nsm) {
-  if (P.precision == 0) k_paint_full<1, 0><<<nsm * 8, 256, 0, s>>>(P, W);
-  else if (P.precision == 1) k_paint_full<0, 2><<<nsm * 8, 256, 0, s>>>(P, W);
-  else k_paint_full<0, 0><<<nsm * 8, 256, 0, s>>>(P, W);
+  const int g = nsm * P.full_grid;
+  if (P.precision == 0) k_paint_full<1, 0><<<g, 256, 0, s>>>(P, W);
+  else if (P.precision == 1) k_paint_full<0, 2><<<g, 256, 0, s>>>(P, W);
+  else k_paint_full<0, 0><<<g, 256, 0, s>>>(P, W);
 }
 template <int EXACT, int ACC>
 static void launch_paint_halos(const PaintParams &P, const SweepBuffers &W, cudaStream_t s,
@@ -1772,7 +1773,7 @@ static void launch_paint_halos(const PaintParams &P, const SweepBuffers &W, cuda
     carveout = true;
   }
   /* warps claim 32-halo batches until none is left */
-  k_paint_halos<EXACT, ACC><<<nsm * 8, 256, 0, s>>>(P, W);
+  k_paint_halos<EXACT, ACC><<<nsm * P.halos_grid, 256, 0, s>>>(P, W);
 }
 void p2m_launch_paint_halos(const PaintParams &P, const SweepBuffers &W, cudaStream_t s, int nsm) {
   if (P.precision == 0) launch_paint_halos<1, 0>(P, W, s, nsm);
