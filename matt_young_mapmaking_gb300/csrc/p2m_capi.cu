@@ -69,8 +69,12 @@ struct p2m_ctx {
   long long rec_count = 0;
   bool dirty = false, swept = false;
   /* per-call buffers */
-  float *d_records = nullptr;
-  long long cap_rec_floats = 0;
+  /* streamed ingest of host records: two device staging buffers filled on a copy stream
+     while the previous chunk is cut and set up */
+  cudaStream_t cstream = nullptr;
+  float *d_stage[2] = {nullptr, nullptr};
+  long long cap_stage[2] = {0, 0};
+  cudaEvent_t ev_copied[2] = {nullptr, nullptr}, ev_consumed[2] = {nullptr, nullptr};
   unsigned int *d_nring = nullptr;
   long long cap_nring = 0;
   long long *d_ioff = nullptr;
@@ -708,12 +712,12 @@ void p2m_destroy(p2m_ctx *ctx) {
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   if (ctx->zstream) cudaStreamSynchronize(ctx->zstream);
   void *ptrs[] = {ctx->d_rofz, ctx->d_zofr, ctx->d_ringtab, ctx->d_phitab, ctx->d_acc64, ctx->d_fs_acc,
-                  ctx->d_fs_out, ctx->d_halos, ctx->d_items_raw, ctx->d_records,
+                  ctx->d_fs_out, ctx->d_halos, ctx->d_items_raw,
                   ctx->d_nring, ctx->d_ioff, ctx->d_fs_items, ctx->d_scan_tmp, ctx->d_counts,
                   ctx->d_pix_off, ctx->d_nitems, ctx->d_sums, ctx->d_set_rec, ctx->d_set_pix,
                   ctx->d_ctr, ctx->d_prep, ctx->d_lo, ctx->d_tiles,
                   ctx->d_pre_flags, ctx->d_pre_bits, ctx->d_pre_ord, ctx->d_pre_last,
-                  ctx->d_cone_off};
+                  ctx->d_cone_off, ctx->d_stage[0], ctx->d_stage[1]};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   for (int m = 0; m < P2M_MAXMAPS; m++)
@@ -726,6 +730,14 @@ void p2m_destroy(p2m_ctx *ctx) {
   if (ctx->ev_zero_start) cudaEventDestroy(ctx->ev_zero_start);
   if (ctx->ev_zero_done) cudaEventDestroy(ctx->ev_zero_done);
   if (ctx->zstream) cudaStreamDestroy(ctx->zstream);
+  if (ctx->cstream) {
+    cudaStreamSynchronize(ctx->cstream);
+    cudaStreamDestroy(ctx->cstream);
+  }
+  for (int b = 0; b < 2; b++) {
+    if (ctx->ev_copied[b]) cudaEventDestroy(ctx->ev_copied[b]);
+    if (ctx->ev_consumed[b]) cudaEventDestroy(ctx->ev_consumed[b]);
+  }
   for (int k = 0; k < P2M_NPHASE; k++)
     for (int e = 0; e < 2; e++)
       if (ctx->tev[k][e]) cudaEventDestroy(ctx->tev[k][e]);
@@ -818,21 +830,72 @@ p2m_status p2m_set_preprocess(p2m_ctx *ctx, int32_t scramble, int32_t centre, in
   return P2M_OK;
 }
 
+p2m_status upload_offsets(p2m_ctx *ctx, const int64_t *offsets, int32_t ncones, long long off,
+                          long long n, cudaStream_t s);
+
+/* Host records in chunks of at most P2M_STREAM_CHUNK (and max_records): chunk k + 1 is
+   copied on the copy stream into one of two device staging buffers while chunk k is cut
+   and set up on the context's stream.  A buffer is refilled only after the chunk that
+   used it has been ingested (the cut and set-up kernel is its only reader).  From pinned
+   host memory the copies overlap the ingest; from pageable memory the driver stages each
+   copy first.  Scramble and centre need the whole catalogue in one piece: they take a
+   single chunk.  With cone offsets (ensembles) each chunk gets its own clamped table. */
+p2m_status stream_host_records(p2m_ctx *ctx, const float *records, long long nrec, int nfloat,
+                               const int64_t *offsets, int ncones) {
+  const bool pre = ctx->pre.scramble || ctx->pre.centre;
+  long long chunk = std::max<long long>(ctx->cfg.max_records, 1024);
+  if (!pre) chunk = std::min<long long>(chunk, P2M_STREAM_CHUNK);
+  if (nrec <= 0) return P2M_OK;
+  const long long nchunk = (nrec + chunk - 1) / chunk;
+  if (!ctx->cstream) {
+    CK(cudaStreamCreateWithFlags(&ctx->cstream, cudaStreamNonBlocking));
+    for (int b = 0; b < 2; b++) {
+      CK(cudaEventCreateWithFlags(&ctx->ev_copied[b], cudaEventDisableTiming));
+      CK(cudaEventCreateWithFlags(&ctx->ev_consumed[b], cudaEventDisableTiming));
+      /* no chunk has used the buffer yet */
+      CK(cudaEventRecord(ctx->ev_consumed[b], ctx->stream));
+    }
+  }
+  const long long per = std::min(chunk, nrec) * nfloat;
+  for (int b = 0; b < (nchunk > 1 ? 2 : 1); b++) {
+    if (ctx->cap_stage[b] < per) {
+      /* nothing may still read the old buffer */
+      CK(cudaEventSynchronize(ctx->ev_consumed[b]));
+      CK(grow(&ctx->d_stage[b], &ctx->cap_stage[b], per));
+    }
+  }
+  auto issue = [&](long long k) -> p2m_status {
+    const int b = (int)(k & 1);
+    const long long off = k * chunk, n = std::min(chunk, nrec - off);
+    CK(cudaStreamWaitEvent(ctx->cstream, ctx->ev_consumed[b], 0));
+    CK(cudaMemcpyAsync(ctx->d_stage[b], records + off * nfloat, sizeof(float) * (size_t)(n * nfloat),
+                       cudaMemcpyHostToDevice, ctx->cstream));
+    CK(cudaEventRecord(ctx->ev_copied[b], ctx->cstream));
+    return P2M_OK;
+  };
+  ST(issue(0));
+  for (long long k = 0; k < nchunk; k++) {
+    if (k + 1 < nchunk) ST(issue(k + 1));
+    const int b = (int)(k & 1);
+    const long long off = k * chunk, n = std::min(chunk, nrec - off);
+    CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_copied[b], 0));
+    if (offsets) ST(upload_offsets(ctx, offsets, ncones, off, n, ctx->stream));
+    p2m_status st = ingest_device(ctx, ctx->d_stage[b], n, nfloat, ctx->stream, offsets ? ncones : 0);
+    CK(cudaEventRecord(ctx->ev_consumed[b], ctx->stream));
+    if (st) {
+      cudaStreamSynchronize(ctx->cstream);
+      return st;
+    }
+  }
+  return P2M_OK;
+}
+
 p2m_status p2m_paint_records(p2m_ctx *ctx, const float *records, int64_t nrec, int32_t nfloat) {
   if (!ctx) return P2M_ERR_BADARG;
   if (nrec > 0 && !records) return fail(ctx, P2M_ERR_BADARG, "null records");
   CK(cudaSetDevice(ctx->cfg.device));
   if (nfloat != 7 && nfloat != 10) return fail(ctx, P2M_ERR_BADARG, "nfloat must be 7 or 10");
-  long long chunk = std::max<long long>(ctx->cfg.max_records, 1024);
-  for (long long off = 0; off < nrec; off += chunk) {
-    long long n = std::min(chunk, nrec - off);
-    long long need = n * nfloat;
-    CK(grow(&ctx->d_records, &ctx->cap_rec_floats, need));
-    CK(cudaMemcpyAsync(ctx->d_records, records + off * nfloat, sizeof(float) * (size_t)need,
-                       cudaMemcpyHostToDevice, ctx->stream));
-    ST(ingest_device(ctx, ctx->d_records, n, nfloat, ctx->stream));
-  }
-  return P2M_OK;
+  return stream_host_records(ctx, records, nrec, nfloat, nullptr, 0);
 }
 
 p2m_status p2m_paint_records_device(p2m_ctx *ctx, const float *d_records, int64_t nrec,
@@ -843,8 +906,6 @@ p2m_status p2m_paint_records_device(p2m_ctx *ctx, const float *d_records, int64_
   cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
   return ingest_device(ctx, d_records, nrec, nfloat, s);
 }
-
-namespace {
 
 p2m_status check_offsets(p2m_ctx *ctx, const int64_t *offsets, int32_t ncones) {
   if (!offsets) return fail(ctx, P2M_ERR_BADARG, "null cone offsets");
@@ -871,8 +932,6 @@ p2m_status upload_offsets(p2m_ctx *ctx, const int64_t *offsets, int32_t ncones, 
   return P2M_OK;
 }
 
-}  // namespace
-
 p2m_status p2m_paint_ensemble(p2m_ctx *ctx, const float *records, const int64_t *offsets,
                               int32_t ncones, int32_t nfloat) {
   if (!ctx) return P2M_ERR_BADARG;
@@ -882,17 +941,7 @@ p2m_status p2m_paint_ensemble(p2m_ctx *ctx, const float *records, const int64_t 
   if (nrec > 0 && !records) return fail(ctx, P2M_ERR_BADARG, "null records");
   if (nfloat != 7 && nfloat != 10) return fail(ctx, P2M_ERR_BADARG, "nfloat must be 7 or 10");
   CK(cudaSetDevice(ctx->cfg.device));
-  long long chunk = std::max<long long>(ctx->cfg.max_records, 1024);
-  for (long long off = 0; off < nrec; off += chunk) {
-    long long n = std::min(chunk, nrec - off);
-    long long need = n * nfloat;
-    CK(grow(&ctx->d_records, &ctx->cap_rec_floats, need));
-    CK(cudaMemcpyAsync(ctx->d_records, records + off * nfloat, sizeof(float) * (size_t)need,
-                       cudaMemcpyHostToDevice, ctx->stream));
-    ST(upload_offsets(ctx, offsets, ncones, off, n, ctx->stream));
-    ST(ingest_device(ctx, ctx->d_records, n, nfloat, ctx->stream, ncones));
-  }
-  return P2M_OK;
+  return stream_host_records(ctx, records, nrec, nfloat, offsets, ncones);
 }
 
 p2m_status p2m_paint_ensemble_device(p2m_ctx *ctx, const float *d_records,

@@ -26,6 +26,7 @@
 
 #include "p2m_scalar.h"
 
+#define P2M_STREAM_CHUNK (1LL << 21) /* host records per streamed ingest chunk */
 #define P2M_BIG_RINGS 64      /* default: halos spanning more rings go through the item buffer */
 #define P2M_TILE_SHIFT 5      /* compensated path: a flagged tile is 32 pixels (128 bytes) */
 #define P2M_TILE_PIX (1 << P2M_TILE_SHIFT)
