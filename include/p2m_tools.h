@@ -62,6 +62,12 @@ typedef struct p2m_tuning {
   int32_t halos_grid; /* blocks per SM of the fused enumerate-and-paint kernel, 1..16; 8 */
   int32_t full_grid;  /* blocks per SM of the stored-item kernel, 1..32; 8 */
   int32_t full_chunk; /* candidates per warp chunk of the stored-item kernel, 32..65536; 1024 */
+  int32_t stream_chunk; /* host records per chunk of the streamed ingest of p2m_paint_records
+                           (copy of chunk k+1 overlapped with chunk k), 65536..2^26; 2^22 */
+  int32_t stream_paint; /* 1: whenever a full chunk's worth of records (this call's or
+                           earlier calls') awaits painting, paint it before the next chunk is
+                           ingested, so that the copies overlap the painting too; 0: paint
+                           at the read-out; 1 */
   float ms;           /* p2m_autotune: device time of one paint call with the choice */
 } p2m_tuning;
 int32_t p2m_get_tuning(struct p2m_ctx *ctx, p2m_tuning *out);

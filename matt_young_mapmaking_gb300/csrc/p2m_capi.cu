@@ -44,7 +44,7 @@ struct p2m_ctx {
   bool th_set = false;
   float *d_tab[P2M_MAXTABLES] = {};
   float band_u = 2e-4f;
-  p2m_tuning tune = {P2M_BIG_RINGS, 8, 8, 1024, 0.0f}; /* launch parameters of the sweep */
+  p2m_tuning tune = {P2M_BIG_RINGS, 8, 8, 1024, (int32_t)P2M_STREAM_CHUNK, 1, 0.0f};
   /* outputs: hp_npix counts every cone's pixels (ncones * cone_npix) */
   long long hp_npix = 0, fs_npix = 0;
   long long cone_npix = 0;
@@ -68,6 +68,8 @@ struct p2m_ctx {
   long long cap_items_raw = 0, n_items = 0;
   long long rec_count = 0;
   bool dirty = false, swept = false;
+  bool unfolded = false; /* painted into the accumulators, read-out not yet run */
+  long long pending_recs = 0; /* records ingested since the last paint */
   /* per-call buffers */
   /* streamed ingest of host records: two device staging buffers filled on a copy stream
      while the previous chunk is cut and set up */
@@ -263,6 +265,8 @@ p2m_status read_counters(p2m_ctx *ctx, cudaStream_t s) {
   CK(cudaMemcpyAsync(ctx->h_ctr, ctx->d_ctr, sizeof(DevCounters), cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
   const DevCounters &h = *ctx->h_ctr;
+  /* an error flag stays set until it is reported here */
+  if (h.err) CK(cudaMemsetAsync(&ctx->d_ctr->err, 0, sizeof(unsigned int), s));
   if (h.err & P2M_DEVERR_RADIUS)
     return fail(ctx, P2M_ERR_BADARG, "a halo's disc radius exceeds pi (query_disc aborts)");
   if (h.err & P2M_DEVERR_ITEMS)
@@ -486,6 +490,7 @@ p2m_status ingest_device(p2m_ctx *ctx, const float *d_rec, long long nrec, int n
   if (st) return st;
   ctx->rec_count += nrec;
   ctx->n_records += nrec;
+  ctx->pending_recs += nrec;
   return P2M_OK;
 }
 
@@ -509,23 +514,17 @@ SweepBuffers sweep_buffers(const p2m_ctx *ctx) {
   return W;
 }
 
-/* produces the HEALPix output maps from everything ingested since the last sweep */
-p2m_status sweep(p2m_ctx *ctx, cudaStream_t s) {
+/* paints the HEALPix halos ingested since the last paint into the accumulators (the
+   output maps' high words and the low words, or the FP64 accumulator); the read-out
+   that turns them into maps is left to the next sweep */
+p2m_status paint_pending(p2m_ctx *ctx, cudaStream_t s) {
   ST(flush_prepared(ctx));
   ST(wait_zero(ctx, s));
   if (ctx->cfg.nside <= 0) {
     ctx->dirty = false;
     return P2M_OK;
   }
-  if (!ctx->dirty) {
-    if (!ctx->swept) {
-      for (int m = 0; m < ctx->cfg.nmaps; m++)
-        CK(cudaMemsetAsync(ctx->d_out[m], 0, sizeof(float) * (size_t)ctx->hp_npix, s));
-      ctx->swept = true;
-      ctx->outs_zeroed = true;
-    }
-    return P2M_OK;
-  }
+  if (!ctx->dirty) return P2M_OK;
   join_in(ctx, s);
   const long long n = ctx->n_items;
   CK(cudaMemsetAsync(ctx->d_ctr, 0, CALL_CTR_BYTES, s));
@@ -557,6 +556,32 @@ p2m_status sweep(p2m_ctx *ctx, cudaStream_t s) {
   p2m_launch_paint_halos(P, W, s, ctx->nsm);
   if (n > 0) CK(cudaStreamWaitEvent(s, ctx->ev_zero_done, 0));
   TE(PH_PAINT);
+  CK(cudaGetLastError());
+  join_out(ctx, s);
+  ctx->n_items = 0;
+  ctx->n_halos = 0;
+  ctx->pending_recs = 0;
+  ctx->dirty = false;
+  ctx->unfolded = true;
+  return P2M_OK;
+}
+
+/* produces the HEALPix output maps from everything ingested since the last sweep */
+p2m_status sweep(p2m_ctx *ctx, cudaStream_t s) {
+  ST(paint_pending(ctx, s));
+  if (ctx->cfg.nside <= 0) return P2M_OK;
+  if (!ctx->unfolded) {
+    if (!ctx->swept) {
+      for (int m = 0; m < ctx->cfg.nmaps; m++)
+        CK(cudaMemsetAsync(ctx->d_out[m], 0, sizeof(float) * (size_t)ctx->hp_npix, s));
+      ctx->swept = true;
+      ctx->outs_zeroed = true;
+    }
+    return P2M_OK;
+  }
+  join_in(ctx, s);
+  PaintParams P = make_params(ctx, 7);
+  SweepBuffers W = sweep_buffers(ctx);
   TB(PH_READOUT);
   if (compensated(ctx)) {
     /* fold the sparse low words into the maps and clear them */
@@ -572,6 +597,7 @@ p2m_status sweep(p2m_ctx *ctx, cudaStream_t s) {
   CK(cudaGetLastError());
   p2m_status st = read_counters(ctx, s);
   join_out(ctx, s);
+  ctx->unfolded = false;
   if (st) {
     /* accumulators may hold partial sums: clear them so the context stays usable */
     if (ctx->d_acc64)
@@ -585,9 +611,6 @@ p2m_status sweep(p2m_ctx *ctx, cudaStream_t s) {
     }
     return st;
   }
-  ctx->n_items = 0;
-  ctx->n_halos = 0;
-  ctx->dirty = false;
   ctx->swept = true;
   return P2M_OK;
 }
@@ -783,7 +806,7 @@ p2m_status p2m_load_table(p2m_ctx *ctx, int32_t slot, const void *image, int64_t
     for (int k = 0; k < P2M_MAXTABLES; k++) loaded += (ctx->d_tab[k] != nullptr && k != slot);
     if (!same && loaded) return fail(ctx, P2M_ERR_BADARG, "all tables of a context must share one header");
   }
-  if (ctx->dirty || !ctx->prep.empty())
+  if (ctx->dirty || ctx->unfolded || !ctx->prep.empty())
     return fail(ctx, P2M_ERR_STATE, "tables cannot change while painted halos await a read-out");
   CK(cudaSetDevice(ctx->cfg.device));
   CK(cudaStreamSynchronize(ctx->stream));
@@ -805,9 +828,23 @@ p2m_status p2m_reset_maps(p2m_ctx *ctx) {
   ctx->n_items = 0;
   ctx->rec_count = 0;
   ctx->n_records = 0;
+  ctx->pending_recs = 0;
   ctx->dirty = false;
   ctx->swept = false;
   ctx->outs_zeroed = false;
+  if (ctx->unfolded) {
+    /* painted but never read out: the accumulators that stay zero between read-outs
+       hold contributions */
+    if (ctx->d_acc64)
+      CK(cudaMemsetAsync(ctx->d_acc64, 0,
+                         sizeof(double) * (size_t)ctx->cfg.nmaps * (size_t)ctx->hp_npix, s));
+    if (ctx->d_lo) {
+      CK(cudaMemsetAsync(ctx->d_lo, 0, sizeof(float) * (size_t)ctx->cfg.nmaps * (size_t)ctx->hp_npix, s));
+      CK(cudaMemsetAsync(ctx->d_tiles, 0,
+                         (size_t)((ctx->hp_npix + P2M_TILE_PIX - 1) >> P2M_TILE_SHIFT), s));
+    }
+    ctx->unfolded = false;
+  }
   if (ctx->d_fs_acc)
     CK(cudaMemsetAsync(ctx->d_fs_acc, 0, 8 * (size_t)ctx->cfg.nmaps * (size_t)ctx->fs_npix, s));
   CK(cudaMemsetAsync(ctx->d_ctr, 0, sizeof(DevCounters), s));
@@ -820,7 +857,7 @@ p2m_status p2m_set_preprocess(p2m_ctx *ctx, int32_t scramble, int32_t centre, in
   if ((scramble != 0 && scramble != 1) || (centre != 0 && centre != 1) || ntasks < 1 ||
       ntasks > 25)
     return fail(ctx, P2M_ERR_BADARG, "scramble and centre must be 0 or 1, ntasks 1..25");
-  if (ctx->dirty || ctx->rec_count > 0 || !ctx->prep.empty())
+  if (ctx->dirty || ctx->unfolded || ctx->rec_count > 0 || !ctx->prep.empty())
     return fail(ctx, P2M_ERR_STATE, "set the pre-processing right after p2m_reset_maps");
   if ((scramble || centre) && ctx->ncones > 1)
     return fail(ctx, P2M_ERR_BADARG, "scramble and centre act on one catalogue, not an ensemble");
@@ -833,7 +870,7 @@ p2m_status p2m_set_preprocess(p2m_ctx *ctx, int32_t scramble, int32_t centre, in
 p2m_status upload_offsets(p2m_ctx *ctx, const int64_t *offsets, int32_t ncones, long long off,
                           long long n, cudaStream_t s);
 
-/* Host records in chunks of at most P2M_STREAM_CHUNK (and max_records): chunk k + 1 is
+/* Host records in chunks of at most the tuning's stream_chunk (and max_records): chunk k + 1 is
    copied on the copy stream into one of two device staging buffers while chunk k is cut
    and set up on the context's stream.  A buffer is refilled only after the chunk that
    used it has been ingested (the cut and set-up kernel is its only reader).  From pinned
@@ -844,7 +881,7 @@ p2m_status stream_host_records(p2m_ctx *ctx, const float *records, long long nre
                                const int64_t *offsets, int ncones) {
   const bool pre = ctx->pre.scramble || ctx->pre.centre;
   long long chunk = std::max<long long>(ctx->cfg.max_records, 1024);
-  if (!pre) chunk = std::min<long long>(chunk, P2M_STREAM_CHUNK);
+  if (!pre) chunk = std::min<long long>(chunk, ctx->tune.stream_chunk);
   if (nrec <= 0) return P2M_OK;
   const long long nchunk = (nrec + chunk - 1) / chunk;
   if (!ctx->cstream) {
@@ -882,6 +919,11 @@ p2m_status stream_host_records(p2m_ctx *ctx, const float *records, long long nre
     if (offsets) ST(upload_offsets(ctx, offsets, ncones, off, n, ctx->stream));
     p2m_status st = ingest_device(ctx, ctx->d_stage[b], n, nfloat, ctx->stream, offsets ? ncones : 0);
     CK(cudaEventRecord(ctx->ev_consumed[b], ctx->stream));
+    /* once a full chunk's worth of records awaits painting, paint it while the next
+       chunk (of this call or the next) is copied; smaller remainders wait for the
+       read-out, where one launch serves them all */
+    if (!st && ctx->tune.stream_paint && ctx->pending_recs >= chunk)
+      st = paint_pending(ctx, ctx->stream);
     if (st) {
       cudaStreamSynchronize(ctx->cstream);
       return st;
@@ -962,7 +1004,9 @@ namespace {
 
 bool tuning_ok(const p2m_tuning &t) {
   return t.big_rings >= 0 && t.big_rings <= 4096 && t.halos_grid >= 1 && t.halos_grid <= 16 &&
-         t.full_grid >= 1 && t.full_grid <= 32 && t.full_chunk >= 32 && t.full_chunk <= 65536;
+         t.full_grid >= 1 && t.full_grid <= 32 && t.full_chunk >= 32 && t.full_chunk <= 65536 &&
+         t.stream_chunk >= 65536 && t.stream_chunk <= (1 << 26) &&
+         (t.stream_paint == 0 || t.stream_paint == 1);
 }
 
 struct EventPair {
@@ -1082,7 +1126,7 @@ p2m_status p2m_bind_healpix_device(p2m_ctx *ctx, int32_t map, float *d_out) {
   if (!ctx) return P2M_ERR_BADARG;
   if (map < 0 || map >= ctx->cfg.nmaps || ctx->cfg.nside <= 0)
     return fail(ctx, P2M_ERR_BADARG, "map index out of range");
-  if (ctx->dirty || ctx->swept)
+  if (ctx->dirty || ctx->unfolded || ctx->swept)
     return fail(ctx, P2M_ERR_STATE, "bind output buffers right after p2m_reset_maps");
   ctx->d_out[map] = d_out ? d_out : ctx->d_out_own[map];
   ctx->outs_zeroed = false;

@@ -26,22 +26,22 @@
 
 #include "p2m_scalar.h"
 
-#define P2M_STREAM_CHUNK (1LL << 21) /* host records per streamed ingest chunk */
+#define P2M_STREAM_CHUNK (1LL << 22) /* host records per streamed ingest chunk */
 #define P2M_BIG_RINGS 64      /* default: halos spanning more rings go through the item buffer */
 #define P2M_TILE_SHIFT 5      /* compensated path: a flagged tile is 32 pixels (128 bytes) */
 #define P2M_TILE_PIX (1 << P2M_TILE_SHIFT)
 #define P2M_PHITAB 4096       /* grid angles 2 pi k / P2M_PHITAB of the disc-centre phi reduction */
 
 struct DevCounters {
-  /* per call (cleared before every ingest call and every sweep) */
+  /* per call (cleared before every ingest call and every paint) */
   unsigned long long n_surv, n_items, n_pix, n_fs_items, n_fs_rows;
-  unsigned int err, next_unit;
+  unsigned int next_unit, pad0;
   /* cumulative since the last reset */
   unsigned long long hp_updates, fs_updates, n_sets, n_recheck, n_shell, n_massive, n_enum,
       n_cand;
   unsigned long long val_checked, val_bad_set, val_bad_index;
   unsigned int val_max_du; /* float bits of the largest |u_fast - u_exact| */
-  unsigned int pad1;
+  unsigned int err;        /* P2M_DEVERR_* raised since it was last reported */
 };
 
 enum {

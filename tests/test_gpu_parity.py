@@ -205,6 +205,26 @@ def test_large_flatsky_field():
     assert_maps_close(fs[0], rfs[0], rel=1e-6, what="flat sky")
 
 
+@pytest.mark.parametrize("precision", PRECISIONS)
+def test_reset_discards_streamed_unread_paint(precision):
+    """A call streamed in chunks paints each chunk as it arrives; a reset before any
+    read-out must discard those contributions."""
+    a = catalogs.shell(27, 6000)
+    b = catalogs.shell(28, 5000)
+    tab = catalogs.table()
+    with p2m.Painter(nside=128, precision=precision, maps=((0, 1),), flags=FLAGS,
+                     max_records=1024) as pt:
+        pt.load_table(0, tab)
+        pt.paint_records(a)  # six chunks, painted one by one, never read
+        pt.reset()
+        pt.paint_records(b)
+        hp, st, sets = pt.healpix(0), pt.stats(), pt.pixel_sets()
+    rhp, _, rst, rsets = run_oracle(b, [tab], 128)
+    assert_sets_equal(sets, rsets)
+    assert st["hp_updates"] == rst["hp_updates"]
+    assert_maps_close(hp, rhp[0])
+
+
 def test_layout7_chihview_and_bad_records():
     rec = catalogs.shell(5, 20_000, nfloat=7).copy()
     rec[::997, 0] = np.nan
