@@ -225,6 +225,24 @@ def test_reset_discards_streamed_unread_paint(precision):
     assert_maps_close(hp, rhp[0])
 
 
+@pytest.mark.parametrize("model", [1, 2, 3])
+def test_profile_models_and_redshift_cuts(model):
+    """Each pressure-profile model (its overdensity enters the per-halo mass conversion,
+    pks2map.f90:293) with both redshift cuts active."""
+    rec = catalogs.shell(29 + model, 20_000, r=(100.0, 6000.0), m=(1e12, 3e15))
+    tab = catalogs.table(model=model, nu=0.0)
+    maps = ((0, 1), (0, 2))
+    kw = dict(model=model, zmin=0.05, zmax=1.5)
+    hp, _, st, sets = run_gpu(rec, [tab], "mixed", 1024, maps=maps, **kw)
+    rhp, _, rst, rsets = run_oracle(rec, [tab], 1024, maps=maps, **kw)
+    assert st["n_shell"] == rst["n_cut"] and st["n_painted"] == rst["n_painted"]
+    assert st["hp_updates"] == rst["hp_updates"] > 1000
+    assert 0 < st["n_shell"] < len(rec)
+    assert_sets_equal(sets, rsets)
+    for m in range(2):
+        assert_maps_close(hp[m], rhp[m], what="model %d map %d" % (model, m))
+
+
 def test_layout7_chihview_and_bad_records():
     rec = catalogs.shell(5, 20_000, nfloat=7).copy()
     rec[::997, 0] = np.nan
@@ -316,9 +334,11 @@ def test_fmath_bit_identical_host_device():
         assert same.all(), "fn %d: %d of %d differ" % (fn, (~same).sum(), n)
 
 
-def test_maptable_gpu_matches_oracle():
-    gpu = p2m.make_maptable(1, 148.0, 0.0, nchit=12, nmht=10, nrt=30)
-    ref = oracle.make_maptable(1, 148.0, 0.0, nchit=12, nmht=10, nrt=30)
+@pytest.mark.parametrize("model,nu,alpha", [(1, 148.0, 0.0), (1, 0.0, 0.0), (2, 545.0, 0.0),
+                                             (3, 218.0, 0.0), (1, 353.0, 1.0)])
+def test_maptable_gpu_matches_oracle(model, nu, alpha):
+    gpu = p2m.make_maptable(model, nu, alpha, nchit=12, nmht=10, nrt=30)
+    ref = oracle.make_maptable(model, nu, alpha, nchit=12, nmht=10, nrt=30)
     assert gpu[:36] == ref[:36]
     g = p2m.table_array(gpu).astype(np.float64)
     r = p2m.table_array(ref).astype(np.float64)
