@@ -35,7 +35,7 @@ MASS = (1e12, 3e15)
 SEED = 2
 ZMAX = 6.0
 MAPS = ((0, 1), (0, 2))
-LAUNCHES_PER_STEP = 12
+LAUNCHES_PER_STEP = 9
 # DRAM bytes (read + write) per pixel update of k_paint_halos from the ncu capture
 # summarised in profiles/paint_pipeline_1e7_nside2048.md
 PAINT_DRAM_BYTES_PER_UPDATE = 96.4
@@ -610,9 +610,9 @@ def run_ours(args):
                    "ms_per_step": e2e_ms, "h2d_bytes_per_step": int(rec.nbytes),
                    "d2h_bytes_per_step": int(len(MAPS) * npix * 4),
                    "h2d_ms": h2d_ms, "d2h_ms": d2h_ms}}
-    # per step: the fused cut and set-up, 3-kernel ring scan and the item kernel of the
-    # large halos, their candidate counts and 3-kernel scan, the fused paint, the
-    # large-halo paint and the fold of the low words (memsets are not kernels)
+    # per step: the fused cut and set-up, the item kernel of the large halos, their
+    # candidate counts and 3-kernel scan, the fused paint, the large-halo paint and the
+    # fold of the low words (memsets are not kernels)
     out["gpu_launches"] = LAUNCHES_PER_STEP * args.steps
 
     if not args.no_plain and args.precision == "mixed":

@@ -29,8 +29,8 @@ void p2m_philox4x32(const uint32_t c[4], const uint32_t k[2], uint32_t out[4]);
 
 /* Device time (ms) of each phase of the last paint call and of the last map read-out,
    for a context created with P2M_FLAG_TIMING: [0] cut with the per-halo set-up of
-   catalogue records (one kernel), [1] set-up of p2m_project_halo batches, [2] ring
-   offsets of the large halos, [3] their ring spans, [4] flat sky, [5] their candidate
+   catalogue records (one kernel), [1] set-up of p2m_project_halo batches, [2] unused
+   (0: the large halos reserve their item ranges during the set-up), [3] their ring spans, [4] flat sky, [5] their candidate
    offsets, [6] HEALPix paint (both painting kernels, which run concurrently), [7] the
    large halos' painting kernel alone, [8] read-out.  Diagnostics only (the reference prints no
    timings). */

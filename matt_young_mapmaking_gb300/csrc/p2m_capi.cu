@@ -280,10 +280,7 @@ p2m_status read_counters(p2m_ctx *ctx, cudaStream_t s) {
    The set-up kernel has been queued on s; n_max bounds the halo count. */
 p2m_status ingest_tail(p2m_ctx *ctx, const PaintParams &P, long long n_max, cudaStream_t s) {
   IngestBuffers B = ingest_buffers(ctx, nullptr);
-  TB(PH_SCAN);
-  p2m_launch_scan_u32(ctx->d_nring, &ctx->d_ctr->n_surv, ctx->d_ioff, &ctx->d_ctr->n_items,
-                      ctx->d_scan_tmp, s);
-  TE(PH_SCAN);
+  /* the large halos reserved their item ranges (d_ioff, n_items) during the set-up */
   ST(read_counters(ctx, s));
   long long n_halo = (long long)ctx->h_ctr->n_surv;
   long long n_items = P.nside > 0 ? (long long)ctx->h_ctr->n_items : 0;

@@ -305,9 +305,13 @@ __device__ void halo_geometry(const PaintParams &P, float xh, float yh, float zh
 __device__ __forceinline__ void store_halo(const PaintParams &P, const IngestBuffers &B, long long s,
                                            const HaloRec &H, unsigned long long &fsrows) {
   B.halos[s] = H;
-  /* items are made at ingest for the large halos only; the sweep enumerates the others */
+  /* items are made at ingest for the large halos only; the sweep enumerates the others.
+     A large halo reserves its items' place with one atomic add (they are rare, a few per
+     thousand halos, so the reservations hardly contend) */
   int nr = H.ir_hi - H.ir_lo + 1;
-  B.nring[s] = nr > P.big_rings ? (unsigned)nr : 0u;
+  const unsigned big = nr > P.big_rings ? (unsigned)nr : 0u;
+  B.nring[s] = big;
+  if (big) B.ioff[s] = (long long)atomicAdd(&B.ctr->n_items, (unsigned long long)big);
   if (H.jmin <= H.jmax && H.kmin <= H.kmax) fsrows += (unsigned long long)(H.kmax - H.kmin + 1);
 }
 
@@ -632,28 +636,19 @@ __global__ void __launch_bounds__(256) k_items(PaintParams P, IngestBuffers B) {
   const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
   for (long long h0 = warp * 32; h0 < n; h0 += nwarps * 32) {
-    long long h = h0 + lane;
-    long long off = h < n ? B.ioff[h] : (1LL << 62);
-    long long off0 = __shfl_sync(FULL, off, 0);
-    long long hl = min(h0 + 31, n - 1);
-    long long end = B.ioff[hl] + B.nring[hl];
-    int rel = (int)min(off - off0, (long long)0x7fffffff);
-    int total = (int)(end - off0);
-    for (int t = lane; t < total + ((32 - (total & 31)) & 31); t += 32) {
-      bool act = t < total;
-      int j = 0;
-#pragma unroll
-      for (int step = 16; step > 0; step >>= 1) {
-        int o = __shfl_sync(FULL, rel, j + step);
-        if (o <= t) j += step;
-      }
-      int relj = __shfl_sync(FULL, rel, j);
-      if (act) {
-        long long hh = h0 + j;
-        const HaloRec &H = B.halos[hh];
-        B.items[off0 + t] =
-            make_item(P, geom_of(H), (int)(B.halo_base + hh), H.ir_lo + (t - relj));
-      }
+    const long long h = h0 + lane;
+    /* the warp makes the items of each large halo of its 32 in turn, one ring per lane */
+    unsigned big = __ballot_sync(FULL, h < n && B.nring[h] > 0);
+    while (big) {
+      const int j = __ffs(big) - 1;
+      big &= big - 1;
+      const long long hh = h0 + j;
+      const HaloRec &H = B.halos[hh];
+      const long long off = B.ioff[hh];
+      const int cnt = (int)B.nring[hh];
+      const DiscGeom g = geom_of(H);
+      for (int t = lane; t < cnt; t += 32)
+        B.items[off + t] = make_item(P, g, (int)(B.halo_base + hh), H.ir_lo + t);
     }
   }
 }
