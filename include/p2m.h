@@ -47,8 +47,12 @@ enum {
                          recheck near every decision boundary; compensated FP32
                          accumulation: the float maps hold the high words, the exact
                          rounding errors are summed apart and added at read-out */
-  P2M_PREC_MIXED_F64 = 2 /* the same decisions; FP64 accumulation (atomic adds executed in
-                            L2, not on the SM's FP64 units) */
+  P2M_PREC_MIXED_F64 = 2, /* the same decisions; FP64 accumulation (atomic adds executed in
+                             L2, not on the SM's FP64 units) */
+  P2M_PREC_FIXED = 3      /* the same decisions; 64-bit fixed-point accumulation in units of
+                             2^-56 (each value rounded to the unit, |pixel sum| < 128):
+                             integer adds do not depend on their order, so the maps are
+                             bit-identical from run to run and across launch parameters */
 };
 
 /* catalogue layouts (floats per record): 7 = x,y,z,vx,vy,vz,RTH after a 2-word header

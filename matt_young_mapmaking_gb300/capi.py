@@ -18,7 +18,7 @@ LIB_PATH = os.path.join(_HERE, "libp2m_gb300.so")
 MAXMAPS = 8
 NOALLOC_MAXMAPS = 8  # P2M_NOALLOC_MAXMAPS of include/p2m_tools.h
 P2M_OK, P2M_ERR_BADARG, P2M_ERR_CUDA, P2M_ERR_CAPACITY = 0, 1, 2, 3
-PREC_FP64, PREC_MIXED, PREC_MIXED_F64 = 0, 1, 2
+PREC_FP64, PREC_MIXED, PREC_MIXED_F64, PREC_FIXED = 0, 1, 2, 3
 FLAG_RECORD_SETS, FLAG_ALL_HALOS, FLAG_TIMING, FLAG_VALIDATE = 1, 2, 4, 8
 STATUS = {0: "OK", 1: "BADARG", 2: "CUDA", 3: "CAPACITY", 4: "TIMEOUT", 5: "IO", 6: "STATE",
           7: "NOMEM"}
@@ -178,7 +178,7 @@ class Painter:
         cfg.zmin, cfg.zmax, cfg.chihview, cfg.model = zmin, zmax, chihview, model
         if isinstance(precision, str):
             precision = {"fp64": PREC_FP64, "mixed": PREC_MIXED,
-                         "mixed64": PREC_MIXED_F64}[precision]
+                         "mixed64": PREC_MIXED_F64, "fixed": PREC_FIXED}[precision]
         cfg.precision = precision
         maps = list(maps)
         if not 1 <= len(maps) <= MAXMAPS:

@@ -624,7 +624,7 @@ p2m_status p2m_create(const p2m_config *cfg, p2m_ctx **out) {
   if (cfg->nside == 0 && cfg->npix_fs == 0) return P2M_ERR_BADARG;
   if (cfg->model < 1 || cfg->model > 3) return P2M_ERR_BADARG;
   if (cfg->nmaps < 1 || cfg->nmaps > P2M_MAXMAPS) return P2M_ERR_BADARG;
-  if (cfg->precision < P2M_PREC_FP64 || cfg->precision > P2M_PREC_MIXED_F64) return P2M_ERR_BADARG;
+  if (cfg->precision < P2M_PREC_FP64 || cfg->precision > P2M_PREC_FIXED) return P2M_ERR_BADARG;
   if (cfg->ncones < 0 || cfg->ncones > P2M_MAXCONES) return P2M_ERR_BADARG;
   if (cfg->ncones > 1 && (cfg->nside == 0 || cfg->npix_fs != 0)) return P2M_ERR_BADARG;
   for (int m = 0; m < cfg->nmaps; m++) {

@@ -709,8 +709,9 @@ __device__ __forceinline__ HotHalo hot_of(const HaloRec &H) {
    (fire-and-forget red.add.f64); ACC 1: two-float (hi, lo) FP32 accumulator, hi by an
    atomic add that returns the old value, lo the exact TwoSum rounding error; ACC 2:
    compensated accumulation with the float output map as the high word, the low words
-   sparse (nonzero only where an add rounded) and their tiles flagged.  All maps' adds are
-   issued before any result is used. */
+   sparse (nonzero only where an add rounded) and their tiles flagged; ACC 3: 64-bit
+   fixed-point accumulator (value * 2^56 rounded to an integer, fire-and-forget).  All
+   maps' adds are issued before any result is used. */
 template <int ACC>
 __device__ __forceinline__ void accumulate_vals(const PaintParams &P, void *acc, long long slot,
                                                 const float *vals, const SweepBuffers *W) {
@@ -738,6 +739,14 @@ __device__ __forceinline__ void accumulate_vals(const PaintParams &P, void *acc,
       }
     }
     if (any) W->tiles[slot >> P2M_TILE_SHIFT] = 1;
+  } else if (ACC == 3) {
+    /* 64-bit fixed point: integer adds are associative, so the sums do not depend on the
+       order in which the atomics land */
+    unsigned long long *a = (unsigned long long *)acc + slot * P.nmaps;
+#pragma unroll
+    for (int m = 0; m < P2M_MAXMAPS; m++)
+      if (m < P.nmaps && vals[m] != 0.0f)
+        atomicAdd(a + m, (unsigned long long)__double2ll_rn((double)vals[m] * P2M_FIXED_ONE));
   } else {
     float *a = (float *)acc + 2 * slot * P.nmaps;
     float olds[P2M_MAXMAPS];
@@ -1377,6 +1386,22 @@ __global__ void __launch_bounds__(256) k_item_counts(const RingItem *items, long
    afterwards with a memset, because overwriting the lines that a pass has just read runs
    at a fraction of the HBM rate of a read pass followed by a separate clear (measured on
    GB300: 1.0 TB/s against 6.8 TB/s + a 7.7 TB/s memset) */
+template <int FIXED>
+__device__ __forceinline__ double2 acc_pair(const double *acc, long long p) {
+  if (FIXED) {
+    const longlong2 q = __ldcs((const longlong2 *)acc + p);
+    return make_double2((double)q.x * P2M_FIXED_UNIT, (double)q.y * P2M_FIXED_UNIT);
+  }
+  return __ldcs((const double2 *)acc + p);
+}
+template <int FIXED>
+__device__ __forceinline__ double acc_one(const double *acc, long long i) {
+  if (FIXED) return (double)__ldcs((const long long *)acc + i) * P2M_FIXED_UNIT;
+  return __ldcs(acc + i);
+}
+
+/* FIXED 1: the accumulator holds 64-bit fixed-point sums (unit 2^-56) */
+template <int FIXED>
 __global__ void __launch_bounds__(256) k_finalize_full(const double *acc, long long npix, int nmaps,
                                                        float *o0, float *o1, float *o2, float *o3,
                                                        float *o4, float *o5, float *o6, float *o7,
@@ -1384,12 +1409,11 @@ __global__ void __launch_bounds__(256) k_finalize_full(const double *acc, long l
   float *outs[8] = {o0, o1, o2, o3, o4, o5, o6, o7};
   const long long stride = (long long)gridDim.x * blockDim.x;
   if (nmaps == 2) {
-    const double2 *a2 = (const double2 *)acc;
     for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < npix; p += 4 * stride) {
       double2 a[4];
 #pragma unroll
       for (int u = 0; u < 4; u++)
-        if (p + u * stride < npix) a[u] = __ldcs(a2 + p + u * stride);
+        if (p + u * stride < npix) a[u] = acc_pair<FIXED>(acc, p + u * stride);
 #pragma unroll
       for (int u = 0; u < 4; u++) {
         long long q = p + u * stride;
@@ -1416,7 +1440,7 @@ __global__ void __launch_bounds__(256) k_finalize_full(const double *acc, long l
       double r[P2M_MAXMAPS];
 #pragma unroll
       for (int k = 0; k < P2M_MAXMAPS; k++)
-        if (t + k * 256 < n) r[k] = __ldcs(a + t + k * 256);
+        if (t + k * 256 < n) r[k] = acc_one<FIXED>(a, t + k * 256);
 #pragma unroll
       for (int k = 0; k < P2M_MAXMAPS; k++)
         if (t + k * 256 < n) sv[t + k * 256] = (float)r[k];
@@ -1535,6 +1559,8 @@ __global__ void __launch_bounds__(256) k_finalize_fs(const void *acc, long long 
     float v;
     if (PREC == 0) {
       v = (float)((const double *)acc)[p * nmaps + map];
+    } else if (PREC == 3) {
+      v = (float)((double)((const long long *)acc)[p * nmaps + map] * P2M_FIXED_UNIT);
     } else {
       float2 a = ((const float2 *)acc)[p * nmaps + map];
       v = __fadd_rn(a.x, a.y);
@@ -1749,12 +1775,14 @@ void p2m_launch_fs(const PaintParams &P, const IngestBuffers &B, long long n_max
                    int nsm) {
   k_fs_emit<<<grid_for(n_max, 256, nsm, 4), 256, 0, s>>>(P, B);
   if (P.precision == 1) k_paint_fs<1><<<nsm * 8, 256, 0, s>>>(P, B);
+  else if (P.precision == 3) k_paint_fs<3><<<nsm * 8, 256, 0, s>>>(P, B);
   else k_paint_fs<0><<<nsm * 8, 256, 0, s>>>(P, B);
 }
 void p2m_launch_paint_full(const PaintParams &P, const SweepBuffers &W, cudaStream_t s, int nsm) {
   const int g = nsm * P.full_grid;
   if (P.precision == 0) k_paint_full<1, 0><<<g, 256, 0, s>>>(P, W);
   else if (P.precision == 1) k_paint_full<0, 2><<<g, 256, 0, s>>>(P, W);
+  else if (P.precision == 3) k_paint_full<0, 3><<<g, 256, 0, s>>>(P, W);
   else k_paint_full<0, 0><<<g, 256, 0, s>>>(P, W);
 }
 template <int EXACT, int ACC>
@@ -1773,6 +1801,7 @@ static void launch_paint_halos(const PaintParams &P, const SweepBuffers &W, cuda
 void p2m_launch_paint_halos(const PaintParams &P, const SweepBuffers &W, cudaStream_t s, int nsm) {
   if (P.precision == 0) launch_paint_halos<1, 0>(P, W, s, nsm);
   else if (P.precision == 1) launch_paint_halos<0, 2>(P, W, s, nsm);
+  else if (P.precision == 3) launch_paint_halos<0, 3>(P, W, s, nsm);
   else launch_paint_halos<0, 0>(P, W, s, nsm);
 }
 void p2m_launch_item_counts(const RingItem *items, long long n, unsigned int *counts,
@@ -1787,14 +1816,19 @@ void p2m_launch_map_sum(const float *map, long long n, double *sum, cudaStream_t
 }
 void p2m_launch_finalize_full(const PaintParams &P, const void *acc, long long npix,
                               float *const *out, int accumulate, cudaStream_t s, int nsm) {
-  k_finalize_full<<<grid_for(npix, 256, nsm, 8), 256, 0, s>>>(
-      (const double *)acc, npix, P.nmaps, out[0], out[1], out[2], out[3], out[4], out[5], out[6], out[7],
-      accumulate);
+  const int g = grid_for(npix, 256, nsm, 8);
+  if (P.precision == 3)
+    k_finalize_full<1><<<g, 256, 0, s>>>((const double *)acc, npix, P.nmaps, out[0], out[1], out[2],
+                                         out[3], out[4], out[5], out[6], out[7], accumulate);
+  else
+    k_finalize_full<0><<<g, 256, 0, s>>>((const double *)acc, npix, P.nmaps, out[0], out[1], out[2],
+                                         out[3], out[4], out[5], out[6], out[7], accumulate);
 }
 void p2m_launch_finalize_fs(const PaintParams &P, const void *acc, long long npix, float *out,
                             int map, double *sum, cudaStream_t s, int nsm) {
   int g = grid_for(npix, 256, nsm, 8);
   if (P.precision == 1) k_finalize_fs<1><<<g, 256, 0, s>>>(acc, npix, P.nmaps, map, out, sum);
+  else if (P.precision == 3) k_finalize_fs<3><<<g, 256, 0, s>>>(acc, npix, P.nmaps, map, out, sum);
   else k_finalize_fs<0><<<g, 256, 0, s>>>(acc, npix, P.nmaps, map, out, sum);
 }
 void p2m_launch_maptable(const PaintParams &P, const TableConsts &K, const p2m_tabhdr &th,

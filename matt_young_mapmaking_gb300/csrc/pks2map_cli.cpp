@@ -8,7 +8,7 @@
  * argument that is a single dot, or does not parse, takes its default, textlib.f90:33-86),
  * the same report lines, and the same output files: <fileout>_dp.bin, _fs.map, _hp.fits.
  * The halo loop runs on the GPU through the C ABI (include/p2m.h).  The environment
- * selects the precision (P2M_PRECISION = mixed | fp64 | mixed64, default mixed) and the
+ * selects the precision (P2M_PRECISION = mixed | fp64 | mixed64 | fixed, default mixed) and the
  * device (P2M_DEVICE, default 0).  scramble and center follow the reference's random
  * stream and rotation; P2M_RANKS (default 1, at most 25) is the MPI rank count whose
  * halo blocks and streams they reproduce (`mpirun -np <ranks> pks2map ...`).
@@ -166,6 +166,7 @@ int main(int argc, char **argv) {
   if (const char *e = std::getenv("P2M_PRECISION")) {
     if (!std::strcmp(e, "fp64")) cfg.precision = P2M_PREC_FP64;
     else if (!std::strcmp(e, "mixed64")) cfg.precision = P2M_PREC_MIXED_F64;
+    else if (!std::strcmp(e, "fixed")) cfg.precision = P2M_PREC_FIXED;
   }
   cfg.nmaps = 1;
   cfg.map_table[0] = 0;

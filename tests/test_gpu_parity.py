@@ -17,7 +17,7 @@ SUM_TOL = 1e-7       # map totals
 # r differs from the reference's FP64-angle r by ~1 ulp, about 1e-6 of a pixel's value
 SUM_TOL_MIXED_FEW = 1e-6
 FLAGS = p2m.FLAG_RECORD_SETS | p2m.FLAG_ALL_HALOS
-PRECISIONS = ["fp64", "mixed", "mixed64"]
+PRECISIONS = ["fp64", "mixed", "mixed64", "fixed"]
 
 
 def run_gpu(records, tables, precision, nside, npix_fs=0, maps=((0, 1),), flags=FLAGS,
@@ -241,6 +241,41 @@ def test_profile_models_and_redshift_cuts(model):
     assert_sets_equal(sets, rsets)
     for m in range(2):
         assert_maps_close(hp[m], rhp[m], what="model %d map %d" % (model, m))
+
+
+def test_fixed_point_maps_are_bit_identical():
+    """P2M_PREC_FIXED: the same maps, bit for bit, from repeated runs and from launch
+    parameters that route every halo through the other painting kernel (the atomics land
+    in a different order each time), HEALPix and flat sky; and within tolerance of FP64."""
+    rec = np.concatenate([catalogs.edge_cases(),
+                          catalogs.cone(33, 20_000, (1.0, 0.0, 0.0), 8.0, r=(100.0, 3000.0))])
+    tab = catalogs.table(nu=0.0)
+    maps = ((0, 1), (0, 2))
+    runs = []
+    for tune in (None, None, dict(big_rings=0, full_grid=3, full_chunk=96),
+                 dict(big_rings=4096, halos_grid=1)):
+        with p2m.Painter(nside=256, npix_fs=256, fov_deg=10.0, precision="fixed", maps=maps,
+                         max_records=len(rec)) as pt:
+            if tune:
+                pt.set_tuning(**tune)
+            pt.load_table(0, tab)
+            pt.paint_records(rec)
+            runs.append([pt.healpix(m) for m in range(2)] + [pt.flatsky(m) for m in range(2)])
+    for r in runs[1:]:
+        for a, b in zip(runs[0], r):
+            assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+    # against the compensated path, which takes the same decisions and profile values,
+    # and against FP64 on the single-signed tSZ maps (the signed kSZ sums of this dense
+    # cone cancel in places, which magnifies the FP32 profile values' rounding)
+    hpm, fsm, _, _ = run_gpu(rec, [tab], "mixed", 256, npix_fs=256, fov_deg=10.0, maps=maps,
+                             flags=0)
+    hp64, fs64, _, _ = run_gpu(rec, [tab], "fp64", 256, npix_fs=256, fov_deg=10.0, maps=maps,
+                               flags=0)
+    for m in range(2):
+        assert_maps_close(runs[0][m], hpm[m], rel=1e-6, what="healpix %d vs mixed" % m)
+        assert_maps_close(runs[0][2 + m], fsm[m], rel=1e-6, what="flat sky %d vs mixed" % m)
+    assert_maps_close(runs[0][0], hp64[0], what="healpix tSZ vs fp64")
+    assert_maps_close(runs[0][2], fs64[0], rel=1e-6, what="flat sky tSZ vs fp64")
 
 
 def test_layout7_chihview_and_bad_records():
