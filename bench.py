@@ -632,6 +632,29 @@ def run_ours(args):
                 errs[name]["cl_ratio"] = dict(cl_ratio(spec), lmax=args.cl_lmax)
         out["error_vs_fp64"] = errs
 
+        # the deterministic arm: 64-bit fixed-point accumulation; its maps are compared bit
+        # for bit with a second run whose launch parameters send every halo through the
+        # other painting kernel (so the atomics land in another order)
+        pf = make("fixed")
+        msf, _ = timed(pf, max(2, args.steps // 2), 1)
+        fixed_maps = [o.cpu().numpy() for o in outs]
+        pf.close()
+        pf = p2m.Painter(nside=nside, precision="fixed", maps=MAPS, zmax=ZMAX, max_records=N,
+                         device=local)
+        pf.load_table(0, table)
+        pf.set_tuning(big_rings=0)
+        pf.paint_records_device(d_rec.data_ptr(), N, 10)
+        other = [pf.healpix(m) for m in range(len(MAPS))]
+        pf.close()
+        out["fixed_point"] = {
+            "value": total_halos / (msf * 1e-3), "ms_per_step": msf,
+            "bit_identical_across_launch_parameters": all(
+                np.array_equal(a.view(np.uint32), b.view(np.uint32))
+                for a, b in zip(fixed_maps, other)),
+            "tuning": tunings.get("fixed"),
+            "error_vs_fp64": {name: map_errors(fixed_maps[m], ref_maps[m])
+                              for m, name in enumerate(("tsz", "ksz"))}}
+
     # the other configurations' reports run in single-GPU runs only (replica runs time
     # the headline workload alone)
     if rank == 0 and ws == 1 and not args.no_precision_form:
