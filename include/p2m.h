@@ -168,6 +168,15 @@ p2m_status p2m_flush(p2m_ctx *ctx);
    (12*nside^2 or npix_fs^2 floats, RING / column-major j-fastest order) ... */
 p2m_status p2m_get_healpix(p2m_ctx *ctx, int32_t map, float *out);
 p2m_status p2m_get_flatsky(p2m_ctx *ctx, int32_t map, float *out);
+/* The same read-out into host memory, returning as soon as it is queued: the map is
+   finished on the device and copied on a read-out stream of its own, beside whatever the
+   caller does next; p2m_synchronize waits for the copies.  Pinned host memory makes the
+   copy asynchronous.  Anything that would write the map's buffer before its copy is done
+   (a clear after p2m_reset_maps, more painting, another read-out) waits for the copy, so
+   a caller who paints the next catalogue while the maps are copied binds other buffers
+   (p2m_bind_healpix_device) to the maps first.  No counterpart in the reference, which
+   reads each map once at the end of its run. */
+p2m_status p2m_get_healpix_async(p2m_ctx *ctx, int32_t map, float *out);
 /* ... or device memory, ordered on `stream` (NULL = the context's stream). */
 p2m_status p2m_get_healpix_device(p2m_ctx *ctx, int32_t map, float *d_out, void *stream);
 /* Make a caller-owned device buffer of 12*nside^2 floats (times ncones for an ensemble)

@@ -127,6 +127,7 @@ def load_library():
         "p2m_paint_ensemble_device": (I32, [VP, VP, VP, I32, I32, VP]),
         "p2m_get_healpix_cone": (I32, [VP, I32, I32, VP]),
         "p2m_get_tuning": (I32, [VP, ctypes.POINTER(P2MTuning)]),
+        "p2m_get_healpix_async": (I32, [VP, I32, VP]),
         "p2m_set_tuning": (I32, [VP, ctypes.POINTER(P2MTuning)]),
         "p2m_autotune": (I32, [VP, VP, I64, I32, I32, ctypes.POINTER(P2MTuning)]),
         "p2m_cl_flatsky": (I32, [I32, VP, VP, I32, F, D, I32, VP, VP, VP, VP, VP]),
@@ -151,7 +152,7 @@ def exported_symbols():
             "p2m_dpdy", "p2m_write_dpdy",
             "p2m_write_flatsky", "p2m_write_healpix_fits", "p2m_cl_healpix", "p2m_cl_flatsky",
             "p2m_paint_ensemble", "p2m_paint_ensemble_device", "p2m_get_healpix_cone",
-            "p2m_get_tuning", "p2m_set_tuning", "p2m_autotune"]
+            "p2m_get_tuning", "p2m_set_tuning", "p2m_autotune", "p2m_get_healpix_async"]
 
 
 PHASES = ["cut", "setup", "big_scan", "big_items", "flatsky", "big_offsets", "paint", "paint_big",
@@ -322,6 +323,11 @@ class Painter:
     def healpix_into(self, m, host_ptr):
         """Read map m into host memory at host_ptr (12*nside^2 floats, e.g. pinned)."""
         self._check(self._lib.p2m_get_healpix(self._h, m, ctypes.c_void_p(host_ptr)))
+
+    def healpix_async(self, m, host_ptr):
+        """Queue the read-out of map m into host memory at host_ptr (pinned) and return;
+        synchronize() waits for it."""
+        self._check(self._lib.p2m_get_healpix_async(self._h, m, ctypes.c_void_p(host_ptr)))
 
     def bind_healpix_device(self, m, dptr):
         """Make device buffer dptr (12*nside^2 floats) the storage of map m."""

@@ -74,6 +74,16 @@ struct p2m_ctx {
   /* streamed ingest of host records: two device staging buffers filled on a copy stream
      while the previous chunk is cut and set up */
   cudaStream_t cstream = nullptr;
+  /* asynchronous read-outs (p2m_get_healpix_async): copies on their own stream; the buffer
+     each map's last one reads, and the event that marks its end */
+  cudaStream_t rstream = nullptr;
+  cudaEvent_t ev_ready = nullptr;
+  /* one guard per buffer with a read-out queued: its last copy's end; a guard is reused
+     (after a host wait for its copy) when more buffers than guards are in flight */
+  static const int NGUARD = 4 * P2M_MAXMAPS;
+  const float *rd_buf[NGUARD] = {};
+  cudaEvent_t rd_ev[NGUARD] = {};
+  unsigned long long rd_seq[NGUARD] = {}, rd_clock = 0;
   float *d_stage[2] = {nullptr, nullptr};
   long long cap_stage[2] = {0, 0};
   cudaEvent_t ev_copied[2] = {nullptr, nullptr}, ev_consumed[2] = {nullptr, nullptr};
@@ -93,7 +103,8 @@ struct p2m_ctx {
   double *d_sums = nullptr; /* [0, MAXMAPS): HEALPix, [MAXMAPS, 2 MAXMAPS): flat sky */
   long long *d_set_rec = nullptr, *d_set_pix = nullptr;
   long long cap_set = 0;
-  DevCounters *d_ctr = nullptr, *h_ctr = nullptr;
+  DevCounters *d_ctr = nullptr, *h_ctr = nullptr; /* h_ctr: mapped pinned host memory */
+  DevCounters *h_ctr_dev = nullptr;                /* its device address */
   float *d_prep = nullptr;
   long long cap_prep = 0;
   std::vector<float> prep;
@@ -262,7 +273,8 @@ p2m_status check_tables(p2m_ctx *ctx) {
 }
 
 p2m_status read_counters(p2m_ctx *ctx, cudaStream_t s) {
-  CK(cudaMemcpyAsync(ctx->h_ctr, ctx->d_ctr, sizeof(DevCounters), cudaMemcpyDeviceToHost, s));
+  p2m_launch_copy_counters(ctx->d_ctr, ctx->h_ctr_dev, s);
+  CK(cudaGetLastError());
   CK(cudaStreamSynchronize(s));
   const DevCounters &h = *ctx->h_ctr;
   /* an error flag stays set until it is reported here */
@@ -315,15 +327,32 @@ bool compensated(const p2m_ctx *ctx) { return ctx->d_lo != nullptr; }
    paint after a reset (the buffers bound at that time).  The clear is bandwidth-bound
    and independent of the ingest, so it runs on a side stream after the work already on
    s; the sweep waits for it before painting. */
+p2m_status wait_reads(p2m_ctx *ctx, cudaStream_t s);
+
 p2m_status zero_outputs(p2m_ctx *ctx, cudaStream_t s) {
   if (!compensated(ctx) || ctx->outs_zeroed) return P2M_OK;
   CK(cudaEventRecord(ctx->ev_zero_start, s));
   CK(cudaStreamWaitEvent(ctx->zstream, ctx->ev_zero_start, 0));
+  ST(wait_reads(ctx, ctx->zstream));
   for (int m = 0; m < ctx->cfg.nmaps; m++)
     CK(cudaMemsetAsync(ctx->d_out[m], 0, sizeof(float) * (size_t)ctx->hp_npix, ctx->zstream));
   CK(cudaEventRecord(ctx->ev_zero_done, ctx->zstream));
   ctx->zero_pending = true;
   ctx->outs_zeroed = true;
+  return P2M_OK;
+}
+
+/* orders s after the asynchronous read-outs that may still be copying a map buffer bound
+   now, so that nothing writes a map while it is being read out */
+p2m_status wait_reads(p2m_ctx *ctx, cudaStream_t s) {
+  for (int r = 0; r < p2m_ctx::NGUARD; r++) {
+    if (!ctx->rd_buf[r]) continue;
+    for (int m = 0; m < ctx->cfg.nmaps; m++)
+      if (ctx->d_out[m] == ctx->rd_buf[r]) {
+        CK(cudaStreamWaitEvent(s, ctx->rd_ev[r], 0));
+        break;
+      }
+  }
   return P2M_OK;
 }
 
@@ -523,6 +552,7 @@ p2m_status paint_pending(p2m_ctx *ctx, cudaStream_t s) {
   }
   if (!ctx->dirty) return P2M_OK;
   join_in(ctx, s);
+  ST(wait_reads(ctx, s));
   const long long n = ctx->n_items;
   CK(cudaMemsetAsync(ctx->d_ctr, 0, CALL_CTR_BYTES, s));
   PaintParams P = make_params(ctx, 7);
@@ -569,6 +599,7 @@ p2m_status sweep(p2m_ctx *ctx, cudaStream_t s) {
   if (ctx->cfg.nside <= 0) return P2M_OK;
   if (!ctx->unfolded) {
     if (!ctx->swept) {
+      ST(wait_reads(ctx, s));
       for (int m = 0; m < ctx->cfg.nmaps; m++)
         CK(cudaMemsetAsync(ctx->d_out[m], 0, sizeof(float) * (size_t)ctx->hp_npix, s));
       ctx->swept = true;
@@ -577,6 +608,7 @@ p2m_status sweep(p2m_ctx *ctx, cudaStream_t s) {
     return P2M_OK;
   }
   join_in(ctx, s);
+  ST(wait_reads(ctx, s));
   PaintParams P = make_params(ctx, 7);
   SweepBuffers W = sweep_buffers(ctx);
   TB(PH_READOUT);
@@ -708,7 +740,8 @@ p2m_status p2m_create(const p2m_config *cfg, p2m_ctx **out) {
   }
   CK(cudaMalloc((void **)&ctx->d_scan_tmp, sizeof(long long) * 1024));
   CK(cudaMalloc((void **)&ctx->d_ctr, sizeof(DevCounters)));
-  CK(cudaMallocHost((void **)&ctx->h_ctr, sizeof(DevCounters)));
+  CK(cudaHostAlloc((void **)&ctx->h_ctr, sizeof(DevCounters), cudaHostAllocMapped));
+  CK(cudaHostGetDevicePointer((void **)&ctx->h_ctr_dev, ctx->h_ctr, 0));
   CK(cudaMalloc((void **)&ctx->d_nitems, sizeof(unsigned long long)));
   CK(cudaMalloc((void **)&ctx->d_pre_bits, sizeof(unsigned int)));
   CK(cudaMalloc((void **)&ctx->d_sums, sizeof(double) * 2 * P2M_MAXMAPS));
@@ -754,6 +787,13 @@ void p2m_destroy(p2m_ctx *ctx) {
     cudaStreamSynchronize(ctx->cstream);
     cudaStreamDestroy(ctx->cstream);
   }
+  if (ctx->rstream) {
+    cudaStreamSynchronize(ctx->rstream);
+    cudaStreamDestroy(ctx->rstream);
+  }
+  if (ctx->ev_ready) cudaEventDestroy(ctx->ev_ready);
+  for (int r = 0; r < p2m_ctx::NGUARD; r++)
+    if (ctx->rd_ev[r]) cudaEventDestroy(ctx->rd_ev[r]);
   for (int b = 0; b < 2; b++) {
     if (ctx->ev_copied[b]) cudaEventDestroy(ctx->ev_copied[b]);
     if (ctx->ev_consumed[b]) cudaEventDestroy(ctx->ev_consumed[b]);
@@ -1158,6 +1198,41 @@ p2m_status p2m_get_healpix(p2m_ctx *ctx, int32_t map, float *out) {
   return P2M_OK;
 }
 
+p2m_status p2m_get_healpix_async(p2m_ctx *ctx, int32_t map, float *out) {
+  if (!ctx || !out) return P2M_ERR_BADARG;
+  if (map < 0 || map >= ctx->cfg.nmaps || ctx->cfg.nside <= 0)
+    return fail(ctx, P2M_ERR_BADARG, "map index out of range");
+  CK(cudaSetDevice(ctx->cfg.device));
+  ST(sweep(ctx, ctx->stream));
+  if (!ctx->rstream) {
+    CK(cudaStreamCreateWithFlags(&ctx->rstream, cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&ctx->ev_ready, cudaEventDisableTiming));
+    for (int r = 0; r < p2m_ctx::NGUARD; r++)
+      CK(cudaEventCreateWithFlags(&ctx->rd_ev[r], cudaEventDisableTiming));
+  }
+  /* the guard of this buffer: its own, a free one, or the oldest after its copy is done */
+  const float *buf = ctx->d_out[map];
+  int g = -1;
+  for (int r = 0; r < p2m_ctx::NGUARD && g < 0; r++)
+    if (ctx->rd_buf[r] == buf) g = r;
+  for (int r = 0; r < p2m_ctx::NGUARD && g < 0; r++)
+    if (!ctx->rd_buf[r]) g = r;
+  if (g < 0) {
+    g = 0;
+    for (int r = 1; r < p2m_ctx::NGUARD; r++)
+      if (ctx->rd_seq[r] < ctx->rd_seq[g]) g = r;
+    CK(cudaEventSynchronize(ctx->rd_ev[g]));
+  }
+  CK(cudaEventRecord(ctx->ev_ready, ctx->stream));
+  CK(cudaStreamWaitEvent(ctx->rstream, ctx->ev_ready, 0));
+  CK(cudaMemcpyAsync(out, buf, sizeof(float) * (size_t)ctx->hp_npix, cudaMemcpyDeviceToHost,
+                     ctx->rstream));
+  CK(cudaEventRecord(ctx->rd_ev[g], ctx->rstream));
+  ctx->rd_buf[g] = buf;
+  ctx->rd_seq[g] = ++ctx->rd_clock;
+  return P2M_OK;
+}
+
 p2m_status p2m_get_flatsky(p2m_ctx *ctx, int32_t map, float *out) {
   if (!ctx || !out) return P2M_ERR_BADARG;
   if (map < 0 || map >= ctx->cfg.nmaps || ctx->cfg.npix_fs <= 0)
@@ -1219,6 +1294,7 @@ p2m_status p2m_synchronize(p2m_ctx *ctx) {
   CK(cudaSetDevice(ctx->cfg.device));
   CK(cudaStreamSynchronize(ctx->zstream));
   CK(cudaStreamSynchronize(ctx->stream));
+  if (ctx->rstream) CK(cudaStreamSynchronize(ctx->rstream));
   return P2M_OK;
 }
 

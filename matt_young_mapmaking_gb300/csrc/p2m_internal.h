@@ -185,6 +185,9 @@ void p2m_launch_finalize_fs(const PaintParams &P, const void *acc, long long npi
                             int map, double *sum, cudaStream_t s, int nsm);
 void p2m_launch_fold_lo(const PaintParams &P, const SweepBuffers &W, cudaStream_t s, int nsm);
 void p2m_launch_map_sum(const float *map, long long n, double *sum, cudaStream_t s, int nsm);
+/* copies the counters into mapped host memory with the SMs' stores: no copy engine, so a
+   counter read never queues behind a large read-out copy */
+void p2m_launch_copy_counters(const DevCounters *d, DevCounters *h_mapped, cudaStream_t s);
 struct TableConsts {
   float y0, tau0, x0const, nu, alpha;
   int model;

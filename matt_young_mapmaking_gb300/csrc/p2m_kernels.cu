@@ -1811,6 +1811,14 @@ void p2m_launch_item_counts(const RingItem *items, long long n, unsigned int *co
 void p2m_launch_fold_lo(const PaintParams &P, const SweepBuffers &W, cudaStream_t s, int nsm) {
   k_fold_lo<<<nsm * 8, 256, 0, s>>>(W, P.nmaps);
 }
+__global__ void k_copy_counters(const DevCounters *__restrict__ d, DevCounters *__restrict__ h) {
+  const unsigned int *src = (const unsigned int *)d;
+  unsigned int *dst = (unsigned int *)h;
+  for (int i = threadIdx.x; i < (int)(sizeof(DevCounters) / 4); i += blockDim.x) dst[i] = src[i];
+}
+void p2m_launch_copy_counters(const DevCounters *d, DevCounters *h_mapped, cudaStream_t s) {
+  k_copy_counters<<<1, 64, 0, s>>>(d, h_mapped);
+}
 void p2m_launch_map_sum(const float *map, long long n, double *sum, cudaStream_t s, int nsm) {
   k_map_sum<<<grid_for(n, 256, nsm, 8), 256, 0, s>>>(map, n, sum);
 }

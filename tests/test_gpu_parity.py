@@ -278,6 +278,37 @@ def test_fixed_point_maps_are_bit_identical():
     assert_maps_close(runs[0][2], fs64[0], rel=1e-6, what="flat sky tSZ vs fp64")
 
 
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_async_readout_overlapping_the_next_paint(precision):
+    """p2m_get_healpix_async: a catalogue painted while the previous maps are copied out,
+    into alternate bound buffers, and into the same buffer (the clear and the painting
+    then wait for the copy)."""
+    torch = pytest.importorskip("torch")
+    a, b = catalogs.shell(61, 20_000), catalogs.shell(62, 15_000)
+    tab = catalogs.table()
+    ra, rb = run_oracle(a, [tab], 256)[0][0], run_oracle(b, [tab], 256)[0][0]
+    npix = 12 * 256 * 256
+    dev = [torch.empty(npix, dtype=torch.float32, device="cuda") for _ in range(2)]
+    host = [torch.empty(npix, dtype=torch.float32).pin_memory() for _ in range(5)]
+    with p2m.Painter(nside=256, precision=precision, max_records=1 << 16) as pt:
+        pt.load_table(0, tab)
+        for k, rec in enumerate((a, b, a)):  # alternate buffers; the third reuses the first
+            pt.reset()
+            pt.bind_healpix_device(0, dev[k & 1].data_ptr())
+            pt.paint_records(rec)
+            pt.healpix_async(0, host[k].data_ptr())
+        pt.reset()
+        pt.bind_healpix_device(0, dev[0].data_ptr())
+        pt.paint_records(b)
+        pt.healpix_async(0, host[3].data_ptr())
+        pt.reset()  # the same buffer stays bound
+        pt.paint_records(a)
+        pt.healpix_async(0, host[4].data_ptr())
+        pt.synchronize()
+    for h, ref in zip(host, (ra, rb, ra, rb, ra)):
+        assert_maps_close(h.numpy(), ref)
+
+
 def test_layout7_chihview_and_bad_records():
     rec = catalogs.shell(5, 20_000, nfloat=7).copy()
     rec[::997, 0] = np.nan
