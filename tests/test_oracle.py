@@ -243,3 +243,37 @@ def test_golden_fixture_regression():
     assert np.array_equal(hp, g["hp"])
     assert np.array_equal(fs, g["fs"])
     assert np.array_equal(sets[0], g["set_rec"]) and np.array_equal(sets[1], g["set_pix"])
+
+
+def test_isolated_halo_total_is_the_table_sum_over_its_disc():
+    """Self-pinned invariant: one halo's map total equals its profile summed over the
+    pixels whose centres lie inside its disc.  The pixels are found by brute force over
+    every pixel centre of the sphere (numpy, from the ring layout), and each pixel's
+    value is the table at that pixel's angle from the centre."""
+    import spectra
+    nside = 512
+    rec = np.array([[330.0, 140.0, -210.0, 100.0, 50.0, -20.0, 20.0, 0.0, 0.0, 0.0]], np.float32)
+    rec[0, 7:10] = rec[0, :3] - 0.01 * rec[0, 3:6]
+    tab = catalogs.table(nu=0.0)
+    p = oracle.params(nside=nside, npix_fs=0, maps=((0, 1),), zmax=2.0)
+    hp, _, st, sets = oracle.paint(p, [oracle.Table(tab)], rec, record_sets=True)
+    cos = oracle.Cosmo()
+    ok, q = oracle.halo_setup(cos, p, rec[0])
+    assert ok
+    xh, yh, zh, rh, chi, mh, z, T = (float(v) for v in q)
+    centre = np.array([zh, yh, xh]) / chi  # the halo loop's (x, y, z) -> (z, y, x) order
+    rings = spectra.healpix_rings(nside)
+    th = np.concatenate([np.full(len(r[1]), r[0]) for r in rings])
+    ph = np.concatenate([r[1] for r in rings])
+    v = np.stack([np.sin(th) * np.cos(ph), np.sin(th) * np.sin(ph), np.cos(th)], axis=1)
+    cross = np.linalg.norm(np.cross(v, centre / np.linalg.norm(centre)), axis=1)
+    ang = np.arctan2(cross, v @ (centre / np.linalg.norm(centre)))
+    inside = np.flatnonzero(ang < T)
+    assert 50 < inside.size < 5000
+    # no pixel centre sits on the boundary within float noise
+    assert np.min(np.abs(ang - T)) > 1e-7
+    assert np.array_equal(np.sort(sets[1]), inside)
+    tabo = oracle.Table(tab)
+    total = sum(tabo.interpolate(cos, float(ang[i]), z, mh, 1)[0] for i in inside)
+    assert hp[0].sum() == pytest.approx(total, rel=1e-5)
+    assert st["hp_updates"] == inside.size
