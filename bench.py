@@ -555,6 +555,11 @@ def run_ours(args):
     barrier()
     e2e_ms = max_over_ranks(1e3 * (time.perf_counter() - t0) / args.steps, dev)
     pt.close()
+    # the last pipelined step's maps, as they arrived in host memory, against the resident
+    # steps' maps (the same catalogue; the compensated sums agree to float rounding)
+    last = h_sets[(args.steps - 1) & 1]
+    e2e_check = max(map_errors(last[m].numpy(), maps_main[m])["max_rel_masked"]
+                    for m in range(len(MAPS)))
     # the host link alone: the same copies without the painting
     d_tmp = torch.empty_like(h_rec, device=dev)
     barrier()
@@ -640,7 +645,8 @@ def run_ours(args):
                    "pipelined": "step k's map read-back (p2m_get_healpix_async) overlaps "
                                 "step k+1's catalogue copy and paint into alternate buffers",
                    "sequential": {"value": total_halos / (e2e_seq_ms * 1e-3),
-                                  "ms_per_step": e2e_seq_ms}}}
+                                  "ms_per_step": e2e_seq_ms},
+                   "maps_vs_resident_max_rel": e2e_check}}
     # per step: the fused cut and set-up, the item kernel of the large halos, their
     # candidate counts and 3-kernel scan, the fused paint, the large-halo paint, the fold
     # of the low words, and the two counter read-outs (memsets are not kernels)

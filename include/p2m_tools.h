@@ -68,6 +68,11 @@ typedef struct p2m_tuning {
                            earlier calls') awaits painting, paint it before the next chunk is
                            ingested, so that the copies overlap the painting too; 0: paint
                            at the read-out; 1 */
+  int32_t halo_batch; /* halos per warp batch of the fused kernel, 1..32; 16 */
+  int32_t sort_halos; /* 1: paint the halos in order of their first ring (a counting sort:
+                         the set-up counts the keys, the paint scans and scatters them), so
+                         that the halos in flight cover a narrow band of the maps; 0: in
+                         catalogue order; 1 */
   float ms;           /* p2m_autotune: device time of one paint call with the choice */
 } p2m_tuning;
 int32_t p2m_get_tuning(struct p2m_ctx *ctx, p2m_tuning *out);
@@ -75,7 +80,7 @@ int32_t p2m_set_tuning(struct p2m_ctx *ctx, const p2m_tuning *t);
 /* Autotuner: paints the caller's catalogue (device records, as p2m_paint_records_device)
    with candidate launch parameters and keeps the fastest.  The search is coordinate
    descent: big_rings, then the fused kernel's grid, then the stored-item kernel's grid,
-   then its chunk.  Each candidate is timed by device events around the whole paint call
+   then its chunk, then the painting order, then the fused kernel's batch.  Each candidate is timed by device events around the whole paint call
    (reset, ingest, sweep), best of `reps`.  The maps are reset before the first and after
    the last candidate.  Writes the choice to *out when out is not NULL. */
 int32_t p2m_autotune(struct p2m_ctx *ctx, const float *d_records, int64_t nrec, int32_t nfloat,

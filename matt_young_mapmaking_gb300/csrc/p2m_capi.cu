@@ -44,7 +44,13 @@ struct p2m_ctx {
   bool th_set = false;
   float *d_tab[P2M_MAXTABLES] = {};
   float band_u = 2e-4f;
-  p2m_tuning tune = {P2M_BIG_RINGS, 8, 8, 1024, (int32_t)P2M_STREAM_CHUNK, 1, 0.0f};
+  p2m_tuning tune = {P2M_BIG_RINGS, 8, 8, 1024, (int32_t)P2M_STREAM_CHUNK, 1, 16, 1, 0.0f};
+  /* painting order (p2m_tuning.sort_halos): counting sort by first ring */
+  int *d_order = nullptr, *d_ring_key = nullptr;
+  long long cap_order = 0, cap_ring_key = 0;
+  unsigned int *d_ring_hist = nullptr;
+  long long *d_ring_off = nullptr;
+  unsigned long long *d_nbins = nullptr;
   /* outputs: hp_npix counts every cone's pixels (ncones * cone_npix) */
   long long hp_npix = 0, fs_npix = 0;
   long long cone_npix = 0;
@@ -232,6 +238,7 @@ PaintParams make_params(const p2m_ctx *ctx, int nfloat) {
   P.halos_grid = ctx->tune.halos_grid;
   P.full_grid = ctx->tune.full_grid;
   P.full_chunk = ctx->tune.full_chunk;
+  P.halo_batch = ctx->tune.halo_batch;
   P.cone_npix = ctx->cone_npix;
   if (ctx->th_set) {
     float fr;
@@ -261,6 +268,10 @@ IngestBuffers ingest_buffers(const p2m_ctx *ctx, const float *records) {
   B.set_rec = ctx->d_set_rec;
   B.set_pix = ctx->d_set_pix;
   B.set_cap = ctx->cap_set;
+  if (ctx->tune.sort_halos && ctx->d_ring_hist) {
+    B.ring_key = ctx->d_ring_key + ctx->n_halos;
+    B.ring_hist = ctx->d_ring_hist;
+  }
   return B;
 }
 
@@ -370,6 +381,18 @@ p2m_status begin_call(p2m_ctx *ctx, long long n, cudaStream_t s) {
   CK(grow(&ctx->d_nring, &ctx->cap_nring, std::max(n, 1LL)));
   CK(grow(&ctx->d_ioff, &ctx->cap_ioff, std::max(n, 1LL)));
   CK(grow(&ctx->d_halos, &ctx->cap_halos, ctx->n_halos + std::max(n, 1LL), ctx->n_halos, s));
+  if (ctx->tune.sort_halos && ctx->cfg.nside > 0) {
+    CK(grow(&ctx->d_ring_key, &ctx->cap_ring_key, ctx->n_halos + std::max(n, 1LL), ctx->n_halos, s));
+    if (!ctx->d_ring_hist) {
+      const long long nbins = 4LL * ctx->cfg.nside + 1;
+      CK(cudaMalloc((void **)&ctx->d_ring_hist, sizeof(unsigned int) * (size_t)nbins));
+      CK(cudaMemset(ctx->d_ring_hist, 0, sizeof(unsigned int) * (size_t)nbins));
+      CK(cudaMalloc((void **)&ctx->d_ring_off, sizeof(long long) * (size_t)nbins));
+      CK(cudaMalloc((void **)&ctx->d_nbins, sizeof(unsigned long long)));
+      const unsigned long long nb = (unsigned long long)nbins;
+      CK(cudaMemcpy(ctx->d_nbins, &nb, sizeof(nb), cudaMemcpyHostToDevice));
+    }
+  }
   for (int k = 0; k < P2M_NPHASE; k++) ctx->tev_used[k] = false;
   CK(cudaMemsetAsync(ctx->d_ctr, 0, CALL_CTR_BYTES, s));
   return P2M_OK;
@@ -567,8 +590,19 @@ p2m_status paint_pending(p2m_ctx *ctx, cudaStream_t s) {
     p2m_launch_scan_u32(ctx->d_counts, ctx->d_nitems, ctx->d_pix_off, &ctx->d_ctr->n_pix,
                         ctx->d_scan_tmp, s);
   }
-  TE(PH_GROUP);
   SweepBuffers W = sweep_buffers(ctx);
+  if (ctx->tune.sort_halos && ctx->d_ring_hist) {
+    /* counting sort of the halos by first ring (keys and counts came from the set-up):
+       the halos painted at any one time then cover a narrow band of rings, a contiguous
+       stretch of each map that the L2 holds */
+    const long long nbins = 4LL * ctx->cfg.nside + 1;
+    CK(grow(&ctx->d_order, &ctx->cap_order, std::max(ctx->n_halos, 1LL)));
+    p2m_launch_scan_u32(ctx->d_ring_hist, ctx->d_nbins, ctx->d_ring_off, nullptr, ctx->d_scan_tmp, s);
+    p2m_launch_ring_scatter(ctx->d_ring_key, ctx->n_halos, ctx->d_ring_off, ctx->d_order, s, ctx->nsm);
+    CK(cudaMemsetAsync(ctx->d_ring_hist, 0, sizeof(unsigned int) * (size_t)nbins, s));
+    W.order = ctx->d_order;
+  }
+  TE(PH_GROUP);
   TB(PH_PAINT); /* the paint phase spans both painting kernels */
   if (n > 0) {
     /* the large halos' items are painted on the side stream, beside the fused kernel's
@@ -770,7 +804,8 @@ void p2m_destroy(p2m_ctx *ctx) {
                   ctx->d_pix_off, ctx->d_nitems, ctx->d_sums, ctx->d_set_rec, ctx->d_set_pix,
                   ctx->d_ctr, ctx->d_prep, ctx->d_lo, ctx->d_tiles,
                   ctx->d_pre_flags, ctx->d_pre_bits, ctx->d_pre_ord, ctx->d_pre_last,
-                  ctx->d_cone_off, ctx->d_stage[0], ctx->d_stage[1]};
+                  ctx->d_cone_off, ctx->d_stage[0], ctx->d_stage[1], ctx->d_order,
+                  ctx->d_ring_key, ctx->d_ring_hist, ctx->d_ring_off, ctx->d_nbins};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   for (int m = 0; m < P2M_MAXMAPS; m++)
@@ -884,6 +919,8 @@ p2m_status p2m_reset_maps(p2m_ctx *ctx) {
   }
   if (ctx->d_fs_acc)
     CK(cudaMemsetAsync(ctx->d_fs_acc, 0, 8 * (size_t)ctx->cfg.nmaps * (size_t)ctx->fs_npix, s));
+  if (ctx->d_ring_hist)
+    CK(cudaMemsetAsync(ctx->d_ring_hist, 0, sizeof(unsigned int) * (size_t)(4LL * ctx->cfg.nside + 1), s));
   CK(cudaMemsetAsync(ctx->d_ctr, 0, sizeof(DevCounters), s));
   CK(cudaMemsetAsync(ctx->d_sums, 0, sizeof(double) * 2 * P2M_MAXMAPS, s));
   return P2M_OK;
@@ -1043,7 +1080,8 @@ bool tuning_ok(const p2m_tuning &t) {
   return t.big_rings >= 0 && t.big_rings <= 4096 && t.halos_grid >= 1 && t.halos_grid <= 16 &&
          t.full_grid >= 1 && t.full_grid <= 32 && t.full_chunk >= 32 && t.full_chunk <= 65536 &&
          t.stream_chunk >= 65536 && t.stream_chunk <= (1 << 26) &&
-         (t.stream_paint == 0 || t.stream_paint == 1);
+         (t.stream_paint == 0 || t.stream_paint == 1) && t.halo_batch >= 1 &&
+         t.halo_batch <= 32 && (t.sort_halos == 0 || t.sort_halos == 1);
 }
 
 struct EventPair {
@@ -1102,6 +1140,8 @@ int32_t p2m_autotune(p2m_ctx *ctx, const float *d_records, int64_t nrec, int32_t
   static const int kHalos[] = {1, 2, 3, 4, 8};
   static const int kFull[] = {2, 4, 8, 16};
   static const int kChunk[] = {256, 512, 1024, 2048, 4096};
+  static const int kBatch[] = {8, 16, 32};
+  static const int kSort[] = {0, 1};
   p2m_tuning best = ctx->tune;
   ST(trial(best, &best.ms));
   auto descend = [&](const int *vals, int n, int32_t p2m_tuning::*field) -> p2m_status {
@@ -1118,6 +1158,8 @@ int32_t p2m_autotune(p2m_ctx *ctx, const float *d_records, int64_t nrec, int32_t
   if (!st) st = descend(kHalos, 5, &p2m_tuning::halos_grid);
   if (!st) st = descend(kFull, 4, &p2m_tuning::full_grid);
   if (!st) st = descend(kChunk, 5, &p2m_tuning::full_chunk);
+  if (!st) st = descend(kSort, 2, &p2m_tuning::sort_halos);
+  if (!st) st = descend(kBatch, 3, &p2m_tuning::halo_batch);
   ctx->tune = best;
   if (st) return st;
   ST(p2m_reset_maps(ctx));

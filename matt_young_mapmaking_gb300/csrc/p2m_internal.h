@@ -120,6 +120,7 @@ struct PaintParams {
   int halos_grid;        /* blocks per SM of k_paint_halos */
   int full_grid;         /* blocks per SM of k_paint_full */
   int full_chunk;        /* candidates per warp chunk of k_paint_full */
+  int halo_batch;        /* halos per warp batch of k_paint_halos (1..32) */
 };
 
 /* buffers of one ingest call */
@@ -128,6 +129,8 @@ struct IngestBuffers {
   long long rec_base;   /* record index of records[0] */
   const long long *cone_off; /* ensemble: first record of each cone (call-local), ncones + 1 */
   int ncones;           /* 0: every record belongs to cone 0 */
+  int *ring_key;        /* painting order by first ring: each halo's key (call-local) ... */
+  unsigned int *ring_hist; /* ... and the keys' counts, or null when the order is not kept */
   HaloRec *halos;       /* halos[0..n_surv) of this call */
   long long halo_base;  /* global index of halos[0] */
   unsigned int *nring;  /* rings per large halo, 0 for the others */
@@ -157,6 +160,7 @@ struct SweepBuffers {
   DevCounters *ctr;
   long long *set_rec, *set_pix;
   long long set_cap;
+  const int *order;            /* halos in painting order (sorted by first ring), or null */
 };
 
 /* launchers (p2m_kernels.cu) */
@@ -188,6 +192,11 @@ void p2m_launch_map_sum(const float *map, long long n, double *sum, cudaStream_t
 /* copies the counters into mapped host memory with the SMs' stores: no copy engine, so a
    counter read never queues behind a large read-out copy */
 void p2m_launch_copy_counters(const DevCounters *d, DevCounters *h_mapped, cudaStream_t s);
+/* counting sort of halos [0, n) by first ring into order[]: the set-up stored each halo's
+   key and counted it; off holds the bins' first positions (the scan of the counts) and is
+   consumed */
+void p2m_launch_ring_scatter(const int *keys, long long n, long long *off, int *order,
+                             cudaStream_t s, int nsm);
 struct TableConsts {
   float y0, tau0, x0const, nu, alpha;
   int model;

@@ -312,6 +312,10 @@ __device__ __forceinline__ void store_halo(const PaintParams &P, const IngestBuf
   const unsigned big = nr > P.big_rings ? (unsigned)nr : 0u;
   B.nring[s] = big;
   if (big) B.ioff[s] = (long long)atomicAdd(&B.ctr->n_items, (unsigned long long)big);
+  if (B.ring_hist) { /* painting order by first ring */
+    B.ring_key[s] = H.ir_lo;
+    atomicAdd(&B.ring_hist[H.ir_lo], 1u);
+  }
   if (H.jmin <= H.jmax && H.kmin <= H.kmax) fsrows += (unsigned long long)(H.kmax - H.kmin + 1);
 }
 
@@ -1249,6 +1253,7 @@ __device__ __forceinline__ int warp_find(int key, int t) {
    banks) */
 struct WarpStage {
   HotHalo hot[32];
+  int hidx[32]; /* index of the staged halo in W.halos */
   float gzh[32], gzl[32], gsh[32], gsl[32], gph[32], gpl[32], gcs[32];
   int girlo[32];
   float iA[32], iB[32], if0[32], ihd[32];
@@ -1274,15 +1279,18 @@ __global__ void __launch_bounds__(256, P2M_HALOS_MINBLOCKS) k_paint_halos(PaintP
   PendingDeposit pend;
   pend.slot = -1;
   pend.v0 = pend.v1 = pend.o0 = pend.o1 = 0.0f;
+  const int batch = P.halo_batch;
   for (;;) {
     long long h0 = 0;
-    if (lane == 0) h0 = 32LL * (long long)atomicAdd(&W.ctr->next_unit, 1u);
+    if (lane == 0) h0 = (long long)batch * (long long)atomicAdd(&W.ctr->next_unit, 1u);
     h0 = __shfl_sync(FULL, h0, 0);
     if (h0 >= nh) break;
     int nr = 0;
     __syncwarp();
-    if (h0 + lane < nh) {
-      const HaloRec &H = W.halos[h0 + lane];
+    if (lane < batch && h0 + lane < nh) {
+      const int hi = W.order ? W.order[h0 + lane] : (int)(h0 + lane);
+      S.hidx[lane] = hi;
+      const HaloRec &H = W.halos[hi];
       int r = H.ir_hi - H.ir_lo + 1;
       if (r > 0 && r <= P.big_rings) {
         nr = r;
@@ -1344,7 +1352,7 @@ __global__ void __launch_bounds__(256, P2M_HALOS_MINBLOCKS) k_paint_halos(PaintP
         if (c < ctot) {
           RingItem ci;
           const int jj = S.ij[i];
-          ci.halo = (int)(h0 + jj);
+          ci.halo = S.hidx[jj];
           ci.ring_n0 = S.in0[i];
           ci.lo = S.ilo[i];
           ci.count = 0;
@@ -1815,6 +1823,18 @@ __global__ void k_copy_counters(const DevCounters *__restrict__ d, DevCounters *
   const unsigned int *src = (const unsigned int *)d;
   unsigned int *dst = (unsigned int *)h;
   for (int i = threadIdx.x; i < (int)(sizeof(DevCounters) / 4); i += blockDim.x) dst[i] = src[i];
+}
+__global__ void k_ring_scatter(const int *__restrict__ keys, long long n,
+                               long long *__restrict__ off, int *__restrict__ order) {
+  for (long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x; s < n;
+       s += (long long)gridDim.x * blockDim.x) {
+    const unsigned long long pos = atomicAdd((unsigned long long *)&off[keys[s]], 1ull);
+    order[pos] = (int)s;
+  }
+}
+void p2m_launch_ring_scatter(const int *keys, long long n, long long *off, int *order,
+                             cudaStream_t s, int nsm) {
+  k_ring_scatter<<<grid_for(n, 256, nsm, 8), 256, 0, s>>>(keys, n, off, order);
 }
 void p2m_launch_copy_counters(const DevCounters *d, DevCounters *h_mapped, cudaStream_t s) {
   k_copy_counters<<<1, 64, 0, s>>>(d, h_mapped);

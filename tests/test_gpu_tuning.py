@@ -38,7 +38,10 @@ def check(pt, rec, ref):
 @pytest.mark.parametrize("tune", [dict(big_rings=0, halos_grid=1, full_grid=1, full_chunk=32),
                                   dict(big_rings=16, halos_grid=2, full_grid=3, full_chunk=100),
                                   dict(big_rings=4096, halos_grid=16, full_grid=32,
-                                       full_chunk=65536)])
+                                       full_chunk=65536),
+                                  dict(sort_halos=0, halo_batch=32),
+                                  dict(sort_halos=1, halo_batch=8),
+                                  dict(sort_halos=1, halo_batch=1, big_rings=32)])
 def test_tuning_extremes_keep_parity(precision, tune):
     rec = catalogue()
     ref = run_oracle(rec, [catalogs.table(nu=0.0)], 512, maps=MAPS, zmax=6.0)
@@ -59,6 +62,7 @@ def test_autotune_choice_and_parity():
         assert t["big_rings"] in (0, 16, 32, 48, 64, 96, 128, 256)
         assert t["halos_grid"] in (1, 2, 3, 4, 8) and t["full_grid"] in (2, 4, 8, 16)
         assert t["full_chunk"] in (256, 512, 1024, 2048, 4096) and t["ms"] > 0
+        assert t["sort_halos"] in (0, 1) and t["halo_batch"] in (8, 16, 32)
         assert pt.tuning()["big_rings"] == t["big_rings"]
         assert not np.any(pt.healpix(0))  # the autotuner leaves the maps reset
         check(pt, rec, ref)
