@@ -948,7 +948,7 @@ p2m_status upload_offsets(p2m_ctx *ctx, const int64_t *offsets, int32_t ncones, 
    copied on the copy stream into one of two device staging buffers while chunk k is cut
    and set up on the context's stream.  A buffer is refilled only after the chunk that
    used it has been ingested (the cut and set-up kernel is its only reader).  From pinned
-   host memory the copies overlap the ingest; from pageable memory the driver stages each
+   host memory the copies overlap the ingest; from pageable memory the CUDA driver stages each
    copy first.  Scramble and centre need the whole catalogue in one piece: they take a
    single chunk.  With cone offsets (ensembles) each chunk gets its own clamped table. */
 p2m_status stream_host_records(p2m_ctx *ctx, const float *records, long long nrec, int nfloat,

@@ -1,5 +1,6 @@
 """Seeded synthetic catalogues and tables for the tests (the reference's own catalogue
-and tables are not available; these stand in with the BASELINE shapes)."""
+and tables are not available; these stand in with the benchmark workloads' shells, mass
+ranges and record layouts)."""
 import functools
 
 import numpy as np
