@@ -35,12 +35,12 @@ MASS = (1e12, 3e15)
 SEED = 2
 ZMAX = 6.0
 MAPS = ((0, 1), (0, 2))
-LAUNCHES_PER_STEP = 11
+LAUNCHES_PER_STEP = 15
 # DRAM bytes (read + write) per pixel update of k_paint_halos from the ncu capture
 # summarised in profiles/paint_pipeline_1e7_nside2048.md
-PAINT_DRAM_BYTES_PER_UPDATE = 96.4
+PAINT_DRAM_BYTES_PER_UPDATE = 76.4
 # L2 atomic throughput of this GB300 (sectors/s): ncu lts__t_sectors_srcunit_tex_op_atom
-# of the same capture, 32.9 sectors/ns at 8.69 % of peak sustained
+# of the same capture, 27.3 sectors/ns at 7.20 % of peak sustained
 L2_ATOMIC_SECTORS_PER_S = 3.79e11
 METRIC = "halos/sec & pixel-updates/sec at Nside=4096, 1 GB300; rel err vs FP64 oracle"
 
@@ -648,8 +648,9 @@ def run_ours(args):
                                   "ms_per_step": e2e_seq_ms},
                    "maps_vs_resident_max_rel": e2e_check}}
     # per step: the fused cut and set-up, the item kernel of the large halos, their
-    # candidate counts and 3-kernel scan, the fused paint, the large-halo paint, the fold
-    # of the low words, and the two counter read-outs (memsets are not kernels)
+    # candidate counts and 3-kernel scan, the painting order's 3-kernel scan and scatter,
+    # the fused paint, the large-halo paint, the fold of the low words, and the two
+    # counter read-outs (memsets are not kernels)
     out["gpu_launches"] = LAUNCHES_PER_STEP * args.steps
 
     if not args.no_plain and args.precision == "mixed":
