@@ -177,7 +177,10 @@ p2m_status p2m_get_flatsky(p2m_ctx *ctx, int32_t map, float *out);
    (p2m_bind_healpix_device) to the maps first.  No counterpart in the reference, which
    reads each map once at the end of its run. */
 p2m_status p2m_get_healpix_async(p2m_ctx *ctx, int32_t map, float *out);
-/* ... or device memory, ordered on `stream` (NULL = the context's stream). */
+/* ... or device memory, ordered on `stream` (NULL = the context's stream).  This one
+   does not wait for the device: an error the painting kernels raise is reported by the
+   next call that does (the next paint call, a host read-out, p2m_get_stats or
+   p2m_synchronize). */
 p2m_status p2m_get_healpix_device(p2m_ctx *ctx, int32_t map, float *d_out, void *stream);
 /* Make a caller-owned device buffer of 12*nside^2 floats (times ncones for an ensemble)
    the storage of HEALPix map `map`

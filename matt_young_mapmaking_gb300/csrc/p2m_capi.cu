@@ -283,12 +283,10 @@ p2m_status check_tables(p2m_ctx *ctx) {
   return P2M_OK;
 }
 
-p2m_status read_counters(p2m_ctx *ctx, cudaStream_t s) {
-  p2m_launch_copy_counters(ctx->d_ctr, ctx->h_ctr_dev, s);
-  CK(cudaGetLastError());
-  CK(cudaStreamSynchronize(s));
+/* reports the device error flags in the counters last copied to host memory (after a
+   wait for them); a flag stays set on the device until it is reported here */
+p2m_status check_errors(p2m_ctx *ctx, cudaStream_t s) {
   const DevCounters &h = *ctx->h_ctr;
-  /* an error flag stays set until it is reported here */
   if (h.err) CK(cudaMemsetAsync(&ctx->d_ctr->err, 0, sizeof(unsigned int), s));
   if (h.err & P2M_DEVERR_RADIUS)
     return fail(ctx, P2M_ERR_BADARG, "a halo's disc radius exceeds pi (query_disc aborts)");
@@ -297,6 +295,13 @@ p2m_status read_counters(p2m_ctx *ctx, cudaStream_t s) {
   if (h.err & P2M_DEVERR_FS_OVERFLOW)
     return fail(ctx, P2M_ERR_CAPACITY, "flat-sky row buffer overflow (maps are incomplete)");
   return P2M_OK;
+}
+
+p2m_status read_counters(p2m_ctx *ctx, cudaStream_t s) {
+  p2m_launch_copy_counters(ctx->d_ctr, ctx->h_ctr_dev, s);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(s));
+  return check_errors(ctx, s);
 }
 
 /* Everything after the per-halo set-up of one ingest call: item offsets, items, flat sky.
@@ -658,22 +663,14 @@ p2m_status sweep(p2m_ctx *ctx, cudaStream_t s) {
   }
   TE(PH_READOUT);
   CK(cudaGetLastError());
-  p2m_status st = read_counters(ctx, s);
+  /* the counters go to mapped host memory without a wait.  A device error flag raised
+     by the painting is reported by the next call that waits for the device: the next
+     ingest, a host read-out, the statistics or p2m_synchronize.  The fold and the FP64
+     read-out leave the accumulators clear either way. */
+  p2m_launch_copy_counters(ctx->d_ctr, ctx->h_ctr_dev, s);
+  CK(cudaGetLastError());
   join_out(ctx, s);
   ctx->unfolded = false;
-  if (st) {
-    /* accumulators may hold partial sums: clear them so the context stays usable */
-    if (ctx->d_acc64)
-      cudaMemsetAsync(ctx->d_acc64, 0, sizeof(double) * (size_t)ctx->cfg.nmaps * (size_t)ctx->hp_npix,
-                      ctx->stream);
-    if (ctx->d_lo) {
-      cudaMemsetAsync(ctx->d_lo, 0, sizeof(float) * (size_t)ctx->cfg.nmaps * (size_t)ctx->hp_npix,
-                      ctx->stream);
-      cudaMemsetAsync(ctx->d_tiles, 0, (size_t)((ctx->hp_npix + P2M_TILE_PIX - 1) >> P2M_TILE_SHIFT),
-                      ctx->stream);
-    }
-    return st;
-  }
   ctx->swept = true;
   return P2M_OK;
 }
@@ -1177,7 +1174,7 @@ p2m_status p2m_get_healpix_cone(p2m_ctx *ctx, int32_t cone, int32_t map, float *
   CK(cudaMemcpyAsync(out, ctx->d_out[map] + (size_t)cone * (size_t)ctx->cone_npix,
                      sizeof(float) * (size_t)ctx->cone_npix, cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
-  return P2M_OK;
+  return check_errors(ctx, ctx->stream);
 }
 
 p2m_status p2m_project_halo(p2m_ctx *ctx, float *x, float *y, float *z, const float *r,
@@ -1237,7 +1234,7 @@ p2m_status p2m_get_healpix(p2m_ctx *ctx, int32_t map, float *out) {
   CK(cudaMemcpyAsync(out, ctx->d_out[map], sizeof(float) * (size_t)ctx->hp_npix,
                      cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
-  return P2M_OK;
+  return check_errors(ctx, ctx->stream);
 }
 
 p2m_status p2m_get_healpix_async(p2m_ctx *ctx, int32_t map, float *out) {
@@ -1305,6 +1302,7 @@ p2m_status p2m_get_stats(p2m_ctx *ctx, p2m_stats *out) {
     CK(cudaGetLastError());
   }
   CK(cudaStreamSynchronize(ctx->stream));
+  ST(check_errors(ctx, ctx->stream));
   DevCounters h;
   CK(cudaMemcpy(&h, ctx->d_ctr, sizeof(h), cudaMemcpyDeviceToHost));
   double sums[2 * P2M_MAXMAPS];
@@ -1337,7 +1335,7 @@ p2m_status p2m_synchronize(p2m_ctx *ctx) {
   CK(cudaStreamSynchronize(ctx->zstream));
   CK(cudaStreamSynchronize(ctx->stream));
   if (ctx->rstream) CK(cudaStreamSynchronize(ctx->rstream));
-  return P2M_OK;
+  return check_errors(ctx, ctx->stream);
 }
 
 p2m_status p2m_get_pixel_sets(p2m_ctx *ctx, int64_t *rec, int64_t *pix, int64_t cap, int64_t *n) {
@@ -1347,6 +1345,7 @@ p2m_status p2m_get_pixel_sets(p2m_ctx *ctx, int64_t *rec, int64_t *pix, int64_t 
   CK(cudaSetDevice(ctx->cfg.device));
   ST(sweep(ctx, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
+  ST(check_errors(ctx, ctx->stream));
   DevCounters h;
   CK(cudaMemcpy(&h, ctx->d_ctr, sizeof(h), cudaMemcpyDeviceToHost));
   long long total = (long long)h.n_sets;
