@@ -1243,6 +1243,13 @@ __device__ __forceinline__ int warp_find(int key, int t) {
   return j;
 }
 
+#ifndef P2M_HALOS_CARVEOUT
+/* percent of the SM's unified L1/shared memory preferred as shared: enough for three
+   blocks' 33 KB stages, the rest stays L1 for the table and halo-record loads (measured
+   on GB300: 0.95 ms of paint at 60 % against 1.00 ms at 100 %; at 40 % a third block no
+   longer fits) */
+#define P2M_HALOS_CARVEOUT 60
+#endif
 #ifndef P2M_HALOS_MINBLOCKS
 #define P2M_HALOS_MINBLOCKS 3 /* resident blocks per SM the register budget must allow */
 #endif
@@ -1796,11 +1803,12 @@ void p2m_launch_paint_full(const PaintParams &P, const SweepBuffers &W, cudaStre
 template <int EXACT, int ACC>
 static void launch_paint_halos(const PaintParams &P, const SweepBuffers &W, cudaStream_t s,
                                int nsm) {
-  /* the shared-memory stage (32 KB per block) must not be what limits residency */
+  /* the shared-memory stage (33 KB per block) must not be what limits residency, nor
+     take the L1 the table loads use */
   static bool carveout = false;
   if (!carveout) {
     cudaFuncSetAttribute(k_paint_halos<EXACT, ACC>, cudaFuncAttributePreferredSharedMemoryCarveout,
-                         (int)cudaSharedmemCarveoutMaxShared);
+                         P2M_HALOS_CARVEOUT);
     carveout = true;
   }
   /* warps claim 32-halo batches until none is left */
