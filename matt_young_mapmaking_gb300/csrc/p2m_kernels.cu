@@ -1760,8 +1760,24 @@ void p2m_launch_pre_centre(const PaintParams &P, const float *records, long long
   k_pre_last<<<grid_for(n, 256, nsm, 8), 256, 0, s>>>(P, records, n, flags, rthmax_bits, last);
 }
 
+#ifndef P2M_CUT_CARVEOUT
+#define P2M_CUT_CARVEOUT -1 /* shared-memory carveout preference (percent; -1: the driver's) */
+#endif
+#ifndef P2M_FULL_CARVEOUT
+#define P2M_FULL_CARVEOUT -1
+#endif
+template <class K>
+static void carveout_once(K kernel, int percent, bool &done) {
+  if (done) return;
+  if (percent >= 0)
+    cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, percent);
+  done = true;
+}
+
 void p2m_launch_cut_setup(const PaintParams &P, const IngestBuffers &B, long long n,
                           cudaStream_t s, int nsm) {
+  static bool co = false;
+  carveout_once(k_cut_setup, P2M_CUT_CARVEOUT, co);
   /* one resident wave: each block streams its tiles and sets up its own survivors */
   static int per_sm = 0;
   if (!per_sm &&
@@ -1794,6 +1810,10 @@ void p2m_launch_fs(const PaintParams &P, const IngestBuffers &B, long long n_max
   else k_paint_fs<0><<<nsm * 8, 256, 0, s>>>(P, B);
 }
 void p2m_launch_paint_full(const PaintParams &P, const SweepBuffers &W, cudaStream_t s, int nsm) {
+  static bool co0 = false, co2 = false, co3 = false;
+  carveout_once(k_paint_full<0, 2>, P2M_FULL_CARVEOUT, co2);
+  carveout_once(k_paint_full<0, 3>, P2M_FULL_CARVEOUT, co3);
+  carveout_once(k_paint_full<0, 0>, P2M_FULL_CARVEOUT, co0);
   const int g = nsm * P.full_grid;
   if (P.precision == 0) k_paint_full<1, 0><<<g, 256, 0, s>>>(P, W);
   else if (P.precision == 1) k_paint_full<0, 2><<<g, 256, 0, s>>>(P, W);
