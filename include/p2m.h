@@ -124,7 +124,12 @@ p2m_status p2m_reset_maps(p2m_ctx *ctx);
 
 /* Paint nrec catalogue records (nfloat = 7 or 10 floats each, header already removed)
    held in host memory: radial cut, mass, per-halo set-up and both projections, exactly
-   the halo loop of pks2map.f90:134-303.  Accumulates into the context's maps. */
+   the halo loop of pks2map.f90:134-303.  Accumulates into the context's maps.
+   Where the reference aborts (query_disc on a disc radius above pi,
+   pixel_routines.F90:1962, called at haloproject.f90:55) the call returns an error and
+   paints none of the records of the failing ingest step (host records go in steps of
+   p2m_tuning.stream_chunk; the steps before it stay painted); the context stays
+   usable, and p2m_reset_maps starts over. */
 p2m_status p2m_paint_records(p2m_ctx *ctx, const float *records, int64_t nrec, int32_t nfloat);
 /* The pks2map command-line flags scramble and center (pks2map.f90:75-76, :162-262): 1
    gives every halo that survives the radial cut a random direction from the reference's

@@ -284,15 +284,19 @@ p2m_status check_tables(p2m_ctx *ctx) {
 }
 
 /* reports the device error flags in the counters last copied to host memory (after a
-   wait for them); a flag stays set on the device until it is reported here */
+   wait for them); a flag stays set on the device until it is reported here, and is
+   reported once: both copies are cleared */
 p2m_status check_errors(p2m_ctx *ctx, cudaStream_t s) {
-  const DevCounters &h = *ctx->h_ctr;
-  if (h.err) CK(cudaMemsetAsync(&ctx->d_ctr->err, 0, sizeof(unsigned int), s));
-  if (h.err & P2M_DEVERR_RADIUS)
+  const unsigned int err = ctx->h_ctr->err;
+  if (err) {
+    ctx->h_ctr->err = 0;
+    CK(cudaMemsetAsync(&ctx->d_ctr->err, 0, sizeof(unsigned int), s));
+  }
+  if (err & P2M_DEVERR_RADIUS)
     return fail(ctx, P2M_ERR_BADARG, "a halo's disc radius exceeds pi (query_disc aborts)");
-  if (h.err & P2M_DEVERR_ITEMS)
+  if (err & P2M_DEVERR_ITEMS)
     return fail(ctx, P2M_ERR_STATE, "candidate walk exceeded its round bound (maps are incomplete)");
-  if (h.err & P2M_DEVERR_FS_OVERFLOW)
+  if (err & P2M_DEVERR_FS_OVERFLOW)
     return fail(ctx, P2M_ERR_CAPACITY, "flat-sky row buffer overflow (maps are incomplete)");
   return P2M_OK;
 }
@@ -309,7 +313,15 @@ p2m_status read_counters(p2m_ctx *ctx, cudaStream_t s) {
 p2m_status ingest_tail(p2m_ctx *ctx, const PaintParams &P, long long n_max, cudaStream_t s) {
   IngestBuffers B = ingest_buffers(ctx, nullptr);
   /* the large halos reserved their item ranges (d_ioff, n_items) during the set-up */
-  ST(read_counters(ctx, s));
+  const p2m_status err = read_counters(ctx, s);
+  if (err) {
+    /* the call is discarded: its halos, stored past n_halos, are overwritten by the next
+       call, and they leave the first-ring counts that the next sort scans */
+    if (ctx->tune.sort_halos && ctx->d_ring_hist && ctx->h_ctr->n_surv > 0)
+      p2m_launch_ring_unhist(ctx->d_ring_key + ctx->n_halos, (long long)ctx->h_ctr->n_surv,
+                             ctx->d_ring_hist, s, ctx->nsm);
+    return err;
+  }
   long long n_halo = (long long)ctx->h_ctr->n_surv;
   long long n_items = P.nside > 0 ? (long long)ctx->h_ctr->n_items : 0;
   long long n_fs = (long long)ctx->h_ctr->n_fs_rows;

@@ -197,6 +197,9 @@ void p2m_launch_copy_counters(const DevCounters *d, DevCounters *h_mapped, cudaS
    consumed */
 void p2m_launch_ring_scatter(const int *keys, long long n, long long *off, int *order,
                              cudaStream_t s, int nsm);
+/* takes halos [0, n) of a discarded ingest back out of the first-ring counts */
+void p2m_launch_ring_unhist(const int *keys, long long n, unsigned int *hist, cudaStream_t s,
+                            int nsm);
 struct TableConsts {
   float y0, tau0, x0const, nu, alpha;
   int model;

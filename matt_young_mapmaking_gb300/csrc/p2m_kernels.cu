@@ -1864,6 +1864,16 @@ void p2m_launch_ring_scatter(const int *keys, long long n, long long *off, int *
                              cudaStream_t s, int nsm) {
   k_ring_scatter<<<grid_for(n, 256, nsm, 8), 256, 0, s>>>(keys, n, off, order);
 }
+__global__ void k_ring_unhist(const int *__restrict__ keys, long long n,
+                              unsigned int *__restrict__ hist) {
+  for (long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x; s < n;
+       s += (long long)gridDim.x * blockDim.x)
+    atomicSub(&hist[keys[s]], 1u);
+}
+void p2m_launch_ring_unhist(const int *keys, long long n, unsigned int *hist, cudaStream_t s,
+                            int nsm) {
+  k_ring_unhist<<<grid_for(n, 256, nsm, 8), 256, 0, s>>>(keys, n, hist);
+}
 void p2m_launch_copy_counters(const DevCounters *d, DevCounters *h_mapped, cudaStream_t s) {
   k_copy_counters<<<1, 64, 0, s>>>(d, h_mapped);
 }

@@ -181,6 +181,50 @@ def test_preprocess_needs_one_call():
             pt.paint_records(rec)  # two chunks of 2000 records
 
 
+def too_close_catalogue():
+    """A shell catalogue whose first halo sits 15 Mpc from the observer with
+    R_TH = 120 Mpc: 4 asin(r / chi) = 3.47 > pi, where query_disc aborts."""
+    rec = catalogs.shell(27, 2000).copy()
+    rec[0, :3] = [0.0, 0.0, 15.0]
+    rec[0, 6] = 120.0
+    rec[0, 7:10] = rec[0, :3]
+    return rec
+
+
+@pytest.mark.parametrize("precision", PRECISIONS)
+def test_disc_beyond_pi_is_an_error_and_the_context_survives(precision):
+    """The set-up kernel raises a device flag for a disc radius above pi (the oracle's
+    query_disc refuses it too); the C ABI reports it as an error of the call, which
+    paints none of its records, and the same context then paints a good catalogue like
+    the oracle, without a reset (the failed call's halos left the painting-order counts)
+    and after one."""
+    bad = too_close_catalogue()
+    p = oracle.params(nside=128, maps=((0, 1),), nfloat=10)
+    with pytest.raises(RuntimeError):
+        oracle.paint(p, [oracle.Table(catalogs.table())], bad)
+    good = bad[1:]
+    with p2m.Painter(nside=128, precision=precision, flags=FLAGS,
+                     max_records=len(bad)) as pt:
+        pt.load_table(0, catalogs.table())
+        with pytest.raises(p2m.P2MError, match="radius"):
+            pt.paint_records(bad)
+        pt.synchronize()  # the flag was reported once and cleared
+        pt.paint_records(good)
+        hp = [pt.healpix(0)]
+        sets = [pt.pixel_sets()]
+        with pytest.raises(p2m.P2MError, match="radius"):
+            pt.paint_records(bad)
+        pt.reset()
+        pt.paint_records(good)
+        hp.append(pt.healpix(0))
+        sets.append(pt.pixel_sets())
+    rhp, _, _, rsets = oracle.paint(p, [oracle.Table(catalogs.table())], good,
+                                    record_sets=True)
+    for k in range(2):
+        assert_sets_equal(sets[k], rsets)
+        assert_maps_close(hp[k], rhp[0])
+
+
 @pytest.mark.parametrize("precision", PRECISIONS)
 def test_six_maps_five_tables(precision):
     """The multi-table form: tSZ at 148, 200, 218, 353 and 545 GHz, each from its own
