@@ -59,7 +59,8 @@ int32_t p2m_map_sums_noalloc(const float *const *d_maps, int32_t nmaps, int64_t 
 typedef struct p2m_tuning {
   int32_t big_rings;  /* halos spanning more rings are painted from stored (halo, ring) items
                          by the candidate-balanced kernel (0: every halo), 0..4096; 64 */
-  int32_t halos_grid; /* blocks per SM of the fused enumerate-and-paint kernel, 1..16; 8 */
+  int32_t halos_grid; /* 128-thread blocks per SM of the fused enumerate-and-paint kernel
+                         (8 fit at once), 1..16; 8 */
   int32_t full_grid;  /* blocks per SM of the stored-item kernel, 1..32; 8 */
   int32_t full_chunk; /* candidates per warp chunk of the stored-item kernel, 32..65536; 1024 */
   int32_t stream_chunk; /* host records per chunk of the streamed ingest of p2m_paint_records

@@ -1146,7 +1146,7 @@ int32_t p2m_autotune(p2m_ctx *ctx, const float *d_records, int64_t nrec, int32_t
     return P2M_OK;
   };
   static const int kBig[] = {0, 16, 32, 48, 64, 96, 128, 256};
-  static const int kHalos[] = {1, 2, 3, 4, 8};
+  static const int kHalos[] = {2, 4, 6, 8, 16};
   static const int kFull[] = {2, 4, 8, 16};
   static const int kChunk[] = {256, 512, 1024, 2048, 4096};
   static const int kBatch[] = {8, 16, 32};

@@ -1244,14 +1244,25 @@ __device__ __forceinline__ int warp_find(int key, int t) {
 }
 
 #ifndef P2M_HALOS_CARVEOUT
-/* percent of the SM's unified L1/shared memory preferred as shared: enough for three
-   blocks' 33 KB stages, the rest stays L1 for the table and halo-record loads (measured
-   on GB300: 0.95 ms of paint at 60 % against 1.00 ms at 100 %; at 40 % a third block no
-   longer fits) */
+/* percent of the SM's unified L1/shared memory preferred as shared: enough for eight
+   blocks' 17 KB stages, the rest stays L1 for the table and halo-record loads (measured
+   on GB300: the same paint time at 60 % and 70 %, 3 % slower at 50 %, 16 % slower at
+   100 %) */
 #define P2M_HALOS_CARVEOUT 60
 #endif
+#ifndef P2M_PEND_DEPTH
+#define P2M_PEND_DEPTH 1 /* rounds of candidates whose atomics are in flight before their
+                            TwoSum is finished (compensated path) */
+#endif
+#ifndef P2M_HALOS_THREADS
+/* threads per block of k_paint_halos (a multiple of 32).  128-thread blocks, 8 of them
+   per SM at 64 registers, keep 32 warps resident: measured 6 % faster painting than 24
+   warps of 256-thread blocks at 80 registers, although the 64-register build spills a
+   few words */
+#define P2M_HALOS_THREADS 128
+#endif
 #ifndef P2M_HALOS_MINBLOCKS
-#define P2M_HALOS_MINBLOCKS 3 /* resident blocks per SM the register budget must allow */
+#define P2M_HALOS_MINBLOCKS 8 /* resident blocks per SM the register budget must allow */
 #endif
 
 /* per-warp shared-memory stage of the fused painter: the disc geometry and
@@ -1275,17 +1286,20 @@ struct WarpStage {
    finding its item with a 32-wide search.  Nothing goes to global memory between the
    stages. */
 template <int EXACT, int ACC>
-__global__ void __launch_bounds__(256, P2M_HALOS_MINBLOCKS) k_paint_halos(PaintParams P,
-                                                                         SweepBuffers W) {
-  __shared__ WarpStage s_stage[8];
+__global__ void __launch_bounds__(P2M_HALOS_THREADS, P2M_HALOS_MINBLOCKS)
+    k_paint_halos(PaintParams P, SweepBuffers W) {
+  __shared__ WarpStage s_stage[P2M_HALOS_THREADS / 32];
   const int lane = threadIdx.x & 31;
-  WarpStage &S = s_stage[(threadIdx.x >> 5) & 7];
+  WarpStage &S = s_stage[threadIdx.x >> 5];
   const long long nh = W.n_halos;
   unsigned int nupd = 0, nrc = 0;
   unsigned long long ncand = 0;
-  PendingDeposit pend;
-  pend.slot = -1;
-  pend.v0 = pend.v1 = pend.o0 = pend.o1 = 0.0f;
+  PendingDeposit pend[P2M_PEND_DEPTH];
+#pragma unroll
+  for (int q = 0; q < P2M_PEND_DEPTH; q++) {
+    pend[q].slot = -1;
+    pend[q].v0 = pend[q].v1 = pend[q].o0 = pend[q].o1 = 0.0f;
+  }
   const int batch = P.halo_batch;
   for (;;) {
     long long h0 = 0;
@@ -1375,14 +1389,20 @@ __global__ void __launch_bounds__(256, P2M_HALOS_MINBLOCKS) k_paint_halos(PaintP
                                   ACC == 2 ? &nd : nullptr);
         }
         if (ACC == 2) {
-          finish_pending(W, pend); /* the previous candidate's adds have returned by now */
-          pend = nd;
+          /* the oldest round's adds have returned by now */
+          finish_pending(W, pend[0]);
+#pragma unroll
+          for (int q = 0; q + 1 < P2M_PEND_DEPTH; q++) pend[q] = pend[q + 1];
+          pend[P2M_PEND_DEPTH - 1] = nd;
         }
       }
       if (lane == 0) ncand += (unsigned long long)ctot;
     }
   }
-  if (ACC == 2) finish_pending(W, pend);
+  if (ACC == 2) {
+#pragma unroll
+    for (int q = 0; q < P2M_PEND_DEPTH; q++) finish_pending(W, pend[q]);
+  }
   warp_count(&W.ctr->hp_updates, nupd);
   warp_count(&W.ctr->n_recheck, nrc);
   warp_count(&W.ctr->n_cand, ncand);
@@ -1832,7 +1852,7 @@ static void launch_paint_halos(const PaintParams &P, const SweepBuffers &W, cuda
     carveout = true;
   }
   /* warps claim 32-halo batches until none is left */
-  k_paint_halos<EXACT, ACC><<<nsm * P.halos_grid, 256, 0, s>>>(P, W);
+  k_paint_halos<EXACT, ACC><<<nsm * P.halos_grid, P2M_HALOS_THREADS, 0, s>>>(P, W);
 }
 void p2m_launch_paint_halos(const PaintParams &P, const SweepBuffers &W, cudaStream_t s, int nsm) {
   if (P.precision == 0) launch_paint_halos<1, 0>(P, W, s, nsm);
