@@ -269,6 +269,45 @@ def test_reset_discards_streamed_unread_paint(precision):
     assert_maps_close(hp, rhp[0])
 
 
+def test_reset_clears_every_painted_tile():
+    """A reset clears everything painted before it.  Catalogues on opposite sides of the
+    sky and a full-sky one are painted in turn, with resets, read-outs between paints
+    and a bound buffer that starts out holding garbage; every read-out equals the
+    oracle's map of what was painted since the last reset."""
+    torch = pytest.importorskip("torch")
+    a = catalogs.cone(63, 20_000, (1.0, 0.0, 0.0), 30.0)
+    b = catalogs.cone(64, 20_000, (-1.0, 0.0, 0.0), 30.0)
+    c = catalogs.shell(65, 10_000)
+    tab = catalogs.table()
+    ra, rb, rc = (run_oracle(r, [tab], 256)[0][0] for r in (a, b, c))
+    assert np.abs(ra).max() > 0 and np.abs(rb).max() > 0
+    assert not np.any((ra != 0) & (rb != 0))  # disjoint skies
+    npix = 12 * 256 * 256
+    with p2m.Painter(nside=256, precision="mixed", max_records=1 << 16) as pt:
+        pt.load_table(0, tab)
+        for rec, ref in ((a, ra), (b, rb), (c, rc), (a, ra), (b, rb)):
+            pt.reset()
+            pt.paint_records(rec)
+            assert_maps_close(pt.healpix(0), ref)
+        pt.reset()
+        pt.paint_records(a)
+        assert_maps_close(pt.healpix(0), ra)
+        pt.paint_records(b)  # more painting after a read-out, then a reset
+        assert_maps_close(pt.healpix(0), ra + rb)
+        pt.reset()
+        pt.paint_records(c)
+        assert_maps_close(pt.healpix(0), rc)
+        dev = torch.full((npix,), 7.0, dtype=torch.float32, device="cuda")
+        for k, (rec, ref) in enumerate(((a, ra), (b, rb), (a, ra))):
+            pt.reset()
+            if k == 0:
+                pt.bind_healpix_device(0, dev.data_ptr())
+            pt.paint_records(rec)
+            pt.healpix_device(0, dev.data_ptr())
+            pt.synchronize()
+            assert_maps_close(dev.cpu().numpy(), ref)
+
+
 @pytest.mark.parametrize("model", [1, 2, 3])
 def test_profile_models_and_redshift_cuts(model):
     """Each pressure-profile model (its overdensity enters the per-halo mass conversion,
