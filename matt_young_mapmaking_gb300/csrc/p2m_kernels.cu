@@ -40,6 +40,26 @@ __device__ void block_count(unsigned long long *ctr, unsigned long long v) {
   }
 }
 
+/* *ctr += v over the warp's active lanes with one atomic; returns this lane's place
+   (the old value plus the v of the active lanes below it) */
+__device__ __forceinline__ unsigned long long warp_reserve(unsigned long long *ctr,
+                                                           unsigned long long v) {
+  const unsigned mask = __activemask();
+  const int lane = threadIdx.x & 31;
+  unsigned long long below = 0, tot = 0;
+  for (unsigned m = mask; m;) {
+    const int src = __ffs(m) - 1;
+    m &= m - 1;
+    const unsigned long long x = __shfl_sync(mask, v, src);
+    if (src < lane) below += x;
+    tot += x;
+  }
+  const int leader = __ffs(mask) - 1;
+  unsigned long long base = 0;
+  if (lane == leader && tot) base = atomicAdd(ctr, tot);
+  return __shfl_sync(mask, base, leader) + below;
+}
+
 __device__ __forceinline__ bool p2m_isfinite(float x) { return fabsf(x) <= 3.4028234e38f; }
 
 /* chord^2 of an angle a (radians): 4 sin^2(a/2); a >= pi covers the sphere */
@@ -306,12 +326,13 @@ __device__ __forceinline__ void store_halo(const PaintParams &P, const IngestBuf
                                            const HaloRec &H, unsigned long long &fsrows) {
   B.halos[s] = H;
   /* items are made at ingest for the large halos only; the sweep enumerates the others.
-     A large halo reserves its items' place with one atomic add (they are rare, a few per
-     thousand halos, so the reservations hardly contend) */
+     The warp reserves its large halos' item ranges with one atomic add (with big_rings
+     0, as the plain FP64 path runs, every halo is large) */
   int nr = H.ir_hi - H.ir_lo + 1;
   const unsigned big = nr > P.big_rings ? (unsigned)nr : 0u;
   B.nring[s] = big;
-  if (big) B.ioff[s] = (long long)atomicAdd(&B.ctr->n_items, (unsigned long long)big);
+  const unsigned long long at = warp_reserve(&B.ctr->n_items, big);
+  if (big) B.ioff[s] = (long long)at;
   if (B.ring_hist) { /* painting order by first ring */
     B.ring_key[s] = H.ir_lo;
     atomicAdd(&B.ring_hist[H.ir_lo], 1u);
@@ -632,8 +653,31 @@ __device__ __forceinline__ RingItem make_item(const PaintParams &P, const DiscGe
   return it;
 }
 
-/* one warp expands 32 consecutive halos into their (halo, ring) items; only the large
-   halos have rings here (nring 0 for the others) */
+/* warp-wide inclusive prefix sum */
+__device__ __forceinline__ int warp_incl_scan(int v) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    int y = __shfl_up_sync(FULL, v, o);
+    if (lane >= o) v += y;
+  }
+  return v;
+}
+
+/* largest lane j with key_j <= t, for keys non-decreasing over the lanes (key_0 <= t) */
+__device__ __forceinline__ int warp_find(int key, int t) {
+  int j = 0;
+#pragma unroll
+  for (int step = 16; step > 0; step >>= 1) {
+    int o = __shfl_sync(FULL, key, j + step);
+    if (o <= t) j += step;
+  }
+  return j;
+}
+
+/* one warp expands 32 consecutive halos into their (halo, ring) items, 32 items at a
+   time over the warp's flattened ring list; only the large halos have rings here
+   (nring 0 for the others) */
 __global__ void __launch_bounds__(256) k_items(PaintParams P, IngestBuffers B) {
   const long long n = (long long)B.ctr->n_surv;
   const int lane = threadIdx.x & 31;
@@ -641,18 +685,18 @@ __global__ void __launch_bounds__(256) k_items(PaintParams P, IngestBuffers B) {
   const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
   for (long long h0 = warp * 32; h0 < n; h0 += nwarps * 32) {
     const long long h = h0 + lane;
-    /* the warp makes the items of each large halo of its 32 in turn, one ring per lane */
-    unsigned big = __ballot_sync(FULL, h < n && B.nring[h] > 0);
-    while (big) {
-      const int j = __ffs(big) - 1;
-      big &= big - 1;
-      const long long hh = h0 + j;
-      const HaloRec &H = B.halos[hh];
-      const long long off = B.ioff[hh];
-      const int cnt = (int)B.nring[hh];
-      const DiscGeom g = geom_of(H);
-      for (int t = lane; t < cnt; t += 32)
-        B.items[off + t] = make_item(P, g, (int)(B.halo_base + hh), H.ir_lo + t);
+    const int nr = h < n ? (int)B.nring[h] : 0;
+    const int rx = warp_incl_scan(nr);
+    const int rel = rx - nr, total = __shfl_sync(FULL, rx, 31);
+    for (int t0 = 0; t0 < total; t0 += 32) {
+      const int t = t0 + lane;
+      const int j = warp_find(rel, t);
+      const int r = t - __shfl_sync(FULL, rel, j);
+      if (t < total) {
+        const long long hh = h0 + j;
+        const HaloRec &H = B.halos[hh];
+        B.items[B.ioff[hh] + r] = make_item(P, geom_of(H), (int)(B.halo_base + hh), H.ir_lo + r);
+      }
     }
   }
 }
@@ -1219,28 +1263,6 @@ __global__ void __launch_bounds__(256) k_paint_full(PaintParams P, SweepBuffers 
   warp_count(&W.ctr->hp_updates, nupd);
   warp_count(&W.ctr->n_recheck, nrc);
   warp_count(&W.ctr->n_cand, ncand);
-}
-
-/* warp-wide inclusive prefix sum */
-__device__ __forceinline__ int warp_incl_scan(int v) {
-  const int lane = threadIdx.x & 31;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    int y = __shfl_up_sync(FULL, v, o);
-    if (lane >= o) v += y;
-  }
-  return v;
-}
-
-/* largest lane j with key_j <= t, for keys non-decreasing over the lanes (key_0 <= t) */
-__device__ __forceinline__ int warp_find(int key, int t) {
-  int j = 0;
-#pragma unroll
-  for (int step = 16; step > 0; step >>= 1) {
-    int o = __shfl_sync(FULL, key, j + step);
-    if (o <= t) j += step;
-  }
-  return j;
 }
 
 #ifndef P2M_HALOS_CARVEOUT
