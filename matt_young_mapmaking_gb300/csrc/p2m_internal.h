@@ -13,7 +13,7 @@
  *   k_paint_fs flat-sky rows (exact float sequence of the reference)
  * Sweep:
  *   k_paint_halos  the other halos, enumeration fused with painting: a warp builds the
- *              ring spans of 32 halos in registers and paints their candidates
+ *              ring spans of a batch of halos in registers and paints their candidates
  *   scan + k_paint_full  the large halos' items, load-balanced over candidate pixels
  *   read-out   mixed precision: the maps hold the high words of a compensated sum and
  *              k_fold_lo adds the sparse low words; FP64 accumulation: k_finalize_full

@@ -2,8 +2,9 @@
  * p2m_kernels.cu -- sm_103a kernels of the halo painter (pipeline in p2m_internal.h).
  *
  * The bulk of the halos is enumerated and painted by one fused kernel: a warp builds
- * the (halo, ring) candidate spans of 32 halos in registers and paints their candidate
- * pixels 32 at a time, so no per-item data goes through memory.  Halos spanning many
+ * the (halo, ring) candidate spans of a batch of halos (up to 32, in order of their
+ * first ring) in registers and paints their candidate pixels 32 at a time, so no
+ * per-item data goes through memory.  Halos spanning many
  * rings are load-balanced at the level of candidate pixels instead: their spans are
  * stored and prefix-summed, and each warp walks a contiguous range of the candidate
  * space.  Mixed precision accumulates into the float maps with the exact rounding
@@ -1288,7 +1289,7 @@ __global__ void __launch_bounds__(256) k_paint_full(PaintParams P, SweepBuffers 
 #endif
 
 /* per-warp shared-memory stage of the fused painter: the disc geometry and
-   interpolation fields of the warp's 32 halos, and the 32 (halo, ring) items of the
+   interpolation fields of the warp's batch of halos, and the 32 (halo, ring) items of the
    current round (structure of arrays: lanes reading different entries hit different
    banks) */
 struct WarpStage {
@@ -1302,8 +1303,9 @@ struct WarpStage {
 };
 
 /* Enumeration fused with painting for the halos spanning at most big_rings rings.
-   A warp claims 32 consecutive halos, stages their fields and prefix-sums their ring
-   counts; each lane builds the candidate span of one (halo, ring) item and stages it;
+   A warp claims a batch of halo_batch halos (consecutive in painting order), stages
+   their fields and prefix-sums their ring counts; each lane builds the candidate span
+   of one (halo, ring) item and stages it;
    the warp prefix-sums the spans and paints their candidates 32 at a time, each lane
    finding its item with a 32-wide search.  Nothing goes to global memory between the
    stages. */
