@@ -1519,7 +1519,12 @@ __global__ void __launch_bounds__(256) k_finalize_full(const double *acc, long l
    (out = RN(hi + lo)) and clears them.  A warp reads the flags of 32 consecutive tiles
    and visits the flagged ones (one pixel per lane), up to four tiles with all their loads
    in flight at once for the usual two maps */
-__global__ void __launch_bounds__(256) k_fold_lo(SweepBuffers W, int nmaps) {
+#ifndef P2M_FOLD_MINBLOCKS
+/* 4 resident blocks per SM (64 registers, no spills) keep more tiles' loads in flight than
+   the 3 that 80 registers allow: fold 0.136 ms instead of 0.153 ms at Nside 4096 */
+#define P2M_FOLD_MINBLOCKS 4
+#endif
+__global__ void __launch_bounds__(256, P2M_FOLD_MINBLOCKS) k_fold_lo(SweepBuffers W, int nmaps) {
   const int lane = threadIdx.x & 31;
   const long long ntiles = (W.npix + P2M_TILE_PIX - 1) >> P2M_TILE_SHIFT;
   const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
