@@ -60,7 +60,7 @@ def test_autotune_choice_and_parity():
     with painter("mixed") as pt:
         t = pt.autotune(d.data_ptr(), len(rec), 10, reps=2)
         assert t["big_rings"] in (0, 16, 32, 48, 64, 96, 128, 256)
-        assert t["halos_grid"] in (1, 2, 3, 4, 8) and t["full_grid"] in (2, 4, 8, 16)
+        assert t["halos_grid"] in (2, 4, 6, 8, 16) and t["full_grid"] in (2, 4, 8, 16)
         assert t["full_chunk"] in (256, 512, 1024, 2048, 4096) and t["ms"] > 0
         assert t["sort_halos"] in (0, 1) and t["halo_batch"] in (8, 16, 32)
         assert pt.tuning()["big_rings"] == t["big_rings"]
