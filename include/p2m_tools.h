@@ -134,8 +134,10 @@ int32_t p2m_cl_flatsky(int32_t device, const float *map_a, const float *map_b, i
                        double *cl_aa, double *cl_ab, double *cl_bb, int64_t *nmodes);
 
 /* Self-test of the single-precision math the kernels use (fn: 0 log, 1 exp, 2 pow,
-   3 asin, 4 atan, 5 sin, 6 cos, 7 tan) evaluated on the GPU over n device floats;
-   d_y is read only for pow.  Synchronous.  Returns 0 or a CUDA error code. */
+   3 asin, 4 atan, 5 sin, 6 cos, 7 tan; 8 the fixed-point sum of P2M_PREC_FIXED:
+   x and y each rounded to a multiple of 2^-56, added as integers and rounded back to
+   float) evaluated on the GPU over n device floats; d_y is read only for pow and 8.
+   Synchronous.  Returns 0 or a CUDA error code. */
 int32_t p2m_fmath_eval_device(int32_t device, int32_t fn, const float *d_x, const float *d_y,
                               float *d_out, int64_t n);
 

@@ -27,9 +27,6 @@
 #include "p2m_scalar.h"
 
 #define P2M_STREAM_CHUNK (1LL << 22) /* host records per streamed ingest chunk */
-/* the fixed-point accumulator of P2M_PREC_FIXED: integer units of 2^-56 */
-#define P2M_FIXED_ONE 0x1p56
-#define P2M_FIXED_UNIT 0x1p-56
 #define P2M_BIG_RINGS 64      /* default: halos spanning more rings go through the item buffer */
 #define P2M_TILE_SHIFT 5      /* compensated path: a flagged tile is 32 pixels (128 bytes) */
 #define P2M_TILE_PIX (1 << P2M_TILE_SHIFT)

@@ -754,6 +754,55 @@ __device__ __forceinline__ HotHalo hot_of(const HaloRec &H) {
   return h;
 }
 
+/* The 64-bit fixed point of P2M_PREC_FIXED (unit 2^-56) converted with integer operations
+   only: the FP64 units of this GPU run at a small fraction of the FP32 rate, and a pass
+   converting every pixel of the maps through them took twice its memory time.
+   float_to_fixed(v) = v 2^56 rounded to the nearest integer, ties to even (what
+   __double2ll_rn((double)v * 2^56) gives for |v| < 128); fixed_to_float(q) = q 2^-56
+   rounded to the nearest float, ties to even. */
+__device__ __forceinline__ long long float_to_fixed(float v) {
+  const unsigned int b = __float_as_uint(v);
+  const int ex = (int)((b >> 23) & 0xffu);
+  if (ex == 0) return 0; /* zero or subnormal: below half a unit */
+  const unsigned long long m = (unsigned long long)((b & 0x7fffffu) | 0x800000u);
+  const int sh = ex - 94; /* v 2^56 = m 2^sh */
+  unsigned long long q;
+  if (sh > 39) {
+    q = 0x7fffffffffffffffull; /* |v| >= 128: outside the fixed-point range */
+  } else if (sh >= 0) {
+    q = m << sh;
+  } else if (sh < -25) {
+    q = 0; /* m 2^sh < 1/4 */
+  } else {
+    const int r = -sh;
+    q = m >> r;
+    const unsigned long long rem = m & ((1ull << r) - 1), half = 1ull << (r - 1);
+    if (rem > half || (rem == half && (q & 1ull))) q++;
+  }
+  return (b >> 31) ? -(long long)q : (long long)q;
+}
+__device__ __forceinline__ float fixed_to_float(long long q) {
+  if (q == 0) return 0.0f;
+  const unsigned int sign = q < 0 ? 0x80000000u : 0u;
+  const unsigned long long m = q < 0 ? 0ull - (unsigned long long)q : (unsigned long long)q;
+  int e = 63 - __clzll((long long)m); /* m in [2^e, 2^(e+1)) */
+  unsigned long long top;
+  if (e > 23) {
+    const int r = e - 23;
+    top = m >> r;
+    const unsigned long long rem = m & ((1ull << r) - 1), half = 1ull << (r - 1);
+    if (rem > half || (rem == half && (top & 1ull))) top++;
+    if (top >> 24) { /* rounded up to the next power of two */
+      top >>= 1;
+      e++;
+    }
+  } else {
+    top = m << (23 - e);
+  }
+  /* q 2^-56 = 1.f 2^(e - 56): a normal float for every e in 0..64 */
+  return __uint_as_float(sign | ((unsigned int)(e - 56 + 127) << 23) | (unsigned int)(top & 0x7fffffu));
+}
+
 /* adds one pixel's values (nmaps of them) at slot `slot`.  ACC 0: FP64 accumulator
    (fire-and-forget red.add.f64); ACC 1: two-float (hi, lo) FP32 accumulator, hi by an
    atomic add that returns the old value, lo the exact TwoSum rounding error; ACC 2:
@@ -795,7 +844,7 @@ __device__ __forceinline__ void accumulate_vals(const PaintParams &P, void *acc,
 #pragma unroll
     for (int m = 0; m < P2M_MAXMAPS; m++)
       if (m < P.nmaps && vals[m] != 0.0f)
-        atomicAdd(a + m, (unsigned long long)__double2ll_rn((double)vals[m] * P2M_FIXED_ONE));
+        atomicAdd(a + m, (unsigned long long)float_to_fixed(vals[m]));
   } else {
     float *a = (float *)acc + 2 * slot * P.nmaps;
     float olds[P2M_MAXMAPS];
@@ -1446,17 +1495,18 @@ __global__ void __launch_bounds__(256) k_item_counts(const RingItem *items, long
    at a fraction of the HBM rate of a read pass followed by a separate clear (measured on
    GB300: 1.0 TB/s against 6.8 TB/s + a 7.7 TB/s memset) */
 template <int FIXED>
-__device__ __forceinline__ double2 acc_pair(const double *acc, long long p) {
+__device__ __forceinline__ float2 acc_pair(const double *acc, long long p) {
   if (FIXED) {
     const longlong2 q = __ldcs((const longlong2 *)acc + p);
-    return make_double2((double)q.x * P2M_FIXED_UNIT, (double)q.y * P2M_FIXED_UNIT);
+    return make_float2(fixed_to_float(q.x), fixed_to_float(q.y));
   }
-  return __ldcs((const double2 *)acc + p);
+  const double2 d = __ldcs((const double2 *)acc + p);
+  return make_float2((float)d.x, (float)d.y);
 }
 template <int FIXED>
-__device__ __forceinline__ double acc_one(const double *acc, long long i) {
-  if (FIXED) return (double)__ldcs((const long long *)acc + i) * P2M_FIXED_UNIT;
-  return __ldcs(acc + i);
+__device__ __forceinline__ float acc_one(const double *acc, long long i) {
+  if (FIXED) return fixed_to_float(__ldcs((const long long *)acc + i));
+  return (float)__ldcs(acc + i);
 }
 
 /* FIXED 1: the accumulator holds 64-bit fixed-point sums (unit 2^-56) */
@@ -1469,7 +1519,7 @@ __global__ void __launch_bounds__(256) k_finalize_full(const double *acc, long l
   const long long stride = (long long)gridDim.x * blockDim.x;
   if (nmaps == 2) {
     for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < npix; p += 4 * stride) {
-      double2 a[4];
+      float2 a[4];
 #pragma unroll
       for (int u = 0; u < 4; u++)
         if (p + u * stride < npix) a[u] = acc_pair<FIXED>(acc, p + u * stride);
@@ -1477,7 +1527,7 @@ __global__ void __launch_bounds__(256) k_finalize_full(const double *acc, long l
       for (int u = 0; u < 4; u++) {
         long long q = p + u * stride;
         if (q >= npix) break;
-        float v0 = (float)a[u].x, v1 = (float)a[u].y;
+        float v0 = a[u].x, v1 = a[u].y;
         if (accumulate) {
           v0 = __fadd_rn(o0[q], v0);
           v1 = __fadd_rn(o1[q], v1);
@@ -1496,13 +1546,13 @@ __global__ void __launch_bounds__(256) k_finalize_full(const double *acc, long l
       const int np = (int)(npix - base < 256 ? npix - base : 256);
       const int n = np * nmaps;
       const double *a = acc + base * nmaps;
-      double r[P2M_MAXMAPS];
+      float r[P2M_MAXMAPS];
 #pragma unroll
       for (int k = 0; k < P2M_MAXMAPS; k++)
         if (t + k * 256 < n) r[k] = acc_one<FIXED>(a, t + k * 256);
 #pragma unroll
       for (int k = 0; k < P2M_MAXMAPS; k++)
-        if (t + k * 256 < n) sv[t + k * 256] = (float)r[k];
+        if (t + k * 256 < n) sv[t + k * 256] = r[k];
       __syncthreads();
       if (t < np)
         for (int m = 0; m < nmaps; m++) {
@@ -1624,7 +1674,7 @@ __global__ void __launch_bounds__(256) k_finalize_fs(const void *acc, long long 
     if (PREC == 0) {
       v = (float)((const double *)acc)[p * nmaps + map];
     } else if (PREC == 3) {
-      v = (float)((double)((const long long *)acc)[p * nmaps + map] * P2M_FIXED_UNIT);
+      v = fixed_to_float(((const long long *)acc)[p * nmaps + map]);
     } else {
       float2 a = ((const float2 *)acc)[p * nmaps + map];
       v = __fadd_rn(a.x, a.y);
@@ -1743,6 +1793,7 @@ __global__ void k_fmath_eval(int fn, const float *x, const float *y, float *out,
     case 4: r = p2m_atanf(a); break;
     case 5: r = p2m_sinf(a); break;
     case 6: r = p2m_cosf(a); break;
+    case 8: r = fixed_to_float(float_to_fixed(a) + float_to_fixed(b)); break;
     default: r = p2m_tanf(a); break;
   }
   out[i] = r;

@@ -483,6 +483,34 @@ def test_fmath_bit_identical_host_device():
         assert same.all(), "fn %d: %d of %d differ" % (fn, (~same).sum(), n)
 
 
+def test_fixed_point_conversions_are_exact():
+    """P2M_PREC_FIXED's integer conversions: each value rounded to a multiple of 2^-56
+    (ties to even), the integers added, the sum rounded to the nearest float (ties to
+    even), against the same arithmetic in numpy: random magnitudes from below half a
+    unit to 50, exact ties, opposite values and zeros."""
+    import torch
+    rng = np.random.default_rng(12)
+    n = 1 << 18
+    mag = 10.0 ** rng.uniform(-18.0, 1.7, n)
+    a = (mag * rng.choice([-1.0, 1.0], n)).astype(np.float32)
+    b = (10.0 ** rng.uniform(-18.0, 1.7, n) * rng.choice([-1.0, 1.0], n)).astype(np.float32)
+    k = rng.integers(0, 1 << 20, n // 8)
+    a[: n // 8] = ((2 * k + 1) * 2.0 ** -57).astype(np.float32)  # a 2^56 = k + 1/2
+    b[n // 8: n // 4] = -a[n // 8: n // 4]
+    a[n // 4: n // 4 + 64] = 0.0
+    qa = np.rint(a.astype(np.float64) * 2.0 ** 56).astype(np.int64)
+    qb = np.rint(b.astype(np.float64) * 2.0 ** 56).astype(np.int64)
+    ref = ((qa + qb).astype(np.float32) * np.float32(2.0 ** -56)).astype(np.float32)
+    lib = p2m.load_library()
+    dx, dy = torch.from_numpy(a).cuda(), torch.from_numpy(b).cuda()
+    dout = torch.empty_like(dx)
+    assert lib.p2m_fmath_eval_device(0, 8, dx.data_ptr(), dy.data_ptr(), dout.data_ptr(), n) == 0
+    dev = dout.cpu().numpy()
+    same = dev.view(np.uint32) == ref.view(np.uint32)
+    assert same.all(), "%d of %d differ, e.g. a=%r b=%r: %r vs %r" % (
+        (~same).sum(), n, a[~same][:1], b[~same][:1], dev[~same][:1], ref[~same][:1])
+
+
 @pytest.mark.parametrize("model,nu,alpha", [(1, 148.0, 0.0), (1, 0.0, 0.0), (2, 545.0, 0.0),
                                              (3, 218.0, 0.0), (1, 353.0, 1.0)])
 def test_maptable_gpu_matches_oracle(model, nu, alpha):
