@@ -14,6 +14,7 @@
 #include <stdint.h>
 
 #include <algorithm>
+#include <atomic>
 
 #include "../../include/p2m_tools.h"
 #include "p2m_internal.h"
@@ -1866,24 +1867,35 @@ void p2m_launch_pre_centre(const PaintParams &P, const float *records, long long
 #ifndef P2M_FULL_CARVEOUT
 #define P2M_FULL_CARVEOUT -1
 #endif
+/* sets a kernel's shared-memory carveout once per device (a bit per device ordinal;
+   contexts on several host threads may race to set it, which is harmless) */
 template <class K>
-static void carveout_once(K kernel, int percent, bool &done) {
-  if (done) return;
+static void carveout_once(K kernel, int percent, std::atomic<unsigned long long> &done) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return;
+  const unsigned long long bit = 1ull << (dev & 63);
+  if (done.load(std::memory_order_relaxed) & bit) return;
   if (percent >= 0)
     cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, percent);
-  done = true;
+  done.fetch_or(bit, std::memory_order_relaxed);
 }
 
 void p2m_launch_cut_setup(const PaintParams &P, const IngestBuffers &B, long long n,
                           cudaStream_t s, int nsm) {
-  static bool co = false;
+  static std::atomic<unsigned long long> co{0};
   carveout_once(k_cut_setup, P2M_CUT_CARVEOUT, co);
-  /* one resident wave: each block streams its tiles and sets up its own survivors */
-  static int per_sm = 0;
-  if (!per_sm &&
-      (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cut_setup, 256, 0) != cudaSuccess ||
-       per_sm < 1))
-    per_sm = 1;
+  /* one resident wave: each block streams its tiles and sets up its own survivors (the
+     blocks per SM, from the occupancy calculator, kept per device ordinal) */
+  static std::atomic<int> resident[64];
+  int dev = 0;
+  cudaGetDevice(&dev);
+  int per_sm = resident[dev & 63].load(std::memory_order_relaxed);
+  if (per_sm < 1) {
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cut_setup, 256, 0) != cudaSuccess ||
+        per_sm < 1)
+      per_sm = 1;
+    resident[dev & 63].store(per_sm, std::memory_order_relaxed);
+  }
   long long tiles = (n + 256LL * CUT_PER_THREAD - 1) / (256LL * CUT_PER_THREAD);
   long long g = std::min<long long>(tiles, (long long)nsm * per_sm);
   k_cut_setup<<<(int)std::max<long long>(g, 1), 256, 0, s>>>(P, B, n);
@@ -1910,7 +1922,8 @@ void p2m_launch_fs(const PaintParams &P, const IngestBuffers &B, long long n_max
   else k_paint_fs<0><<<nsm * 8, 256, 0, s>>>(P, B);
 }
 void p2m_launch_paint_full(const PaintParams &P, const SweepBuffers &W, cudaStream_t s, int nsm) {
-  static bool co0 = false, co2 = false, co3 = false;
+  static std::atomic<unsigned long long> co0{0}, co1{0}, co2{0}, co3{0};
+  carveout_once(k_paint_full<1, 0>, P2M_FULL_CARVEOUT, co1);
   carveout_once(k_paint_full<0, 2>, P2M_FULL_CARVEOUT, co2);
   carveout_once(k_paint_full<0, 3>, P2M_FULL_CARVEOUT, co3);
   carveout_once(k_paint_full<0, 0>, P2M_FULL_CARVEOUT, co0);
@@ -1923,15 +1936,11 @@ void p2m_launch_paint_full(const PaintParams &P, const SweepBuffers &W, cudaStre
 template <int EXACT, int ACC>
 static void launch_paint_halos(const PaintParams &P, const SweepBuffers &W, cudaStream_t s,
                                int nsm) {
-  /* the shared-memory stage (33 KB per block) must not be what limits residency, nor
+  /* the shared-memory stage (17 KB per block) must not be what limits residency, nor
      take the L1 the table loads use */
-  static bool carveout = false;
-  if (!carveout) {
-    cudaFuncSetAttribute(k_paint_halos<EXACT, ACC>, cudaFuncAttributePreferredSharedMemoryCarveout,
-                         P2M_HALOS_CARVEOUT);
-    carveout = true;
-  }
-  /* warps claim 32-halo batches until none is left */
+  static std::atomic<unsigned long long> co{0};
+  carveout_once(k_paint_halos<EXACT, ACC>, P2M_HALOS_CARVEOUT, co);
+  /* warps claim batches of halo_batch halos until none is left */
   k_paint_halos<EXACT, ACC><<<nsm * P.halos_grid, P2M_HALOS_THREADS, 0, s>>>(P, W);
 }
 void p2m_launch_paint_halos(const PaintParams &P, const SweepBuffers &W, cudaStream_t s, int nsm) {
