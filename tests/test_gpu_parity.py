@@ -144,6 +144,26 @@ def test_stored_item_and_fused_paths(precision, big_rings, monkeypatch):
                           sum_tol=SUM_TOL if precision == "fp64" else SUM_TOL_MIXED_FEW)
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed", "fixed"])
+@pytest.mark.parametrize("nside", [1, 2, 4, 8, 16])
+def test_small_nside(nside, precision):
+    """The smallest maps: three to 63 rings, rings of 4 pixels at the poles.  Halos 15-80
+    Mpc away have discs of tens of degrees, so that even at Nside 1 some pixel centres
+    fall inside."""
+    rec = np.concatenate([catalogs.edge_cases(),
+                          catalogs.shell(29, 3000, r=(15.0, 80.0), m=(1e13, 3e15)),
+                          catalogs.shell(30, 2000)])
+    tab = catalogs.table()
+    maps = ((0, 1), (0, 2))
+    hp, _, st, sets = run_gpu(rec, [tab], precision, nside, maps=maps)
+    rhp, _, rst, rsets = run_oracle(rec, [tab], nside, maps=maps)
+    assert_sets_equal(sets, rsets)
+    assert st["hp_updates"] == rst["hp_updates"] > 0
+    for m in range(2):
+        assert_maps_close(hp[m], rhp[m], what="map %d" % m,
+                          sum_tol=SUM_TOL if precision == "fp64" else SUM_TOL_MIXED_FEW)
+
+
 @pytest.mark.parametrize("scramble,centre,ntasks", [(1, 0, 1), (0, 1, 1), (1, 1, 1), (1, 1, 3)])
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_scramble_and_centre(scramble, centre, ntasks, precision):
