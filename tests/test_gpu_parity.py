@@ -259,6 +259,21 @@ def test_six_maps_five_tables(precision):
         assert_maps_close(hp[m], rhp[m], what="map %d" % m)
 
 
+@pytest.mark.parametrize("precision", PRECISIONS)
+def test_eight_maps_eight_tables(precision):
+    """The most maps and tables a context holds: tSZ at seven frequencies from seven
+    tables and kSZ from an eighth, with flat sky as well."""
+    rec = catalogs.cone(31, 15_000, (1.0, 0.0, 0.0), 8.0)
+    tabs = [catalogs.table(nu=nu) for nu in (100.0, 143.0, 148.0, 200.0, 218.0, 353.0, 545.0, 0.0)]
+    maps = tuple((t, 1) for t in range(7)) + ((7, 2),)
+    hp, fs, st, sets = run_gpu(rec, tabs, precision, 128, npix_fs=128, fov_deg=10.0, maps=maps)
+    rhp, rfs, rst, rsets = run_oracle(rec, tabs, 128, npix_fs=128, fov_deg=10.0, maps=maps)
+    assert_sets_equal(sets, rsets)
+    for m in range(8):
+        assert_maps_close(hp[m], rhp[m], what="map %d" % m)
+        assert_maps_close(fs[m], rfs[m], rel=1e-6, what="flat sky %d" % m)
+
+
 def test_large_flatsky_field():
     """A 1024^2 flat-sky map over 10 degrees (the flat-sky form at reduced side)."""
     rec = catalogs.cone(26, 40_000, (1.0, 0.0, 0.0), 8.0)
