@@ -38,7 +38,7 @@ MAPS = ((0, 1), (0, 2))
 LAUNCHES_PER_STEP = 15
 # DRAM bytes (read + write) per pixel update of k_paint_halos from the ncu capture
 # summarised in profiles/paint_pipeline_1e7_nside2048.md
-PAINT_DRAM_BYTES_PER_UPDATE = 78.1
+PAINT_DRAM_BYTES_PER_UPDATE = 78.0
 # L2 atomic throughput of this GB300 (sectors/s): ncu lts__t_sectors_srcunit_tex_op_atom
 # of the same capture, 27.3 sectors/ns at 7.20 % of peak sustained
 L2_ATOMIC_SECTORS_PER_S = 3.79e11
