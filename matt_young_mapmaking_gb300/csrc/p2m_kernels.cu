@@ -1862,7 +1862,8 @@ void p2m_launch_pre_centre(const PaintParams &P, const float *records, long long
 }
 
 #ifndef P2M_CUT_CARVEOUT
-#define P2M_CUT_CARVEOUT -1 /* shared-memory carveout preference (percent; -1: the driver's) */
+#define P2M_CUT_CARVEOUT -1 /* shared-memory carveout preference (percent; -1: left to the
+                               CUDA runtime's choice) */
 #endif
 #ifndef P2M_FULL_CARVEOUT
 #define P2M_FULL_CARVEOUT -1
