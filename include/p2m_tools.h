@@ -45,8 +45,10 @@ int32_t p2m_get_timings(struct p2m_ctx *ctx, double *ms, int32_t n);
    stream) before use.  For callers that may not allocate device memory (a host
    framework whose caching allocator owns the device, or a loop that cannot afford the
    device-wide synchronisation of cudaFree).  The first call on a device looks up the
-   scratch address and may load the module: make it before any stream capture.  Calls on
-   one device share the scratch, so overlapping calls race and must be serialised by the
+   scratch address and may load the module: make it before any stream capture.  That
+   address is cached per device and is not valid across a cudaDeviceReset: do not call
+   this function after the device has been reset in the same process.  Calls on one
+   device share the scratch, so overlapping calls race and must be serialised by the
    caller.  Synchronous.  nmaps > P2M_NOALLOC_MAXMAPS: P2M_ERR_CAPACITY. */
 #define P2M_NOALLOC_MAXMAPS 8
 int32_t p2m_map_sums_noalloc(const float *const *d_maps, int32_t nmaps, int64_t npix,

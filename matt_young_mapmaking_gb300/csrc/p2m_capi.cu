@@ -1421,7 +1421,7 @@ p2m_status p2m_make_maptable(int32_t device, int32_t model, float nu, float alph
   p2m_cosmo cosmo;
   std::vector<float> rofz(P2M_NZTAB), zofr(P2M_NZTAB);
   p2m_cosmo_build(&cosmo, rofz.data(), zofr.data());
-  /* maptable.f90:56-64 with cosmology.f90:231-251 constants (pi is the float literal;
+  /* maptable.f90:56-64 with cosmology.f90:11-38 constants (pi is the float literal;
      mp, mue, 1.932 and 8. are single-precision literals) */
   const double PI_D = P2M_COSMO_PI;
   const double sigmat = 6.65246e-25, me = 9.109383e-28, mp = (double)1.67e-24f, c = 2.99792458e10;

@@ -6,7 +6,7 @@
  * per-pixel quantities in single precision with the compiler runtime's float
  * intrinsics: asin (haloproject.f90:47,105-106), x**(1./3.) (pks2map.f90:298),
  * log and tan (maptable.f90:185,196-202), exp/atan/sin/x**y in the table maker
- * (maptable.f90:100-118, bbps_profile.f90:91-111, integrate_profiles.f90:173).
+ * (maptable.f90:100-118, bbps_profile.f90:91-111, integrate_profiles.f90:28,70).
  * Several of those results feed integer truncations (table indices, flat-sky box
  * bounds) and the float-rounded disc test, so two implementations that differ by one
  * ulp give visibly different maps.  Rather than depend on whichever libm or CUDA math
@@ -24,8 +24,10 @@
  *         pi/2 - atan(1/x) beyond.
  *   sin/cos/tan: x = k pi/2 + r with a three-part Cody-Waite split of pi/2 (valid for
  *         |x| < 2^12 pi/2), Taylor series for sin r and cos r on |r| <= pi/4.
- * Accuracy against correctly rounded results is tested in tests/test_fmath.py (a few
- * ulp); bit-identity between host and device is tested on the GPU.
+ * Accuracy against correctly rounded results (a few ulp) is tested by
+ * tests/test_capi_cpu.py (test_float_math_accuracy, test_pow_accuracy_and_special_cases);
+ * bit-identity between host and device by
+ * tests/test_gpu_parity.py::test_fmath_bit_identical_host_device.
  */
 #ifndef P2M_FMATH_H
 #define P2M_FMATH_H

@@ -1703,7 +1703,7 @@ __device__ float bbps_scale(int row, int i, float mh, float z) {
               p2m_powf(FADD(1.0f, z), c_bbps[row + 2][i]));
 }
 
-/* integrate_profiles.f90:155-238 (which = 1: pressure, 2: gas density) */
+/* integrate_profiles.f90:12-95 (which = 1: pressure, 2: gas density) */
 __device__ float integrate_profile(const PaintParams &P, int model, int which, float theta,
                                    float z, float mh) {
   int i = model - 1;

@@ -17,6 +17,10 @@
  *    caller's stream, before the launch;
  *  - the first call on a device does the one-time set-up (the symbol lookup, which can
  *    load the module): make it before any stream capture begins;
+ *  - the looked-up address belongs to the device's current context: after a
+ *    cudaDeviceReset (by this process or a host framework) it is stale and later calls
+ *    would write through a freed address, so the call must not be used across a reset;
+ *  - the call is synchronous: it returns after the sums have reached the host;
  *  - more than P2M_NOALLOC_MAXMAPS maps is rejected with P2M_ERR_CAPACITY.
  */
 #include <cuda_runtime.h>

@@ -17,19 +17,19 @@
 #define P2M_HP_HALFPI 1.570796326794896619231321691639751442099
 #define P2M_HP_PI 3.141592653589793238462643383279502884197
 #define P2M_HP_TWOPI 6.283185307179586476925286766559005768394
-/* cosmology.f90:226-227: the double parameter pi holds the single-precision literal */
+/* cosmology.f90:8-9: the double parameter pi holds the single-precision literal */
 #define P2M_COSMO_PI 3.1415927410125732421875
-/* cosmology.f90:231-241 */
+/* cosmology.f90:11-23 */
 #define P2M_CKMS (2.99792458e10 / 1e5)
 
 /* Background cosmology of pks2map.f90:118-128 plus the r(z), z(r) tables of
-   cosmology.f90:269-323 (serial float Euler integration). */
+   cosmology.f90:51-105 (serial float Euler integration). */
 typedef struct p2m_cosmo {
   float omegam, omegab, omegal, h, fb, rho_0, rhocrit_0, mypi;
   float drofz, dzofr;
 } p2m_cosmo;
 
-/* cosmology.f90:341-351 */
+/* cosmology.f90:123-133 */
 P2M_HD float p2m_dzdr(const p2m_cosmo *c, float z) {
   float zp1 = FADD(1.0f, z);
   float c3 = FMUL(FMUL(zp1, zp1), zp1);
@@ -38,7 +38,7 @@ P2M_HD float p2m_dzdr(const p2m_cosmo *c, float z) {
   return (float)DMUL(t, (double)s);
 }
 
-/* pks2map.f90:88,118-128 and cosmology.f90:269-323; rofz/zofr receive 10000 floats */
+/* pks2map.f90:88,118-128 and cosmology.f90:51-105; rofz/zofr receive 10000 floats */
 static inline void p2m_cosmo_build(p2m_cosmo *c, float *rofz, float *zofr) {
   c->omegam = 0.25f;
   c->omegab = 0.043f;
@@ -63,7 +63,7 @@ static inline void p2m_cosmo_build(p2m_cosmo *c, float *rofz, float *zofr) {
   }
 }
 
-/* cosmology.f90:355-399 (table minimum is 0 for both tables) */
+/* cosmology.f90:137-181 (table minimum is 0 for both tables) */
 P2M_HD float p2m_lookup(const float *tab, float dt, float x) {
   int itab = (int)FADD(FDIV(FSUB(x, 0.0f), dt), 1.0f);
   if (itab < 1) return tab[0];
@@ -72,14 +72,14 @@ P2M_HD float p2m_lookup(const float *tab, float dt, float x) {
   return FADD(FMUL(FSUB(1.0f, fint), tab[itab - 1]), FMUL(fint, tab[itab]));
 }
 
-/* cosmology.f90:403-413 */
+/* cosmology.f90:185-195 */
 P2M_HD float p2m_rhocrit(const p2m_cosmo *c, float z) {
   float zp1 = FADD(1.0f, z);
   float c3 = FMUL(FMUL(zp1, zp1), zp1);
   return FDIV(FMUL(c->rhocrit_0, FADD(FMUL(c->omegam, c3), c->omegal)), c3);
 }
 
-/* cosmology.f90:417-432 (mixed double/float expression) */
+/* cosmology.f90:199-214 (mixed double/float expression) */
 P2M_HD float p2m_deltacrit(const p2m_cosmo *c, float z) {
   float zp1 = FADD(1.0f, z);
   float c3 = FMUL(FMUL(zp1, zp1), zp1);

@@ -24,10 +24,10 @@ static const double HP_PI = 3.141592653589793238462643383279502884197;
 static const double HP_TWOPI = 6.283185307179586476925286766559005768394;
 static const double HP_TWOTHIRD = 0.6666666666666666666666666666666666666666;
 
-/* cosmology.f90:226-227: `parameter (pi = 3.14159265359)` is a default-real literal,
+/* cosmology.f90:8-9: `parameter (pi = 3.14159265359)` is a default-real literal,
    so the double parameter holds its single-precision value. */
 static const double COSMO_PI = 3.1415927410125732421875;
-/* cosmology.f90:231-241 (c, Mpc2km as double literals; 1e2 and 1e5 are exact reals) */
+/* cosmology.f90:11-23 (c, Mpc2km as double literals; 1e2 and 1e5 are exact reals) */
 static const double COSMO_C = 2.99792458e10;
 static const double COSMO_CKMS = 2.99792458e10 / 1e5;
 
@@ -40,7 +40,7 @@ static const float RMAX_DISC = 4.0f;
 
 /* ---------------------------------------------------------------- cosmology -------- */
 
-/* cosmology.f90:341-351: dzdr = h*100/ckms*sqrt(omegam*(1.+z)**3+1.-omegam) */
+/* cosmology.f90:123-133: dzdr = h*100/ckms*sqrt(omegam*(1.+z)**3+1.-omegam) */
 static float dzdr(const orc_cosmo *c, float z) {
   float zp1 = 1.0f + z;
   float c3 = (zp1 * zp1) * zp1;
@@ -48,10 +48,10 @@ static float dzdr(const orc_cosmo *c, float z) {
   double t = (double)(c->h * 100.0f) / COSMO_CKMS;
   return (float)(t * (double)s);
 }
-/* cosmology.f90:327-337 */
+/* cosmology.f90:109-119 */
 static float drdz(const orc_cosmo *c, float z) { return 1.0f / dzdr(c, z); }
 
-/* pks2map.f90:88,118-132; cosmology.f90:269-323 */
+/* pks2map.f90:88,118-132; cosmology.f90:51-105 */
 void orc_cosmo_init(orc_cosmo *c) {
   c->omegam = 0.25f;
   c->omegab = 0.043f;
@@ -79,7 +79,7 @@ void orc_cosmo_init(orc_cosmo *c) {
   }
 }
 
-/* cosmology.f90:355-375 (and rofz, :379-399): linear lookup, truncated index */
+/* cosmology.f90:137-157 (and rofz, :161-181): linear lookup, truncated index */
 static float table_lookup(const float *tab, float tmin, float dt, float x) {
   int itab = (int)(((x - tmin) / dt) + 1.0f);
   if (itab < 1) return tab[0];
@@ -93,13 +93,13 @@ float orc_zofr(const orc_cosmo *c, float r) {
 float orc_rofz(const orc_cosmo *c, float z) {
   return table_lookup(c->rofztable, c->rofztable_min, c->drofztable, z);
 }
-/* cosmology.f90:403-413 */
+/* cosmology.f90:185-195 */
 float orc_rhocrit(const orc_cosmo *c, float z) {
   float zp1 = 1.0f + z;
   float c3 = (zp1 * zp1) * zp1;
   return (c->rhocrit_0 * ((c->omegam * c3) + c->omegal)) / c3;
 }
-/* cosmology.f90:417-432: 18*pi**2 is double (pi double), 82*x and 39*x**2 are real */
+/* cosmology.f90:199-214: 18*pi**2 is double (pi double), 82*x and 39*x**2 are real */
 float orc_deltacrit(const orc_cosmo *c, float z) {
   float zp1 = 1.0f + z;
   float c3 = (zp1 * zp1) * zp1;
@@ -994,7 +994,7 @@ static float bbps_scaling(float A0, float alpham, float alphaz, float mh, float 
   return (A0 * p2m_powf(mh / 1e14f, alpham)) * p2m_powf(1.0f + z, alphaz);
 }
 
-/* integrate_profiles.f90:155-238 with bbps_profile.f90:60-180; the per-(z, mh)
+/* integrate_profiles.f90:12-95 with bbps_profile.f90:60-180; the per-(z, mh)
    profile parameters are evaluated once (identical values to per-step evaluation) */
 static float integrate_profile(const orc_cosmo *c, int model, int which, float theta,
                                float z, float mh) {
@@ -1044,7 +1044,7 @@ static float integrate_profile(const orc_cosmo *c, int model, int which, float t
   }
 }
 
-/* maptable.f90:25-146 (make_maptable.f90:120-139 sets the same cosmology) */
+/* maptable.f90:25-146 (make_maptable.f90:32-43 sets the same cosmology) */
 int64_t orc_make_maptable(int model, float nu, float alpha_cmb, int nchit, int nmht, int nrt,
                           void *image, int nthreads) {
   if (nchit <= 0) nchit = 100;
@@ -1055,7 +1055,7 @@ int64_t orc_make_maptable(int model, float nu, float alpha_cmb, int nchit, int n
   if (!image) return nbytes;
   orc_cosmo *c = (orc_cosmo *)malloc(sizeof(orc_cosmo));
   orc_cosmo_init(c);
-  /* cosmology.f90:231-251 (mp and mue are single-precision literals) */
+  /* cosmology.f90:11-38 (mp and mue are single-precision literals) */
   const double sigmat = 6.65246e-25, me = 9.109383e-28, mp = (double)1.67e-24f;
   const double msun = 1.9891e33, Mpc2km = 3.08567758e19, Mpc = 3.08567758e24,
                kpc = 3.08567758e21;

@@ -69,7 +69,7 @@ typedef struct orc_stats {
                                        largest halo before and after the rotation */
 } orc_stats;
 
-/* cosmology of pks2map.f90:118-132 and cosmology.f90:269-323 */
+/* cosmology of pks2map.f90:118-132 and cosmology.f90:51-105 */
 void orc_cosmo_init(orc_cosmo *c);
 float orc_zofr(const orc_cosmo *c, float r);
 float orc_rofz(const orc_cosmo *c, float z);

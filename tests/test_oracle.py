@@ -95,7 +95,7 @@ def test_angdist_known():
 # -------------------------------------------------------------- cosmology ----------
 
 def numpy_tables():
-    """Independent float32 restatement of cosmology.f90:269-351 (numpy scalars)."""
+    """Independent float32 restatement of cosmology.f90:51-133 (numpy scalars)."""
     om, h = f32(0.25), f32(0.7)
     ckms = 2.99792458e10 / 1e5
 

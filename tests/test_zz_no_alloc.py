@@ -42,15 +42,25 @@ def painted_maps(nside):
 
 
 def test_noalloc_sums_match_context_sums_twice():
+    import torch
     lib = p2m.load_library()
     outs, ref, npix = painted_maps(512)
     assert abs(ref[0]) > 0 and abs(ref[1]) > 0
     ptrs = [o.data_ptr() for o in outs]
-    for call in range(2):  # each call clears the shared scratch itself
+    free_before = None
+    for call in range(3):  # each call clears the shared scratch itself
         st, sums = sums_noalloc(lib, ptrs, npix)
         assert st == 0, "call %d: status %d" % (call, st)
         for m in range(2):
             assert abs(sums[m] - ref[m]) <= SUM_REL * abs(ref[m]), (call, m, sums[m], ref[m])
+        # the first call may load the module (code and the static scratch); after it,
+        # a call takes no device memory: the device's free bytes and the torch caching
+        # allocator's reserved bytes stay the same from call to call
+        free_now = (torch.cuda.mem_get_info()[0], torch.cuda.memory_reserved())
+        if free_before is not None:
+            assert free_now == free_before, "call %d: (free, reserved) %s -> %s" % (
+                call, free_before, free_now)
+        free_before = free_now
     host = [o.cpu().numpy().astype(np.float64) for o in outs]
     for m in range(2):
         assert abs(sums[m] - host[m].sum()) <= 1e-9 * np.abs(host[m]).sum()
