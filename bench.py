@@ -13,7 +13,8 @@ no explicit flush is needed between steps.
 
 --impl reference times the CPU implementation of the path on the host cores instead:
 the oracle (a C restatement of pks2map, threads as MPI ranks with private float maps and
-a final sum) on a bounded sample of the same catalogue.
+a final sum) over the same whole catalogue every step, generated and painted without
+loading the GPU library.
 """
 import argparse
 import json
@@ -36,8 +37,8 @@ SEED = 2
 ZMAX = 6.0
 MAPS = ((0, 1), (0, 2))
 LAUNCHES_PER_STEP = 15
-# DRAM bytes (read + write) per pixel update of k_paint_halos from the ncu capture
-# summarised in profiles/paint_pipeline_1e7_nside2048.md
+# DRAM bytes (read + write) per pixel update of k_paint_halos from an ncu capture of the
+# same kernel on 1e7 halos at Nside 2048 (dram__bytes_read.sum + dram__bytes_write.sum)
 PAINT_DRAM_BYTES_PER_UPDATE = 78.0
 # L2 atomic throughput of this GB300 (sectors/s): ncu lts__t_sectors_srcunit_tex_op_atom
 # of the same capture, 27.3 sectors/ns at 7.20 % of peak sustained
@@ -48,7 +49,7 @@ METRIC = "halos/sec & pixel-updates/sec at Nside=4096, 1 GB300; rel err vs FP64 
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
@@ -56,7 +57,8 @@ def parse():
     ap.add_argument("--nside", type=int, default=NSIDE)
     ap.add_argument("--no-plain", action="store_true", help="skip the FP64 drop-in comparison")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
-    ap.add_argument("--cpu-fraction", type=float, default=0.1)
+    ap.add_argument("--no-parity", action="store_true",
+                    help="skip the check of this run's maps and pixel sets against the oracle")
     ap.add_argument("--cl-lmax", type=int, default=2047,
                     help="lmax of the C_l ratio of the Nside 4096 maps (0: skip)")
     ap.add_argument("--no-precision-form", action="store_true",
@@ -358,15 +360,32 @@ def ensemble_form(device, steps=20, warmup=3):
             "per_cone_error_note": "largest over the cones of each cone's error"}
 
 
+def workload_name(n, nside):
+    """config.workload of both arms (the same string for the same workload)"""
+    return ("pks2map c2: %d halos x 10 float, shell %g-%g Mpc, masses %g-%g, HEALPix Nside %d, "
+            "tSZ y + kSZ, zmax %g" % (n, SHELL[0], SHELL[1], MASS[0], MASS[1], nside, ZMAX))
+
+
 def catalogue(n):
     import matt_young_mapmaking_gb300 as p2m
     return p2m.generate_catalogue(SEED, n, 10, r=SHELL, m=MASS)
 
 
-def oracle_table():
-    """Full-size make_maptable table (model 1, nu = 0) from the oracle, cached in /tmp."""
+def _oracle():
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
+    return oracle
+
+
+def oracle_catalogue(n):
+    """The same catalogue, generated by the oracle's restatement of the generator (the
+    CPU arm loads no library of the product)"""
+    return _oracle().generate_catalogue(SEED, n, 10, r=SHELL, m=MASS)
+
+
+def oracle_table():
+    """Full-size make_maptable table (model 1, nu = 0) from the oracle, cached in /tmp."""
+    oracle = _oracle()
     path = "/tmp/p2m_table_model1_nu0_full.bin"
     if os.path.exists(path) and os.path.getsize(path) == 36 + 8 * 100 * 100 * 200:
         with open(path, "rb") as f:
@@ -378,61 +397,134 @@ def oracle_table():
     return img
 
 
-def cpu_reference(rec, nside, threads, sample, steps=1, warmup=0):
-    """The oracle in the reference's FP32 mode with `threads` threads standing in for MPI
-    ranks: each owns private float maps, written once at set-up (the reference's
-    `hpmapl = 0`, every rank in parallel), the halo loop of every step paints the next
-    `sample` records of the catalogue (cycling through it, so no step repaints warm data)
-    split over the ranks, and the rank-order sum of the maps is timed once.  halos/s of a step extrapolates to the whole catalogue:
-    N / (set-up + reduction + paint(sample) * N / sample)."""
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle
-    tab = oracle.Table(oracle_table())
-    n = len(rec)
-    ns = max(threads, min(n, int(sample)))
+def cpu_model():
+    """The host CPU's model name (lscpu, else /proc/cpuinfo), and its core count"""
+    name = None
+    try:
+        out = subprocess.run(["lscpu"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL,
+                             text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                name = line.split(":", 1)[1].strip()
+                break
+    except Exception:
+        pass
+    if not name:
+        try:
+            with open("/proc/cpuinfo") as f:
+                info = f.read()
+            for key in ("model name", "Model", "CPU part"):
+                for line in info.splitlines():
+                    if line.startswith(key):
+                        name = line.split(":", 1)[1].strip()
+                        break
+                if name:
+                    break
+        except Exception:
+            pass
+    return "%s, %d cores" % (name or "unknown", os.cpu_count() or 1)
+
+
+def cpu_reference(rec, nside, threads, table, steps, warmup):
+    """The reference's CPU implementation of the path, timed on the host cores: the
+    oracle's halo loop in the reference's FP32 mode with `threads` threads standing in for
+    its MPI ranks.  Every step is one whole pks2map run over the whole catalogue: each
+    rank zeroes its private float maps (hpmapl = 0, pks2map.f90:278-279), paints its
+    contiguous block of records (pksc.f90:51-52), and the ranks' maps are summed in rank
+    order (MPI_Allreduce, pks2map.f90:313-314).  Returns the step times (s) and a
+    description."""
+    oracle = _oracle()
+    tab = oracle.Table(table)
     p = oracle.params(nside=nside, npix_fs=0, maps=MAPS, zmax=ZMAX, fp32=True, nfloat=10)
     t0 = time.perf_counter()
     rm = oracle.RankMaps(p, threads)
-    t_set = time.perf_counter() - t0
-    paints, st = [], None
+    t_alloc = time.perf_counter() - t0
+    times, st = [], None
     for i in range(warmup + steps):
-        a = (i * ns) % max(1, n - ns + 1)
         t0 = time.perf_counter()
-        st = rm.paint(p, [tab], rec[a:a + ns])
+        rm.zero()
+        st = rm.paint(p, [tab], rec)
+        rm.reduce(threads)
         if i >= warmup:
-            paints.append(time.perf_counter() - t0)
-    t0 = time.perf_counter()
-    rm.reduce(threads)
-    t_red = time.perf_counter() - t0
+            times.append(time.perf_counter() - t0)
     del rm
-    values = [n / (t_set + t_red + t * (n / ns)) for t in paints]
-    t_med = float(np.median(paints))
-    info = {"unit": "halos/s", "cores": threads, "kind": "port",
-            "sample": "%d of %d records per step (%.1f%%, successive slices), %d threads as ranks with "
-                      "private float maps (Nside %d, 2 maps) written at set-up and summed at "
-                      "the end; paint time scaled by %.1f, set-up %.2fs and reduction %.2fs "
-                      "counted once; median step paint %.3fs"
-                      % (ns, n, 100.0 * ns / n, threads, nside, n / ns, t_set, t_red, t_med),
-            "pixel_updates_per_s": 2 * st["hp_updates"] / t_med if t_med > 0 else None}
-    return values, info
+    t_med = float(np.median(times))
+    info = {"unit": "halos/s", "cores": threads, "kind": "port", "cpu": cpu_model(),
+            "sample": "the whole %d-record catalogue every step: %d threads as MPI ranks, each "
+                      "zeroing its private float maps (Nside %d, 2 maps), painting its block "
+                      "of records, then the rank-order sum of the maps; median of %d steps "
+                      "after %d warm-up (maps allocated once, %.2fs)"
+                      % (len(rec), threads, nside, steps, warmup, t_alloc),
+            "pixel_updates_per_s": len(MAPS) * st["hp_updates"] / t_med if t_med > 0 else None}
+    return times, info
+
+
+def parity_vs_oracle(rec, table, nside, maps_mixed, maps_fp64, device):
+    """The GPU maps of the timed run (mixed and plain FP64 paths) and the per-record pixel
+    sets of one more paint of the same catalogue, checked against the oracle's FP64 halo
+    loop on the same records and table image (all host cores, orc_paint_parallel)."""
+    import torch
+
+    import matt_young_mapmaking_gb300 as p2m
+    oracle = _oracle()
+    t0 = time.perf_counter()
+    p = oracle.params(nside=nside, maps=MAPS, zmax=ZMAX, nfloat=10)
+    rhp, _, rst, rsets = oracle.paint(p, [oracle.Table(table)], rec, record_sets=True,
+                                      set_cap=1 << 26, threads=os.cpu_count() or 1)
+    t_oracle = time.perf_counter() - t0
+    dev = torch.device("cuda", device)
+
+    def keys(srec, spix):
+        r = torch.from_numpy(np.ascontiguousarray(srec)).to(dev)
+        q = torch.from_numpy(np.ascontiguousarray(spix)).to(dev)
+        return torch.sort(r * (1 << 28) + q).values
+
+    rkeys = keys(*rsets)
+    del rsets
+    os.environ["P2M_SET_CAP"] = str(1 << 26)
+    try:
+        with p2m.Painter(nside=nside, precision="mixed", maps=MAPS, zmax=ZMAX,
+                         flags=p2m.FLAG_RECORD_SETS | p2m.FLAG_ALL_HALOS,
+                         max_records=len(rec), device=device) as pt:
+            pt.load_table(0, table)
+            pt.paint_records(rec)
+            gst = pt.stats()
+            gkeys = keys(*pt.pixel_sets())
+    finally:
+        del os.environ["P2M_SET_CAP"]
+    if gkeys.shape == rkeys.shape:
+        mism = int((gkeys != rkeys).sum())
+    else:
+        mism = abs(int(gkeys.numel()) - int(rkeys.numel()))
+    out = {"oracle": "FP64 halo loop of the oracle (orc_paint_parallel, %d threads, %.1fs), "
+                     "same records and table image" % (os.cpu_count() or 1, t_oracle),
+           "pairs_oracle": int(rkeys.numel()), "pairs_gpu": int(gkeys.numel()),
+           "set_mismatches": mism,
+           "hp_updates_equal": gst["hp_updates"] == rst["hp_updates"]}
+    for name, got in (("mixed", maps_mixed), ("fp64", maps_fp64)):
+        if got is None:
+            continue
+        out[name] = {nm: map_errors(got[m], rhp[m]) for m, nm in enumerate(("tsz", "ksz"))}
+    return out
 
 
 def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
         return
-    rec = catalogue(args.halos)
+    rec = oracle_catalogue(args.halos)
     threads = os.cpu_count() or 1
-    # each step paints a bounded sample: the whole run stays within a couple of minutes
-    sample = min(args.halos * args.cpu_fraction, 2.0e7 / max(1, args.steps + args.warmup))
-    values, info = cpu_reference(rec, args.nside, threads, sample, args.steps, args.warmup)
-    v = float(np.median(values))
+    times, info = cpu_reference(rec, args.nside, threads, oracle_table(), args.steps,
+                                args.warmup)
+    t = float(np.median(times))
+    v = args.halos / t
     out = {"metric": METRIC, "value": v, "unit": "halos/s", "n_gpus": args.gpus,
-           "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * args.halos / v,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
            "data": "synthetic (Philox catalogue, seed %d)" % SEED, "impl": "reference",
-           "config": {"workload": "pks2map c2: %d halos, HEALPix Nside %d, tSZ + kSZ, zmax %g"
-                                  % (args.halos, args.nside, ZMAX)},
+           "config": {"workload": workload_name(args.halos, args.nside)},
+           "timing": "wall clock of each step, median over the steps; total of the timed "
+                     "steps %.2fs" % float(np.sum(times)),
            "cpu_baseline": dict(info, value=v),
            "e2e": {"value": v, "unit": "halos/s", "h2d_bytes_per_step": 0,
                    "d2h_bytes_per_step": 0}}
@@ -624,9 +716,7 @@ def run_ours(args):
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
            "data": "synthetic (Philox catalogue, seed %d; profile table from make_maptable "
                    "on the GPU)" % SEED,
-           "config": {"workload": "pks2map c2: %d halos x 10 float, shell %g-%g Mpc, masses "
-                                  "%g-%g, HEALPix Nside %d, tSZ y + kSZ, zmax %g"
-                                  % (N, SHELL[0], SHELL[1], MASS[0], MASS[1], nside, ZMAX),
+           "config": {"workload": workload_name(N, nside),
                       "precision": args.precision, "l2": "inputs and maps larger than L2",
                       "tuning": tunings.get(args.precision),
                       "parallelism": "replicas" if ws > 1 else "single GPU"},
@@ -653,10 +743,12 @@ def run_ours(args):
     # counter read-outs (memsets are not kernels)
     out["gpu_launches"] = LAUNCHES_PER_STEP * args.steps
 
+    plain_maps = None
     if not args.no_plain and args.precision == "mixed":
         pp = make("fp64")
         ms64, _ = timed(pp, max(2, args.steps // 2), 1)
         ref_maps = [o.cpu().numpy() for o in outs]
+        plain_maps = ref_maps
         phases64 = pp.timings()
         pp.close()
         out["plain_fp64"] = {"value": total_halos / (ms64 * 1e-3), "ms_per_step": ms64,
@@ -702,9 +794,14 @@ def run_ours(args):
     if rank == 0 and ws == 1 and not args.no_multi_table:
         out["multi_table"] = multi_table_form(local)
 
+    # the cpu_baseline leg: the oracle timed as the CPU implementation of the path, and
+    # the oracle as the checker of this run's maps
     if rank == 0 and ws == 1 and not args.no_cpu:
-        vals, info = cpu_reference(rec, nside, os.cpu_count() or 1, N * args.cpu_fraction)
-        out["cpu_baseline"] = dict(info, value=vals[0])
+        times, info = cpu_reference(rec, nside, os.cpu_count() or 1, table, 3, 1)
+        out["cpu_baseline"] = dict(info, value=N / float(np.median(times)))
+        if not args.no_parity:
+            out["parity_vs_oracle"] = parity_vs_oracle(rec, table, nside, maps_main,
+                                                       plain_maps, local)
     if rank == 0:
         print(json.dumps(out))
     if ws > 1:

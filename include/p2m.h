@@ -60,7 +60,9 @@ enum {
 enum { P2M_LAYOUT_7 = 7, P2M_LAYOUT_10 = 10 };
 
 enum {
-  P2M_FLAG_RECORD_SETS = 1, /* keep (record index, pixel) of every HEALPix deposit */
+  P2M_FLAG_RECORD_SETS = 1, /* keep (record index, pixel) of every HEALPix deposit: up to
+                               2^24 pairs, or the count in the environment variable
+                               P2M_SET_CAP read by p2m_create; more is P2M_ERR_CAPACITY */
   P2M_FLAG_ALL_HALOS = 2,   /* enumerate halos whose table value is identically zero */
   P2M_FLAG_TIMING = 4,      /* record per-phase device times (p2m_get_timings) */
   P2M_FLAG_VALIDATE = 8     /* mixed precision: also run the exact path for every candidate

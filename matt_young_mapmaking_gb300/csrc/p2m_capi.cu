@@ -789,7 +789,10 @@ p2m_status p2m_create(const p2m_config *cfg, p2m_ctx **out) {
   CK(cudaMalloc((void **)&ctx->d_pre_bits, sizeof(unsigned int)));
   CK(cudaMalloc((void **)&ctx->d_sums, sizeof(double) * 2 * P2M_MAXMAPS));
   if (cfg->flags & P2M_FLAG_RECORD_SETS) {
+    /* (record, pixel) pairs kept; P2M_SET_CAP raises it for catalogues whose discs hold
+       more pixels in all (16 bytes of device memory per pair) */
     ctx->cap_set = 1LL << 24;
+    if (const char *e = getenv("P2M_SET_CAP")) ctx->cap_set = std::max(1LL, atoll(e));
     CK(cudaMalloc((void **)&ctx->d_set_rec, sizeof(long long) * (size_t)ctx->cap_set));
     CK(cudaMalloc((void **)&ctx->d_set_pix, sizeof(long long) * (size_t)ctx->cap_set));
   }

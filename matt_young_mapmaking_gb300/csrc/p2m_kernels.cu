@@ -916,10 +916,27 @@ __device__ __forceinline__ void deposit_maps(const PaintParams &P, const HotHalo
 }
 
 /* Mixed-precision deposit for the common pair of maps, profiles 1 and 2 of one table
-   (tSZ and kSZ): both profiles of a (corner, r-index) entry come from one 8-byte load,
-   and the bilinear-in-(chi, M), linear-in-log r blend uses corner weights formed once
-   and fused multiply-adds (a few ulp from the reference's sequence, far inside the
-   mixed path's tolerance).  Other map sets and clamped corners use deposit_maps. */
+   (tSZ and kSZ): both profiles of a (corner, r-index) entry come from one 8-byte load.
+   The blend is the reference's float sequence (maptable.f90:204-212, every product and
+   sum rounded in source order), so that a pixel whose (ir, fr) equal the reference's
+   gets the reference's value bit for bit.  Other map sets and clamped corners use
+   deposit_maps. */
+__device__ __forceinline__ float blend_pair_seq(float a0, float b0, float a1, float b1, float a2,
+                                                float b2, float a3, float b3, float fr,
+                                                float ofr, float fc, float ofc, float fm,
+                                                float ofm) {
+  float v = 0.0f;
+  v = FADD(v, FMUL(FMUL(FMUL(a0, ofr), ofc), ofm));
+  v = FADD(v, FMUL(FMUL(FMUL(b0, fr), ofc), ofm));
+  v = FADD(v, FMUL(FMUL(FMUL(a1, ofr), fc), ofm));
+  v = FADD(v, FMUL(FMUL(FMUL(b1, fr), fc), ofm));
+  v = FADD(v, FMUL(FMUL(FMUL(a2, ofr), ofc), fm));
+  v = FADD(v, FMUL(FMUL(FMUL(b2, fr), ofc), fm));
+  v = FADD(v, FMUL(FMUL(FMUL(a3, ofr), fc), fm));
+  v = FADD(v, FMUL(FMUL(FMUL(b3, fr), fc), fm));
+  return v;
+}
+
 __device__ __forceinline__ bool paired_values(const PaintParams &P, const HotHalo &H, int ir,
                                               float fr, float &v1, float &v2) {
   if (!P.paired || H.cb[0] < 0 || H.cb[1] < 0 || H.cb[2] < 0 || H.cb[3] < 0 || ir < 1 ||
@@ -931,18 +948,12 @@ __device__ __forceinline__ bool paired_values(const PaintParams &P, const HotHal
   const float2 a1 = __ldg(tab + (H.cb[1] >> 1) + r), b1 = __ldg(tab + (H.cb[1] >> 1) + r + 1);
   const float2 a2 = __ldg(tab + (H.cb[2] >> 1) + r), b2 = __ldg(tab + (H.cb[2] >> 1) + r + 1);
   const float2 a3 = __ldg(tab + (H.cb[3] >> 1) + r), b3 = __ldg(tab + (H.cb[3] >> 1) + r + 1);
-  const float ofr = 1.0f - fr, fc = H.fc, fm = H.fm, ofc = 1.0f - fc, ofm = 1.0f - fm;
-  const float w0 = ofc * ofm, w1 = fc * ofm, w2 = ofc * fm, w3 = fc * fm;
-  float p1 = w0 * fmaf(a0.x, ofr, b0.x * fr);
-  p1 = fmaf(w1, fmaf(a1.x, ofr, b1.x * fr), p1);
-  p1 = fmaf(w2, fmaf(a2.x, ofr, b2.x * fr), p1);
-  p1 = fmaf(w3, fmaf(a3.x, ofr, b3.x * fr), p1);
-  float p2 = w0 * fmaf(a0.y, ofr, b0.y * fr);
-  p2 = fmaf(w1, fmaf(a1.y, ofr, b1.y * fr), p2);
-  p2 = fmaf(w2, fmaf(a2.y, ofr, b2.y * fr), p2);
-  p2 = fmaf(w3, fmaf(a3.y, ofr, b3.y * fr), p2);
-  v1 = H.w1 * p1;
-  v2 = H.w2 * p2;
+  const float fc = H.fc, fm = H.fm;
+  const float ofr = FSUB(1.0f, fr), ofc = FSUB(1.0f, fc), ofm = FSUB(1.0f, fm);
+  v1 = FMUL(H.w1, blend_pair_seq(a0.x, b0.x, a1.x, b1.x, a2.x, b2.x, a3.x, b3.x, fr, ofr, fc,
+                                 ofc, fm, ofm));
+  v2 = FMUL(H.w2, blend_pair_seq(a0.y, b0.y, a1.y, b1.y, a2.y, b2.y, a3.y, b3.y, fr, ofr, fc,
+                                 ofc, fm, ofm));
   return true;
 }
 
@@ -1124,7 +1135,7 @@ __device__ __forceinline__ int fast_decide(const PaintParams &P, const RingItem 
   float cosd = 1.0f - 2.0f * h2;
   if (cosd < 0.05f) return 2;
   float sind = 2.0f * sqrtf(h2 * (1.0f - h2));
-  float r = H.chi_t * __fdividef(sind, cosd);
+  float r = H.chi_t * (sind / cosd);
   const float dr = 1e-5f;
   if (r > P.th.rmaxt * (1.0f + dr)) {
     zero_val = true;
@@ -1138,7 +1149,10 @@ __device__ __forceinline__ int fast_decide(const PaintParams &P, const RingItem 
     return 1;
   }
   if (r <= P.th.rmint * (1.0f + dr)) return 2;
-  float lr = __logf(r);
+  /* the reference's log (the same float function as the exact path and the oracle):
+     fr is a difference of logs that cancels to ~drt, so a cruder log's error of a few
+     ulp of log r would move the value by ~1e-7 relative, and coherently over a disc */
+  float lr = p2m_logf(r);
   float u = (lr - P.th.lrmin) * P.inv_drt;
   int iu = (int)u;
   float fu = u - (float)iu;

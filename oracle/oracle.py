@@ -92,6 +92,12 @@ def lib():
         L.orc_query_disc.restype = I64
         L.orc_paint.argtypes = [VP, VP, I32, VP, I64, VP, VP, VP, VP, VP, I64, VP]
         L.orc_paint.restype = I32
+        L.orc_generate_catalogue.argtypes = [ctypes.c_uint64, I64, I64, I32, D, D, D, D, D,
+                                             D, VP, I32]
+        L.orc_generate_catalogue.restype = I32
+        L.orc_paint_parallel.argtypes = [VP, VP, I32, VP, I64, VP, VP, VP, VP, VP, I64, VP,
+                                         I32]
+        L.orc_paint_parallel.restype = I32
         L.orc_paint_threads.argtypes = [VP, VP, I32, VP, I64, VP, VP, I32, VP, VP]
         L.orc_paint_threads.restype = I32
         L.orc_paint_ranks.argtypes = [VP, VP, I32, VP, I64, VP, I32, VP]
@@ -211,9 +217,12 @@ def params(nside=512, npix_fs=0, fov_deg=10.0, zmin=0.0, zmax=1.25, chihview=0.0
     return p
 
 
-def paint(p, tables, records, record_sets=False, set_cap=1 << 24):
+def paint(p, tables, records, record_sets=False, set_cap=1 << 24, threads=1):
     """Runs the halo loop.  Returns (hp maps (nmaps, npix) or None, fs maps or None,
-    stats dict, (set_rec, set_pix) or None)."""
+    stats dict, (set_rec, set_pix) or None).  threads > 1 (FP64 accumulation only): the
+    same results bit for bit, computed on that many threads (orc_paint_parallel)."""
+    if threads > 1 and not p.fp32_accumulate:
+        return _paint_parallel(p, tables, records, record_sets, set_cap, threads)
     rec = np.ascontiguousarray(records, dtype=np.float32)
     n = rec.shape[0]
     tabs = (OrcTable * len(tables))(*[t.t for t in tables])
@@ -239,6 +248,31 @@ def paint(p, tables, records, record_sets=False, set_cap=1 << 24):
         k = min(nset.value, set_cap)
         sets = (srec[:k].copy(), spix[:k].copy())
     return hp, fs, stats, sets
+
+
+def _paint_parallel(p, tables, records, record_sets, set_cap, threads):
+    rec = np.ascontiguousarray(records, dtype=np.float32)
+    tabs = (OrcTable * len(tables))(*[t.t for t in tables])
+    hp = np.empty((p.nmaps, 12 * p.nside * p.nside)) if p.nside > 0 else None
+    fs = np.empty((p.nmaps, p.npix_fs * p.npix_fs)) if p.npix_fs > 0 else None
+    st = OrcStats()
+    nset = ctypes.c_int64()
+    srec = np.empty(set_cap, dtype=np.int64) if record_sets else None
+    spix = np.empty(set_cap, dtype=np.int64) if record_sets else None
+    rc = lib().orc_paint_parallel(ctypes.byref(p), tabs, len(tables), _p(rec), rec.shape[0],
+                                  _p(hp) if hp is not None else None,
+                                  _p(fs) if fs is not None else None, ctypes.byref(st),
+                                  _p(srec) if record_sets else None,
+                                  _p(spix) if record_sets else None,
+                                  set_cap if record_sets else 0, ctypes.byref(nset), threads)
+    if rc:
+        raise RuntimeError("oracle paint failed (%d)" % rc)
+    sets = None
+    if record_sets:
+        if nset.value > set_cap:
+            raise RuntimeError("oracle pixel sets: %d pairs, capacity %d" % (nset.value, set_cap))
+        sets = (srec[:nset.value], spix[:nset.value])
+    return hp, fs, _stats_dict(st), sets
 
 
 def paint_threads(p, tables, records, nthreads):
@@ -269,6 +303,10 @@ class RankMaps:
         # every rank writes its own map now (in parallel), not while painting
         lib().orc_zero_ranks(self.ptrs, nranks, self.n)
 
+    def zero(self):
+        """`hpmapl = 0` of every rank, each rank writing its own maps"""
+        lib().orc_zero_ranks(self.ptrs, len(self.maps), self.n)
+
     def paint(self, p, tables, records):
         rec = np.ascontiguousarray(records, dtype=np.float32)
         tabs = (OrcTable * len(tables))(*[t.t for t in tables])
@@ -283,6 +321,18 @@ class RankMaps:
         out = np.empty(self.n, dtype=np.float32)
         lib().orc_reduce_ranks(self.ptrs, len(self.maps), self.n, _p(out), nthreads)
         return out
+
+
+def generate_catalogue(seed, n, nfloat=10, r=(100.0, 3000.0), m=(1e12, 1e15), slope=-0.9,
+                       sigma_v=300.0, first=0, threads=None):
+    """The synthetic catalogue of the GPU library's generate_catalogue, computed here
+    (orc_generate_catalogue): (n, nfloat) float32, bit-identical on the same machine."""
+    out = np.empty((n, nfloat), dtype=np.float32)
+    rc = lib().orc_generate_catalogue(seed, first, n, nfloat, r[0], r[1], m[0], m[1], slope,
+                                      sigma_v, _p(out), threads or os.cpu_count() or 1)
+    if rc:
+        raise ValueError("generate_catalogue: bad arguments")
+    return out
 
 
 def fmath(fn, x, y=None):

@@ -449,14 +449,60 @@ int orc_halo_setup(const orc_cosmo *c, const orc_params *p, const float *rec, fl
   return 1;
 }
 
+/* A growable log of (key, value) pairs: deposits (key = flat map index, flat-sky
+   deposits as -1 - index) or pixel-set entries (key = halo, value slot unused, pix in
+   aux).  Used by orc_paint_parallel to replay every thread's deposits in halo order. */
+typedef struct dep_log {
+  int64_t *key, *aux;
+  float *val;
+  int64_t n, cap;
+  int err;
+} dep_log;
+
+static void log_push(dep_log *l, int64_t key, int64_t aux, float val) {
+  if (l->err) return;
+  if (l->n == l->cap) {
+    int64_t cap = l->cap ? 2 * l->cap : (1 << 16);
+    int64_t *k = (int64_t *)realloc(l->key, sizeof(int64_t) * (size_t)cap);
+    if (k) l->key = k;
+    int64_t *a = (int64_t *)realloc(l->aux, sizeof(int64_t) * (size_t)cap);
+    if (a) l->aux = a;
+    float *v = (float *)realloc(l->val, sizeof(float) * (size_t)cap);
+    if (v) l->val = v;
+    if (!k || !a || !v) {
+      l->err = 1;
+      return;
+    }
+    l->cap = cap;
+  }
+  l->key[l->n] = key;
+  l->aux[l->n] = aux;
+  l->val[l->n] = val;
+  l->n++;
+}
+
+static void log_free(dep_log *l) {
+  free(l->key);
+  free(l->aux);
+  free(l->val);
+  memset(l, 0, sizeof(*l));
+}
+
 typedef struct paint_out {
   int fp32;
   double *hp64, *fs64;
   float *hp32, *fs32;
   int64_t hp_npix, fs_npix2;
+  dep_log *log;  /* non-NULL: deposits are logged instead of added */
+  dep_log *sets; /* non-NULL: HEALPix (halo, pixel) pairs are logged here */
 } paint_out;
 
 static void deposit(const paint_out *o, int hp, int map, int64_t j, float curval) {
+  if (o->log) {
+    log_push(o->log, hp ? (int64_t)map * o->hp_npix + j : -1 - ((int64_t)map * o->fs_npix2 + j),
+             0, curval);
+    return;
+  }
   if (hp) {
     int64_t k = (int64_t)map * o->hp_npix + j;
     if (o->fp32) o->hp32[k] = o->hp32[k] + curval;
@@ -541,6 +587,7 @@ static int projecthalo_healpix(const orc_cosmo *c, const orc_params *p, const or
     float angle = (float)orc_angdist(v1, v2);
     if ((double)angle < dtheta_halo) {
       st->hp_updates++;
+      if (o->sets) log_push(o->sets, halo_index, j, 0.0f);
       if (set_halo && *set_n < set_cap) {
         set_halo[*set_n] = halo_index;
         set_pix[*set_n] = j;
@@ -771,6 +818,142 @@ int orc_paint(const orc_params *p, const orc_table *tables, int ntables, const f
                      set_n, NULL, NULL);
   }
   if (stats) *stats = st;
+  free(c);
+  return rc;
+}
+
+/* orc_paint in FP64 accumulation with nthreads threads, with the same result bit for bit:
+   each thread runs the halo loop over a contiguous block of records and logs its deposits
+   (and pixel-set pairs) instead of adding them; the logs are then replayed in thread
+   order, i.e. in halo order, the adds of every map pixel in the serial loop's order
+   (each replaying thread owns a contiguous range of map pixels).  For catalogues whose
+   serial loop would take minutes.  set_* as orc_paint. */
+int orc_paint_parallel(const orc_params *p, const orc_table *tables, int ntables,
+                       const float *records, int64_t nhalo, double *hp_out, double *fs_out,
+                       orc_stats *stats, int64_t *set_halo, int64_t *set_pix, int64_t set_cap,
+                       int64_t *set_n, int nthreads) {
+  int rc = check_params(p, ntables);
+  if (rc) return rc;
+  if (p->fp32_accumulate) return -16;
+  if (nthreads < 1) nthreads = 1;
+  orc_cosmo *c = (orc_cosmo *)malloc(sizeof(orc_cosmo));
+  if (!c) return -20;
+  orc_cosmo_init(c);
+  const int64_t hp_npix = 12 * (int64_t)p->nside * p->nside;
+  const int64_t fs_npix2 = (int64_t)p->npix_fs * p->npix_fs;
+  const int64_t hp_n = hp_npix * p->nmaps, fs_n = fs_npix2 * p->nmaps;
+  orc_stats st;
+  memset(&st, 0, sizeof(st));
+  float *trec = NULL;
+  unsigned char *surv = NULL;
+  const float *recs = records;
+  if (p->scramble || p->centre) {
+    trec = (float *)malloc(sizeof(float) * (size_t)(nhalo * p->nfloat + 1));
+    surv = (unsigned char *)malloc((size_t)nhalo + 1);
+    if (!trec || !surv) {
+      free(trec);
+      free(surv);
+      free(c);
+      return -20;
+    }
+    preprocess(p, records, nhalo, orc_rofz(c, p->zmin), orc_rofz(c, p->zmax), trec, surv,
+               st.centre);
+    recs = trec;
+  }
+  dep_log *logs = (dep_log *)calloc((size_t)nthreads, sizeof(dep_log));
+  dep_log *sets = (dep_log *)calloc((size_t)nthreads, sizeof(dep_log));
+  orc_stats *sts = (orc_stats *)calloc((size_t)nthreads, sizeof(orc_stats));
+  int *rcs = (int *)calloc((size_t)nthreads, sizeof(int));
+  if (!logs || !sets || !sts || !rcs) {
+    free(logs);
+    free(sets);
+    free(sts);
+    free(rcs);
+    free(trec);
+    free(surv);
+    free(c);
+    return -20;
+  }
+  int64_t per = nhalo > 0 ? (nhalo - 1) / nthreads + 1 : 0;
+#pragma omp parallel num_threads(nthreads)
+  {
+#ifdef _OPENMP
+    int tid = omp_get_thread_num();
+#else
+    int tid = 0;
+#endif
+    int64_t h0 = per * tid, h1 = h0 + per;
+    if (h1 > nhalo) h1 = nhalo;
+    if (h0 < h1) {
+      paint_out o;
+      memset(&o, 0, sizeof(o));
+      o.hp_npix = hp_npix;
+      o.fs_npix2 = fs_npix2;
+      o.log = &logs[tid];
+      o.sets = (set_halo || set_n) ? &sets[tid] : NULL;
+      rcs[tid] = paint_range(c, p, tables, recs, h0, h1, &o, &sts[tid], NULL, NULL, 0, NULL,
+                             surv, surv ? records : NULL);
+    }
+  }
+  for (int t = 0; t < nthreads; t++) {
+    if (rcs[t] && !rc) rc = rcs[t];
+    if ((logs[t].err || sets[t].err) && !rc) rc = -20;
+  }
+  if (!rc) {
+    if (hp_out) memset(hp_out, 0, sizeof(double) * (size_t)(hp_n > 0 ? hp_n : 0));
+    if (fs_out) memset(fs_out, 0, sizeof(double) * (size_t)(fs_n > 0 ? fs_n : 0));
+    /* replay: worker w adds the logged values whose map index falls in its range */
+#pragma omp parallel num_threads(nthreads)
+    {
+#ifdef _OPENMP
+      int w = omp_get_thread_num();
+#else
+      int w = 0;
+#endif
+      int64_t hlo = hp_n * w / nthreads, hhi = hp_n * (w + 1) / nthreads;
+      int64_t flo = fs_n * w / nthreads, fhi = fs_n * (w + 1) / nthreads;
+      for (int t = 0; t < nthreads; t++) {
+        const dep_log *l = &logs[t];
+        for (int64_t i = 0; i < l->n; i++) {
+          int64_t k = l->key[i];
+          if (k >= 0) {
+            if (k >= hlo && k < hhi && hp_out) hp_out[k] = hp_out[k] + (double)l->val[i];
+          } else {
+            k = -1 - k;
+            if (k >= flo && k < fhi && fs_out) fs_out[k] = fs_out[k] + (double)l->val[i];
+          }
+        }
+      }
+    }
+    int64_t n = 0;
+    for (int t = 0; t < nthreads; t++) {
+      for (int64_t i = 0; i < sets[t].n; i++, n++) {
+        if (set_halo && n < set_cap) {
+          set_halo[n] = sets[t].key[i];
+          set_pix[n] = sets[t].aux[i];
+        }
+      }
+    }
+    if (set_n) *set_n = n;
+  }
+  for (int t = 0; t < nthreads; t++) {
+    st.n_in += sts[t].n_in;
+    st.n_cut += sts[t].n_cut;
+    st.n_painted += sts[t].n_painted;
+    st.hp_updates += sts[t].hp_updates;
+    st.fs_updates += sts[t].fs_updates;
+    st.hp_candidates += sts[t].hp_candidates;
+    st.ring_gaps += sts[t].ring_gaps;
+    log_free(&logs[t]);
+    log_free(&sets[t]);
+  }
+  if (stats) *stats = st;
+  free(logs);
+  free(sets);
+  free(sts);
+  free(rcs);
+  free(trec);
+  free(surv);
   free(c);
   return rc;
 }
@@ -1116,4 +1299,80 @@ int64_t orc_make_maptable(int model, float nu, float alpha_cmb, int nchit, int n
   }
   free(c);
   return nbytes;
+}
+
+/* ------------------------------------------------------- synthetic catalogue ------- */
+
+/* The synthetic catalogue generator of the GPU library (include/p2m_tools.h) restated for
+   the CPU arms, so that they never load the product library: Philox4x32-10 (Salmon,
+   Moraes, Dror and Shaw, SC 2011: ten rounds of two 32x32->64 multiplies, Weyl key
+   schedule), counter = record index, two blocks per record; positions uniform in volume
+   in the shell, isotropic directions, masses dN/dlnM ~ M^slope by inverse CDF, RTH from
+   M = (4 pi / 3) 0.31 * 2.775e11 * 0.68^2 RTH^3, Gaussian velocities (Box-Muller),
+   Lagrangian positions x - 0.01 v.  Double precision throughout, stored as float. */
+static void orc_philox(const uint32_t c[4], const uint32_t k[2], uint32_t out[4]) {
+  uint32_t x0 = c[0], x1 = c[1], x2 = c[2], x3 = c[3], k0 = k[0], k1 = k[1];
+  for (int r = 0; r < 10; r++) {
+    uint64_t p0 = (uint64_t)0xD2511F53u * x0, p1 = (uint64_t)0xCD9E8D57u * x2;
+    uint32_t n0 = (uint32_t)(p1 >> 32) ^ x1 ^ k0, n2 = (uint32_t)(p0 >> 32) ^ x3 ^ k1;
+    x1 = (uint32_t)p1;
+    x3 = (uint32_t)p0;
+    x0 = n0;
+    x2 = n2;
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+  out[0] = x0;
+  out[1] = x1;
+  out[2] = x2;
+  out[3] = x3;
+}
+
+#define ORC_M_PI 3.14159265358979323846 /* the double nearest pi, as M_PI */
+
+static double orc_u01(uint32_t x) { return ((double)x + 0.5) * (1.0 / 4294967296.0); }
+
+int orc_generate_catalogue(uint64_t seed, int64_t first, int64_t n, int nfloat, double r_min,
+                           double r_max, double m_min, double m_max, double slope,
+                           double sigma_v, float *out, int nthreads) {
+  if (!out || n < 0 || first < 0 || (nfloat != 7 && nfloat != 10)) return 1;
+  if (!(r_min >= 0 && r_max >= r_min && m_min > 0 && m_max >= m_min && slope != 0.0)) return 1;
+  const uint32_t key[2] = {(uint32_t)(seed & 0xffffffffu), (uint32_t)(seed >> 32)};
+  const double r03 = r_min * r_min * r_min, r13 = r_max * r_max * r_max;
+  const double ma = pow(m_min, slope), mb = pow(m_max, slope);
+  const double rth_fac = 3.0 / (4.0 * ORC_M_PI * 0.31 * 2.775e11 * 0.68 * 0.68);
+  if (nthreads < 1) nthreads = 1;
+#pragma omp parallel for num_threads(nthreads) schedule(static)
+  for (int64_t j = 0; j < n; j++) {
+    uint64_t idx = (uint64_t)(first + j);
+    uint32_t c0[4] = {(uint32_t)idx, (uint32_t)(idx >> 32), 0u, 0u};
+    uint32_t c1[4] = {(uint32_t)idx, (uint32_t)(idx >> 32), 1u, 0u};
+    uint32_t a[4], b[4];
+    orc_philox(c0, key, a);
+    orc_philox(c1, key, b);
+    double r = cbrt(r03 + orc_u01(a[0]) * (r13 - r03));
+    double mu = 2.0 * orc_u01(a[1]) - 1.0;
+    double ph = 2.0 * ORC_M_PI * orc_u01(a[2]);
+    double st = sqrt(fmax(0.0, 1.0 - mu * mu));
+    double x = r * st * cos(ph), y = r * st * sin(ph), z = r * mu;
+    double m = pow(ma + orc_u01(a[3]) * (mb - ma), 1.0 / slope);
+    double rth = cbrt(rth_fac * m);
+    double g1 = sqrt(-2.0 * log(orc_u01(b[0]))), t1 = 2.0 * ORC_M_PI * orc_u01(b[1]);
+    double g2 = sqrt(-2.0 * log(orc_u01(b[2]))), t2 = 2.0 * ORC_M_PI * orc_u01(b[3]);
+    double vx = sigma_v * g1 * cos(t1), vy = sigma_v * g1 * sin(t1), vz = sigma_v * g2 * cos(t2);
+    float *o = out + j * nfloat;
+    o[0] = (float)x;
+    o[1] = (float)y;
+    o[2] = (float)z;
+    o[3] = (float)vx;
+    o[4] = (float)vy;
+    o[5] = (float)vz;
+    o[6] = (float)rth;
+    if (nfloat == 10) {
+      o[7] = (float)(x - 0.01 * vx);
+      o[8] = (float)(y - 0.01 * vy);
+      o[9] = (float)(z - 0.01 * vz);
+    }
+  }
+  return 0;
 }

@@ -100,6 +100,14 @@ int orc_paint(const orc_params *p, const orc_table *tables, int ntables, const f
               int64_t nhalo, void *hp_out, void *fs_out, orc_stats *stats, int64_t *set_halo,
               int64_t *set_pix, int64_t set_cap, int64_t *set_n);
 
+/* orc_paint in FP64 accumulation (p->fp32_accumulate = 0) on nthreads threads, with the
+   same maps, stats and pixel sets bit for bit: the threads log their deposits, which are
+   then added in halo order.  Returns -16 for FP32 accumulation. */
+int orc_paint_parallel(const orc_params *p, const orc_table *tables, int ntables,
+                       const float *records, int64_t nhalo, double *hp_out, double *fs_out,
+                       orc_stats *stats, int64_t *set_halo, int64_t *set_pix, int64_t set_cap,
+                       int64_t *set_n, int nthreads);
+
 /* Same loop split over nthreads contiguous halo blocks, each painting a private float
    map, summed at the end: the reference's MPI decomposition (pksc.f90:51-66,
    pks2map.f90:313-314) with threads as ranks.  Float output only.  Times (seconds)
@@ -125,6 +133,13 @@ void orc_fmath_eval(int fn, const float *x, const float *y, float *out, int64_t 
 
 /* per-halo derived quantities of the loop, for tests: returns 1 if the halo is painted */
 int orc_halo_setup(const orc_cosmo *c, const orc_params *p, const float *rec, float *out8);
+
+/* The synthetic catalogue generator of include/p2m_tools.h (p2m_generate_catalogue),
+   restated so that CPU-only callers need not load the GPU library; bit-identical output
+   on the same machine.  Returns 0, or 1 for bad arguments. */
+int orc_generate_catalogue(uint64_t seed, int64_t first, int64_t n, int nfloat, double r_min,
+                           double r_max, double m_min, double m_max, double slope,
+                           double sigma_v, float *out, int nthreads);
 
 #ifdef __cplusplus
 }

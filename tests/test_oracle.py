@@ -231,6 +231,35 @@ def test_threads_as_ranks_equals_serial():
     assert len(t) == 3
 
 
+@pytest.mark.parametrize("scramble,centre", [(0, 0), (1, 1)])
+def test_parallel_fp64_equals_serial_bit_for_bit(scramble, centre):
+    """orc_paint_parallel replays the threads' deposits in halo order: the same FP64 maps
+    (HEALPix and flat sky), counters and pixel sets as the serial loop, bit for bit."""
+    rec = np.concatenate([catalogs.edge_cases(), catalogs.shell(7, 30_000)])
+    tab = [oracle.Table(catalogs.table())]
+    maps = ((0, 1), (0, 2))
+    p = oracle.params(nside=128, npix_fs=96, fov_deg=20.0, maps=maps, scramble=scramble,
+                      centre=centre)
+    hs, fs, ss, sets = oracle.paint(p, tab, rec, record_sets=True)
+    hp, fp, sp, setp = oracle.paint(p, tab, rec, record_sets=True, threads=5)
+    assert ss["hp_updates"] > 300 and ss["fs_updates"] > 0
+    assert np.array_equal(hs, hp) and np.array_equal(fs, fp)
+    assert ss == sp
+    assert np.array_equal(sets[0], setp[0]) and np.array_equal(sets[1], setp[1])
+
+
+def test_oracle_generator_equals_library_generator():
+    """The CPU arms build their catalogues with the oracle's restatement of the library's
+    generator: the same records bit for bit (both layouts, an offset first record)."""
+    import matt_young_mapmaking_gb300 as p2m
+    for nfloat, first in ((10, 0), (7, 123_457)):
+        a = oracle.generate_catalogue(2, 200_000, nfloat, r=(100.0, 8000.0), m=(1e12, 3e15),
+                                      first=first)
+        b = p2m.generate_catalogue(2, 200_000, nfloat, r=(100.0, 8000.0), m=(1e12, 3e15),
+                                   first=first)
+        assert a.tobytes() == b.tobytes()
+
+
 def test_golden_fixture_regression():
     """Oracle output on the committed golden inputs is unchanged (regression pin)."""
     import os
