@@ -121,6 +121,19 @@ const char *p2m_last_error(const p2m_ctx *ctx);
    into slot 0..7.  All loaded tables must share one header. */
 p2m_status p2m_load_table(p2m_ctx *ctx, int32_t slot, const void *image, int64_t nbytes);
 
+/* Replace the r(z) and z(r) tables of cosmology.f90:51-105 (set_rofztable /
+   set_zofrtable, called at pks2map.f90:131-132), which the context otherwise builds from
+   the reference's hard-wired cosmology (pks2map.f90:118-128): rofz[i] = r at
+   z = i * rofz_zmax / (n - 1) (Mpc), zofr[i] = z at r = i * zofr_rmax / (n - 1), both
+   tables starting at 0, n = 10000 (the reference's table length); looked up as rofz/zofr
+   do (cosmology.f90:137-181, linear, clamped at both ends).  They set the radial cut
+   and each halo's redshift and table distance from the next paint call on.  The other
+   cosmological parameters (omegam, h, rho_0: mass conversion, rhocrit, deltacrit) stay
+   the reference's.  P2M_ERR_STATE while painted halos await a read-out (call it right
+   after p2m_create or p2m_reset_maps). */
+p2m_status p2m_set_cosmology_tables(p2m_ctx *ctx, const float *rofz, const float *zofr,
+                                    int32_t n, float rofz_zmax, float zofr_rmax);
+
 /* Zero the accumulated maps (the reference's `fsmapl=0; hpmapl=0`, pks2map.f90:278-279). */
 p2m_status p2m_reset_maps(p2m_ctx *ctx);
 
@@ -195,6 +208,33 @@ p2m_status p2m_get_healpix_device(p2m_ctx *ctx, int32_t map, float *d_out, void 
    and p2m_get_healpix_device with the same pointer copies nothing.  Call right after
    p2m_create or p2m_reset_maps; NULL restores the context's own buffer. */
 p2m_status p2m_bind_healpix_device(p2m_ctx *ctx, int32_t map, float *d_out);
+
+/* Statistics of one map as a read-out delivers it (pks2map.f90:321-334): the moments
+   sum(map**k) / npix, k = 1..3, and the RMS sqrt(sum((map - mom[0])**2) / npix).  The
+   sums are formed on the device in float-float per thread and FP64 across threads (the
+   reference's `sum` of a real array accumulates in float, in an order the compiler
+   chooses; these are within its rounding of that).  No counterpart as a call in the
+   reference, whose main program runs these loops over the gathered maps. */
+typedef struct p2m_map_stats {
+  int64_t npix;   /* pixels of the map */
+  double mom[3];  /* hpmom1..3 / fsmom1..3 */
+  double rms;     /* Healpix / Flatsky RMS */
+} p2m_map_stats;
+/* HEALPix map `map` (not an ensemble's); with dpdy non-null also the cumulative P(<y) of
+   pks2map.f90:340-357 into dpdy[0..10000): bin m = int(y / 1e-8) + 1 counted in float (a
+   bin stops at 2^24, as the reference's real counter does), divided by the pixel count,
+   then cumulated. */
+p2m_status p2m_get_healpix_stats(p2m_ctx *ctx, int32_t map, p2m_map_stats *out, float *dpdy);
+p2m_status p2m_get_flatsky_stats(p2m_ctx *ctx, int32_t map, p2m_map_stats *out);
+
+/* Write HEALPix map `map` (not an ensemble's) to the FITS file `path` as the reference's
+   output_map does (pks2map.f90:381-385; an empty primary HDU, then a BINTABLE of
+   1024-value float rows, NSIDE and ORDERING = 'RING' cards; see p2m_write_healpix_fits
+   in p2m_tools.h for the layout): the map is converted to big-endian words on the device
+   and copied out in 64 MB slices, each slice's copy overlapping the file write of the
+   one before.  No host copy of the map is needed.  P2M_ERR_IO if the file cannot be
+   written. */
+p2m_status p2m_write_healpix_fits_device(p2m_ctx *ctx, int32_t map, const char *path);
 
 /* Counters and map sums of everything painted since the last reset. */
 p2m_status p2m_get_stats(p2m_ctx *ctx, p2m_stats *out);

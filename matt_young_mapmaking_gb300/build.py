@@ -93,7 +93,7 @@ def build_cli(force=False):
         if not force and not _stale(exe, deps + [path]):
             continue
         _run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-I" + CSRC, "-I" + INCLUDE,
-              path, "-o", exe, "-L" + PKG, "-lp2m_gb300", "-Wl,-rpath,$ORIGIN"])
+              path, "-o", exe, "-L" + PKG, "-lp2m_gb300", "-Wl,-rpath,$ORIGIN", "-pthread"])
     return CLI
 
 

@@ -30,6 +30,10 @@ class P2MError(RuntimeError):
         self.status = status
 
 
+class P2MMapStats(ctypes.Structure):
+    _fields_ = [("npix", ctypes.c_int64), ("mom", ctypes.c_double * 3), ("rms", ctypes.c_double)]
+
+
 class P2MConfig(ctypes.Structure):
     _fields_ = [
         ("nside", ctypes.c_int32),
@@ -118,6 +122,10 @@ def load_library():
         "p2m_get_timings": (I32, [VP, VP, I32]),
         "p2m_map_sums_noalloc": (I32, [VP, I32, I64, VP, VP]),
         "p2m_set_preprocess": (I32, [VP, I32, I32, I32]),
+        "p2m_set_cosmology_tables": (I32, [VP, VP, VP, I32, F, F]),
+        "p2m_get_healpix_stats": (I32, [VP, I32, VP, VP]),
+        "p2m_get_flatsky_stats": (I32, [VP, I32, VP]),
+        "p2m_write_healpix_fits_device": (I32, [VP, I32, ctypes.c_char_p]),
         "p2m_get_centre": (I32, [VP, VP]),
         "p2m_dpdy": (I32, [VP, I64, VP]),
         "p2m_write_dpdy": (I32, [ctypes.c_char_p, VP]),
@@ -150,6 +158,8 @@ def exported_symbols():
             "p2m_synchronize", "p2m_get_pixel_sets", "p2m_make_maptable",
             "p2m_generate_catalogue", "p2m_philox4x32", "p2m_fmath_eval_device",
             "p2m_get_timings", "p2m_map_sums_noalloc", "p2m_set_preprocess", "p2m_get_centre",
+            "p2m_set_cosmology_tables", "p2m_get_healpix_stats", "p2m_get_flatsky_stats",
+            "p2m_write_healpix_fits_device",
             "p2m_dpdy", "p2m_write_dpdy",
             "p2m_write_flatsky", "p2m_write_healpix_fits", "p2m_cl_healpix", "p2m_cl_flatsky",
             "p2m_paint_ensemble", "p2m_paint_ensemble_device", "p2m_get_healpix_cone",
@@ -239,6 +249,33 @@ class Painter:
         v = np.zeros(9, dtype=np.float32)
         self._check(self._lib.p2m_get_centre(self._h, _ptr(v)))
         return v
+
+    def set_cosmology_tables(self, rofz, zofr, rofz_zmax=6.0, zofr_rmax=1.3e4):
+        """Replace the r(z) and z(r) tables (10000 floats each, from 0 to rofz_zmax in z
+        and to zofr_rmax Mpc in r)."""
+        a = np.ascontiguousarray(rofz, dtype=np.float32)
+        b = np.ascontiguousarray(zofr, dtype=np.float32)
+        if a.shape != b.shape or a.ndim != 1:
+            raise P2MError(1, "rofz and zofr must be 1-d arrays of one length")
+        self._check(self._lib.p2m_set_cosmology_tables(self._h, _ptr(a), _ptr(b), a.size,
+                                                       rofz_zmax, zofr_rmax))
+
+    def map_stats(self, m=0, flatsky=False, dpdy=True):
+        """Moments (3), RMS and, for a HEALPix map, the cumulative P(<y) (10000 floats) of
+        map m, computed on the device (pks2map.f90:321-357)."""
+        st = P2MMapStats()
+        if flatsky:
+            self._check(self._lib.p2m_get_flatsky_stats(self._h, m, ctypes.byref(st)))
+            return list(st.mom), st.rms, None
+        dp = np.zeros(NDPDY, dtype=np.float32) if dpdy else None
+        self._check(self._lib.p2m_get_healpix_stats(self._h, m, ctypes.byref(st),
+                                                    _ptr(dp) if dp is not None else None))
+        return list(st.mom), st.rms, dp
+
+    def write_healpix_fits(self, m, path):
+        """HEALPix map m to a FITS file, converted and copied out from the device in
+        slices that overlap the file write."""
+        self._check(self._lib.p2m_write_healpix_fits_device(self._h, m, str(path).encode()))
 
     def load_table(self, slot, image):
         """loadmaptable: `image` is the table file's bytes (header + table)."""

@@ -17,6 +17,7 @@
 
 #include "../../include/p2m.h"
 #include "../../include/p2m_tools.h"
+#include "p2m_fits.h"
 #include "p2m_internal.h"
 
 enum {
@@ -32,6 +33,12 @@ struct p2m_ctx {
   p2m_cosmo cosmo;
   std::vector<float> rofz_host, zofr_host;
   float *d_rofz = nullptr, *d_zofr = nullptr;
+  /* map statistics: three FP64 sums and the P(<y) bin counts */
+  double *d_mstat = nullptr;
+  unsigned int *d_hist = nullptr;
+  /* FITS writer: big-endian slices of a map on the device and in pinned host memory */
+  unsigned int *d_fits[2] = {nullptr, nullptr}, *h_fits[2] = {nullptr, nullptr};
+  cudaEvent_t ev_fits[2] = {nullptr, nullptr};
   float4 *d_ringtab = nullptr;
   float4 *d_phitab = nullptr;
   /* scramble / centre of the catalogue (pks2map.f90:162-262) */
@@ -817,7 +824,8 @@ void p2m_destroy(p2m_ctx *ctx) {
                   ctx->d_ctr, ctx->d_prep, ctx->d_lo, ctx->d_tiles,
                   ctx->d_pre_flags, ctx->d_pre_bits, ctx->d_pre_ord, ctx->d_pre_last,
                   ctx->d_cone_off, ctx->d_stage[0], ctx->d_stage[1], ctx->d_order,
-                  ctx->d_ring_key, ctx->d_ring_hist, ctx->d_ring_off, ctx->d_nbins};
+                  ctx->d_ring_key, ctx->d_ring_hist, ctx->d_ring_off, ctx->d_nbins,
+                  ctx->d_mstat, ctx->d_hist, ctx->d_fits[0], ctx->d_fits[1]};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   for (int m = 0; m < P2M_MAXMAPS; m++)
@@ -825,6 +833,10 @@ void p2m_destroy(p2m_ctx *ctx) {
   for (int t = 0; t < P2M_MAXTABLES; t++)
     if (ctx->d_tab[t]) cudaFree(ctx->d_tab[t]);
   if (ctx->h_ctr) cudaFreeHost(ctx->h_ctr);
+  for (int b = 0; b < 2; b++) {
+    if (ctx->h_fits[b]) cudaFreeHost(ctx->h_fits[b]);
+    if (ctx->ev_fits[b]) cudaEventDestroy(ctx->ev_fits[b]);
+  }
   if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
   if (ctx->ev_back) cudaEventDestroy(ctx->ev_back);
   if (ctx->ev_zero_start) cudaEventDestroy(ctx->ev_zero_start);
@@ -855,6 +867,31 @@ void p2m_destroy(p2m_ctx *ctx) {
 const char *p2m_last_error(const p2m_ctx *ctx) {
   if (!ctx) return "null context";
   return ctx->err.c_str();
+}
+
+p2m_status p2m_set_cosmology_tables(p2m_ctx *ctx, const float *rofz, const float *zofr,
+                                    int32_t n, float rofz_zmax, float zofr_rmax) {
+  if (!ctx) return P2M_ERR_BADARG;
+  if (!rofz || !zofr) return fail(ctx, P2M_ERR_BADARG, "null cosmology table");
+  if (n != P2M_NZTAB)
+    return fail(ctx, P2M_ERR_BADARG, "cosmology tables hold 10000 entries (cosmology.f90:60,89)");
+  if (!(rofz_zmax > 0.0f && zofr_rmax > 0.0f && rofz_zmax < 1e30f && zofr_rmax < 1e30f))
+    return fail(ctx, P2M_ERR_BADARG, "cosmology table ranges must be positive and finite");
+  for (int i = 0; i < n; i++)
+    if (!(rofz[i] == rofz[i] && zofr[i] == zofr[i]))
+      return fail(ctx, P2M_ERR_BADARG, "cosmology table holds a NaN");
+  if (ctx->dirty || ctx->unfolded || !ctx->prep.empty())
+    return fail(ctx, P2M_ERR_STATE, "cosmology tables cannot change while painted halos await a read-out");
+  CK(cudaSetDevice(ctx->cfg.device));
+  CK(cudaStreamSynchronize(ctx->stream));
+  ctx->rofz_host.assign(rofz, rofz + n);
+  ctx->zofr_host.assign(zofr, zofr + n);
+  /* drofztable, dzofrtable of cosmology.f90:61,90 (the tables start at 0) */
+  ctx->cosmo.drofz = FDIV(rofz_zmax, (float)(n - 1));
+  ctx->cosmo.dzofr = FDIV(zofr_rmax, (float)(n - 1));
+  CK(cudaMemcpy(ctx->d_rofz, rofz, sizeof(float) * (size_t)n, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(ctx->d_zofr, zofr, sizeof(float) * (size_t)n, cudaMemcpyHostToDevice));
+  return P2M_OK;
 }
 
 p2m_status p2m_load_table(p2m_ctx *ctx, int32_t slot, const void *image, int64_t nbytes) {
@@ -969,6 +1006,10 @@ p2m_status stream_host_records(p2m_ctx *ctx, const float *records, long long nre
   long long chunk = std::max<long long>(ctx->cfg.max_records, 1024);
   if (!pre) chunk = std::min<long long>(chunk, ctx->tune.stream_chunk);
   if (nrec <= 0) return P2M_OK;
+  if (pre && nrec > chunk)
+    return fail(ctx, P2M_ERR_CAPACITY,
+                "scramble and centre need the whole catalogue in one paint call of at most "
+                "max_records records");
   const long long nchunk = (nrec + chunk - 1) / chunk;
   if (!ctx->cstream) {
     CK(cudaStreamCreateWithFlags(&ctx->cstream, cudaStreamNonBlocking));
@@ -1303,6 +1344,125 @@ p2m_status p2m_get_flatsky(p2m_ctx *ctx, int32_t map, float *out) {
                      cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
   return P2M_OK;
+}
+
+namespace {
+
+/* moments, RMS and (dpdy non-null) P(<y) of the float map d_map (npix pixels) on the
+   context's stream, pks2map.f90:321-357 */
+p2m_status map_stats(p2m_ctx *ctx, const float *d_map, long long npix, p2m_map_stats *out,
+                     float *dpdy) {
+  cudaStream_t s = ctx->stream;
+  if (!ctx->d_mstat) CK(cudaMalloc((void **)&ctx->d_mstat, sizeof(double) * 4));
+  if (dpdy && !ctx->d_hist) CK(cudaMalloc((void **)&ctx->d_hist, sizeof(unsigned int) * P2M_NDPDY));
+  CK(cudaMemsetAsync(ctx->d_mstat, 0, sizeof(double) * 4, s));
+  if (dpdy) CK(cudaMemsetAsync(ctx->d_hist, 0, sizeof(unsigned int) * P2M_NDPDY, s));
+  /* dpdy_dy = dpdy_max / ndpdy (pks2map.f90:40) */
+  const float dy = FDIV(1e-4f, (float)P2M_NDPDY);
+  p2m_launch_map_stats(d_map, npix, ctx->d_mstat, dpdy ? ctx->d_hist : nullptr, P2M_NDPDY, dy,
+                       s, ctx->nsm);
+  CK(cudaGetLastError());
+  double sums[4];
+  std::vector<unsigned int> h(dpdy ? P2M_NDPDY : 0);
+  CK(cudaMemcpyAsync(sums, ctx->d_mstat, sizeof(double) * 4, cudaMemcpyDeviceToHost, s));
+  if (dpdy)
+    CK(cudaMemcpyAsync(h.data(), ctx->d_hist, sizeof(unsigned int) * P2M_NDPDY,
+                       cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  ST(check_errors(ctx, s));
+  const double n = (double)npix;
+  out->npix = npix;
+  for (int k = 0; k < 3; k++) out->mom[k] = sums[k] / n;
+  /* sum((x - mom1)^2) = sum x^2 - 2 mom1 sum x + n mom1^2, in FP64 */
+  const double m1 = out->mom[0];
+  const double ss = sums[1] - 2.0 * m1 * sums[0] + n * m1 * m1;
+  out->rms = std::sqrt(ss > 0.0 ? ss / n : 0.0);
+  if (dpdy) {
+    /* the reference counts in float (:345): a bin stops at 2^24 */
+    for (int k = 0; k < P2M_NDPDY; k++) dpdy[k] = (float)std::min(h[k], 16777216u);
+    const float norm = (float)npix;
+    for (int k = 0; k < P2M_NDPDY; k++) dpdy[k] = dpdy[k] / norm;            /* :347 */
+    for (int k = 1; k < P2M_NDPDY; k++) dpdy[k] = dpdy[k - 1] + dpdy[k];     /* :355-357 */
+  }
+  return P2M_OK;
+}
+
+}  // namespace
+
+p2m_status p2m_get_healpix_stats(p2m_ctx *ctx, int32_t map, p2m_map_stats *out, float *dpdy) {
+  if (!ctx || !out) return P2M_ERR_BADARG;
+  if (map < 0 || map >= ctx->cfg.nmaps || ctx->cfg.nside <= 0)
+    return fail(ctx, P2M_ERR_BADARG, "map index out of range");
+  if (ctx->ncones > 1)
+    return fail(ctx, P2M_ERR_BADARG, "statistics of an ensemble: read the cones out one by one");
+  CK(cudaSetDevice(ctx->cfg.device));
+  ST(sweep(ctx, ctx->stream));
+  return map_stats(ctx, ctx->d_out[map], ctx->hp_npix, out, dpdy);
+}
+
+p2m_status p2m_get_flatsky_stats(p2m_ctx *ctx, int32_t map, p2m_map_stats *out) {
+  if (!ctx || !out) return P2M_ERR_BADARG;
+  if (map < 0 || map >= ctx->cfg.nmaps || ctx->cfg.npix_fs <= 0)
+    return fail(ctx, P2M_ERR_BADARG, "no flat-sky map / map index out of range");
+  CK(cudaSetDevice(ctx->cfg.device));
+  ST(flush_prepared(ctx));
+  cudaStream_t s = ctx->stream;
+  PaintParams P = make_params(ctx, 7);
+  double *sum = ctx->d_sums + P2M_MAXMAPS + map;
+  CK(cudaMemsetAsync(sum, 0, sizeof(double), s));
+  p2m_launch_finalize_fs(P, ctx->d_fs_acc, ctx->fs_npix, ctx->d_fs_out, map, sum, s, ctx->nsm);
+  CK(cudaGetLastError());
+  return map_stats(ctx, ctx->d_fs_out, ctx->fs_npix, out, nullptr);
+}
+
+#define P2M_FITS_SLICE (1LL << 24) /* floats per slice of the device FITS writer (64 MB) */
+
+p2m_status p2m_write_healpix_fits_device(p2m_ctx *ctx, int32_t map, const char *path) {
+  if (!ctx || !path) return P2M_ERR_BADARG;
+  if (map < 0 || map >= ctx->cfg.nmaps || ctx->cfg.nside <= 0)
+    return fail(ctx, P2M_ERR_BADARG, "map index out of range");
+  if (ctx->ncones > 1)
+    return fail(ctx, P2M_ERR_BADARG, "an ensemble's maps: read the cones out one by one");
+  CK(cudaSetDevice(ctx->cfg.device));
+  cudaStream_t s = ctx->stream;
+  ST(sweep(ctx, s));
+  const long long n = ctx->hp_npix, slice = std::min<long long>(n, P2M_FITS_SLICE);
+  for (int b = 0; b < 2; b++) {
+    if (!ctx->d_fits[b]) CK(cudaMalloc((void **)&ctx->d_fits[b], sizeof(unsigned int) * P2M_FITS_SLICE));
+    if (!ctx->h_fits[b]) CK(cudaHostAlloc((void **)&ctx->h_fits[b], sizeof(unsigned int) * P2M_FITS_SLICE, 0));
+    if (!ctx->ev_fits[b]) CK(cudaEventCreateWithFlags(&ctx->ev_fits[b], cudaEventDisableTiming));
+  }
+  FILE *fp = std::fopen(path, "wb");
+  if (!fp) return fail(ctx, P2M_ERR_IO, std::string("cannot open ") + path);
+  bool ok = p2m_fits_put_header(fp, ctx->cfg.nside) == P2M_OK;
+  /* slice k is converted and copied while slice k - 1 is written to the file */
+  const long long nslice = (n + slice - 1) / slice;
+  cudaError_t e = cudaSuccess;
+  for (long long k = 0; k <= nslice && ok && e == cudaSuccess; k++) {
+    if (k < nslice) {
+      const int b = (int)(k & 1);
+      const long long len = std::min(slice, n - k * slice);
+      p2m_launch_to_big_endian(ctx->d_out[map] + k * slice, ctx->d_fits[b], len, s, ctx->nsm);
+      e = cudaGetLastError();
+      if (e == cudaSuccess)
+        e = cudaMemcpyAsync(ctx->h_fits[b], ctx->d_fits[b], sizeof(unsigned int) * (size_t)len,
+                            cudaMemcpyDeviceToHost, s);
+      if (e == cudaSuccess) e = cudaEventRecord(ctx->ev_fits[b], s);
+    }
+    if (k > 0 && e == cudaSuccess) {
+      const int b = (int)((k - 1) & 1);
+      const long long len = std::min(slice, n - (k - 1) * slice);
+      e = cudaEventSynchronize(ctx->ev_fits[b]);
+      if (e == cudaSuccess)
+        ok = std::fwrite(ctx->h_fits[b], sizeof(unsigned int), (size_t)len, fp) == (size_t)len;
+    }
+  }
+  if (ok && e == cudaSuccess) ok = p2m_fits_put_padding(fp, ctx->cfg.nside) == P2M_OK;
+  ok = (std::fclose(fp) == 0) && ok;
+  if (e != cudaSuccess)
+    return fail(ctx, P2M_ERR_CUDA, std::string("FITS read-out: ") + cudaGetErrorString(e));
+  if (!ok) return fail(ctx, P2M_ERR_IO, std::string("cannot write ") + path);
+  return check_errors(ctx, s);
 }
 
 p2m_status p2m_get_stats(p2m_ctx *ctx, p2m_stats *out) {

@@ -82,7 +82,10 @@ struct RingItem {
                                 the k-th candidate sits at x = (n0 + k) + f0, exact integer
                                 part, so x keeps full relative precision near the centre */
   float hdphi;               /* pi / npr */
+  float Al, Bl, f0l, hdl;    /* low words: (A, Al), (B, Bl), (f0, f0l), (hdphi, hdl) are
+                                float-float values (~44 bits) for the pixel's angle */
 };
+static_assert(sizeof(RingItem) == 48, "RingItem layout");
 
 __host__ __device__ __forceinline__ int item_ring(const RingItem &it) { return it.ring_n0 >> 16; }
 __host__ __device__ __forceinline__ int item_n0(const RingItem &it) {
@@ -186,6 +189,13 @@ void p2m_launch_finalize_fs(const PaintParams &P, const void *acc, long long npi
                             int map, double *sum, cudaStream_t s, int nsm);
 void p2m_launch_fold_lo(const PaintParams &P, const SweepBuffers &W, cudaStream_t s, int nsm);
 void p2m_launch_map_sum(const float *map, long long n, double *sum, cudaStream_t s, int nsm);
+/* out[i] = the big-endian bytes of in[i] (FITS data order) */
+void p2m_launch_to_big_endian(const float *in, unsigned int *out, long long n, cudaStream_t s,
+                              int nsm);
+/* sums[0..3) += sums of x, x^2, x^3 over the map; hist (nbins <= 12288 counters, or null)
+   += the P(<y) bin counts of bin width dy */
+void p2m_launch_map_stats(const float *map, long long n, double *sums, unsigned int *hist,
+                          int nbins, float dy, cudaStream_t s, int nsm);
 /* copies the counters into mapped host memory with the SMs' stores: no copy engine, so a
    counter read never queues behind a large read-out copy */
 void p2m_launch_copy_counters(const DevCounters *d, DevCounters *h_mapped, cudaStream_t s);

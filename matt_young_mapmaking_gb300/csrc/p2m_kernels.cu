@@ -196,6 +196,26 @@ __device__ __forceinline__ ffloat ff_mul(ffloat x, ffloat y) {
   return ff_norm(p, e);
 }
 
+/* exact sum of two floats as a float-float (Knuth's two-sum, no ordering needed) */
+__device__ __forceinline__ ffloat ff_two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  return {s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
+}
+
+/* float-float plus float */
+__device__ __forceinline__ ffloat ff_add_f(ffloat x, float y) {
+  const ffloat s = ff_two_sum(x.h, y);
+  return ff_norm(s.h, __fadd_rn(s.l, x.l));
+}
+
+/* square of a float-float */
+__device__ __forceinline__ ffloat ff_sqr(ffloat x) {
+  const float p = __fmul_rn(x.h, x.h);
+  const float e = __fmaf_rn(x.h, x.h, -p);
+  return ff_norm(p, __fmaf_rn(__fmul_rn(2.0f, x.h), x.l, e));
+}
+
 /* x / y with one correction of the FP32 quotient (exact remainder through fmaf) */
 __device__ __forceinline__ ffloat ff_div(ffloat x, ffloat y) {
   const float q = __fdiv_rn(x.h, y.h);
@@ -594,10 +614,13 @@ __device__ __forceinline__ RingItem make_item(const PaintParams &P, const DiscGe
                                               int ring) {
   RingItem it;
   const float4 zs = P.ringtab[ring];
-  const float dz = __fadd_rn(__fsub_rn(zs.x, g.zh), __fsub_rn(zs.y, g.zl));
-  const float ds = __fadd_rn(__fsub_rn(zs.z, g.sh), __fsub_rn(zs.w, g.sl));
-  const float A = __fadd_rn(__fmul_rn(dz, dz), __fmul_rn(ds, ds));
-  const float Bc = __fmul_rn(4.0f, __fmul_rn(zs.z, g.sh));
+  /* A = dz^2 + ds^2 and B = 4 sin(theta_ring) sin(theta_0) as float-float values: the
+     ring's and the centre's (hi, lo) pairs differ without cancellation loss */
+  const ffloat dzf = ff_add_f(ff_two_sum(zs.x, -g.zh), __fsub_rn(zs.y, g.zl));
+  const ffloat dsf = ff_add_f(ff_two_sum(zs.z, -g.sh), __fsub_rn(zs.w, g.sl));
+  const ffloat Af = ff_add(ff_sqr(dzf), ff_sqr(dsf));
+  const ffloat Bf = ff_mul({zs.z, zs.w}, {__fmul_rn(4.0f, g.sh), __fmul_rn(4.0f, g.sl)});
+  const float A = Af.h, Bc = Bf.h;
   int npr, kshift;
   long long npn;
   p2m_ring_info(P.nside, ring, &npr, &kshift, &npn);
@@ -642,16 +665,23 @@ __device__ __forceinline__ RingItem make_item(const PaintParams &P, const DiscGe
   const float a = rintf(qh);
   const float d = __fsub_rn(qh, a);
   const float rf = rintf(__fsub_rn(__fsub_rn(sh, d), ql));
-  const float f0 = __fsub_rn(__fsub_rn(sh - rf, d), ql);
+  /* f0 = ((sh - rf) - d) - ql as a float-float: sh - rf and d are exact */
+  const ffloat f0f = ff_add_f(ff_two_sum(sh - rf, -d), -ql);
   const int n0 = lo - (int)a + (int)rf;
+  /* pi / npr as a float-float (pi = 3.14159274f - 8.74227766e-8f to 2^-48) */
+  const ffloat hd = ff_div({3.14159274e+00f, -8.74227766e-08f}, {fn, 0.0f});
   it.halo = h;
   it.ring_n0 = (ring << 16) | (n0 & 0xffff);
   it.lo = lo;
   it.count = cnt;
   it.A = A;
   it.B = Bc;
-  it.f0 = f0;
-  it.hdphi = 3.14159265358979f / fn;
+  it.f0 = f0f.h;
+  it.hdphi = hd.h;
+  it.Al = Af.l;
+  it.Bl = Bf.l;
+  it.f0l = f0f.l;
+  it.hdl = hd.l;
   return it;
 }
 
@@ -1105,10 +1135,11 @@ __device__ __forceinline__ void record_set(long long *set_rec, long long *set_pi
   }
 }
 
-/* sin(y) by its Taylor series through y^15, for the half longitude offset y of a candidate
-   from the disc centre: |y| < pi/2 + pi/npr <= 2.37, where the truncation stays below 1e-8
-   and the rounding is a few ulp */
-__device__ __forceinline__ float sin_half_offset(float y) {
+/* sin(y) - y by its Taylor series through y^15, for the half longitude offset y of a
+   candidate from the disc centre: |y| < pi/2 + pi/npr <= 2.37, where the truncation stays
+   below 1e-8; the result is a correction to y, so its relative rounding (a few ulp)
+   costs ~y^2/6 ulp of sin(y) */
+__device__ __forceinline__ float sin_minus_arg(float y) {
   const float y2 = y * y;
   float p = 1.0f / 1307674368000.0f;      /* 1/15! */
   p = fmaf(p, y2, -1.0f / 6227020800.0f); /* -1/13! */
@@ -1117,25 +1148,49 @@ __device__ __forceinline__ float sin_half_offset(float y) {
   p = fmaf(p, y2, 1.0f / 5040.0f);        /* 1/7! */
   p = fmaf(p, y2, -1.0f / 120.0f);        /* -1/5! */
   p = fmaf(p, y2, 1.0f / 6.0f);           /* 1/3! */
-  return fmaf(-y * y2, p, y);             /* y - y^3 (1/3! - y^2/5! + ...) */
+  return -y * y2 * p;                     /* -y^3 (1/3! - y^2/5! + ...) */
+}
+
+/* asin(u) - u by its series through u^15 for 0 <= u <= 1/4 (truncation < 1e-12 of u) */
+__device__ __forceinline__ float asin_minus_arg(float u) {
+  const float u2 = u * u;
+  float p = 143.0f / 10240.0f;
+  p = fmaf(p, u2, 231.0f / 13312.0f);
+  p = fmaf(p, u2, 63.0f / 2816.0f);
+  p = fmaf(p, u2, 35.0f / 1152.0f);
+  p = fmaf(p, u2, 5.0f / 112.0f);
+  p = fmaf(p, u2, 3.0f / 40.0f);
+  p = fmaf(p, u2, 1.0f / 6.0f);
+  return u * u2 * p;
 }
 
 /* Fast mixed-precision decision for one candidate.  Returns 0 outside, 1 inside with
-   (ir, fr) or zero value, 2 when the exact path must decide. */
+   (ir, fr) or zero value, 2 when the exact path must decide.
+   The chord^2 between the candidate's centre and the disc centre is formed as a
+   float-float (~44 bits): c2 = A + B sin^2(y), y = x pi / npr.  Its high word decides
+   against the certainly-inside / certainly-outside thresholds.  Inside, the angle
+   2 asin(sqrt(c2) / 2) is carried to ~1e-11 and rounded to float, which is the
+   reference's real(angdist(...)) (haloproject.f90:66) except within ~1e-11 of a rounding
+   tie; from there r, log r and the table indices are the reference's float sequence
+   (maptable.f90:185-202), so the pixel's value is the reference's bit for bit. */
 __device__ __forceinline__ int fast_decide(const PaintParams &P, const RingItem &it,
                                            const HotHalo &H, int k, int &ir, float &fr,
                                            bool &zero_val, float &u_out) {
-  float x = (float)(item_n0(it) + k) + it.f0;
-  float s = sin_half_offset(x * it.hdphi);
-  float c2 = it.A + it.B * (s * s);
+  const ffloat x = ff_add_f(ff_two_sum((float)(item_n0(it) + k), it.f0), it.f0l);
+  const ffloat y = ff_mul(x, {it.hdphi, it.hdl});
+  const ffloat sy = ff_add_f(y, sin_minus_arg(y.h));
+  const ffloat c2f = ff_add({it.A, it.Al}, ff_mul({it.B, it.Bl}, ff_sqr(sy)));
+  const float c2 = c2f.h;
   if (c2 >= H.C_out) return 0;
   if (c2 > H.C_in) return 2;
   zero_val = false;
-  float h2 = 0.25f * c2;
-  float cosd = 1.0f - 2.0f * h2;
-  if (cosd < 0.05f) return 2;
-  float sind = 2.0f * sqrtf(h2 * (1.0f - h2));
-  float r = H.chi_t * (sind / cosd);
+  const ffloat uf = ff_sqrt(c2f);
+  const float u = 0.5f * uf.h;
+  if (u > 0.25f) return 2; /* discs wider than ~29 degrees: the exact path */
+  /* angle = 2 asin(chord / 2) = chord + 2 (asin(u) - u), u = chord / 2 */
+  const ffloat ang = ff_add_f(uf, 2.0f * asin_minus_arg(u));
+  const float angle = ang.h; /* hi = the float nearest hi + lo */
+  const float r = FMUL(H.chi_t, p2m_tanf(angle));
   const float dr = 1e-5f;
   if (r > P.th.rmaxt * (1.0f + dr)) {
     zero_val = true;
@@ -1152,14 +1207,14 @@ __device__ __forceinline__ int fast_decide(const PaintParams &P, const RingItem 
   /* the reference's log (the same float function as the exact path and the oracle):
      fr is a difference of logs that cancels to ~drt, so a cruder log's error of a few
      ulp of log r would move the value by ~1e-7 relative, and coherently over a disc */
-  float lr = p2m_logf(r);
-  float u = (lr - P.th.lrmin) * P.inv_drt;
-  int iu = (int)u;
-  float fu = u - (float)iu;
+  const float lr = p2m_logf(r);
+  const float uu = (lr - P.th.lrmin) * P.inv_drt;
+  const int iu = (int)uu;
+  const float fu = uu - (float)iu;
   if (fu < P.band_u || fu > 1.0f - P.band_u || iu < 0 || iu > P.th.nrt - 2) return 2;
   ir = iu + 1;
   fr = FSUB(lr, FADD(P.th.lrmin, FMUL((float)(ir - 1), P.th.drt)));
-  u_out = u;
+  u_out = uu;
   return 1;
 }
 
@@ -1362,6 +1417,7 @@ struct WarpStage {
   float gzh[32], gzl[32], gsh[32], gsl[32], gph[32], gpl[32], gcs[32];
   int girlo[32];
   float iA[32], iB[32], if0[32], ihd[32];
+  float iAl[32], iBl[32], if0l[32], ihdl[32];
   int ilo[32], in0[32], inpr[32], ij[32];
   long long irb[32]; /* RING index of the item ring's first pixel */
 };
@@ -1439,6 +1495,10 @@ __global__ void __launch_bounds__(P2M_HALOS_THREADS, P2M_HALOS_MINBLOCKS)
         p2m_ring_info(P.nside, ring, &npr, &ks, &npn);
         S.iA[lane] = it.A;
         S.iB[lane] = it.B;
+        S.iAl[lane] = it.Al;
+        S.iBl[lane] = it.Bl;
+        S.if0l[lane] = it.f0l;
+        S.ihdl[lane] = it.hdl;
         S.if0[lane] = it.f0;
         S.ihd[lane] = it.hdphi;
         S.ilo[lane] = it.lo;
@@ -1467,6 +1527,10 @@ __global__ void __launch_bounds__(P2M_HALOS_THREADS, P2M_HALOS_MINBLOCKS)
           ci.count = 0;
           ci.A = S.iA[i];
           ci.B = S.iB[i];
+          ci.Al = S.iAl[i];
+          ci.Bl = S.iBl[i];
+          ci.f0l = S.if0l[i];
+          ci.hdl = S.ihdl[i];
           ci.f0 = S.if0[i];
           ci.hdphi = S.ihd[i];
           const int np = S.inpr[i];
@@ -1676,6 +1740,59 @@ __global__ void __launch_bounds__(256) k_map_sum(const float *map, long long n, 
   double s = (double)hi + (double)lo;
   for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(FULL, s, o);
   if ((threadIdx.x & 31) == 0 && s != 0.0) atomicAdd(sum, s);
+}
+
+/* The statistics of pks2map.f90:321-346 over one float map, in one pass: sums of x, x^2
+   and x^3 (float-float per thread: x^2 by an exact two-product, x^3 as its float-float
+   product with x; FP64 only for the per-thread totals) and, with hist, the counts of the
+   P(<y) bins: m = int(x / dy) + 1 in float (:344), counted where 1 <= m <= nbins (:345).
+   The bins' counters are in shared memory; lanes of a warp that fall in the same bin
+   (most pixels of a y map are in bin 1) are added once by the lowest of them. */
+#define P2M_STATS_THREADS 512
+__global__ void __launch_bounds__(P2M_STATS_THREADS) k_map_stats(const float *map, long long n,
+                                                                double *sums,
+                                                                unsigned int *hist, int nbins,
+                                                                float dy) {
+  extern __shared__ unsigned int s_hist[];
+  if (hist)
+    for (int b = threadIdx.x; b < nbins; b += blockDim.x) s_hist[b] = 0u;
+  __syncthreads();
+  ffloat s1 = {0.0f, 0.0f}, s2 = {0.0f, 0.0f}, s3 = {0.0f, 0.0f};
+  const int lane = threadIdx.x & 31;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long base = (long long)blockIdx.x * blockDim.x; base < n; base += stride) {
+    const long long p = base + threadIdx.x;
+    const bool in = p < n;
+    const float x = in ? map[p] : 0.0f;
+    if (x != 0.0f) {
+      const float q2 = __fmul_rn(x, x);
+      const ffloat x2 = {q2, __fmaf_rn(x, x, -q2)};
+      s1 = ff_add_f(s1, x);
+      s2 = ff_add(s2, x2);
+      s3 = ff_add(s3, ff_mul_f(x2, x));
+    }
+    if (hist) {
+      int m = 0;
+      if (in) {
+        const float q = __fdiv_rn(x, dy);
+        if (q > -1.0f && q < (float)nbins) m = (int)q + 1;
+      }
+      const unsigned same = __match_any_sync(FULL, m);
+      if (m > 0 && lane == __ffs(same) - 1) atomicAdd(&s_hist[m - 1], (unsigned)__popc(same));
+    }
+  }
+  double d[3] = {(double)s1.h + (double)s1.l, (double)s2.h + (double)s2.l,
+                 (double)s3.h + (double)s3.l};
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    for (int o = 16; o > 0; o >>= 1) d[k] += __shfl_down_sync(FULL, d[k], o);
+    if (lane == 0 && d[k] != 0.0) atomicAdd(&sums[k], d[k]);
+  }
+  if (hist) {
+    __syncthreads();
+    for (int b = threadIdx.x; b < nbins; b += blockDim.x)
+      if (s_hist[b]) atomicAdd(&hist[b], s_hist[b]);
+  }
 }
 
 /* flat-sky accumulator -> float map */
@@ -2000,6 +2117,25 @@ void p2m_launch_ring_unhist(const int *keys, long long n, unsigned int *hist, cu
 }
 void p2m_launch_copy_counters(const DevCounters *d, DevCounters *h_mapped, cudaStream_t s) {
   k_copy_counters<<<1, 64, 0, s>>>(d, h_mapped);
+}
+void p2m_launch_map_stats(const float *map, long long n, double *sums, unsigned int *hist,
+                          int nbins, float dy, cudaStream_t s, int nsm) {
+  /* nbins <= 12288: the counters fit the default 48 KB of dynamic shared memory */
+  const size_t smem = hist ? sizeof(unsigned int) * (size_t)nbins : 0;
+  k_map_stats<<<grid_for(n, P2M_STATS_THREADS, nsm, 2), P2M_STATS_THREADS, smem, s>>>(
+      map, n, sums, hist, nbins, dy);
+}
+/* float map -> big-endian IEEE words (the byte order of FITS data) */
+__global__ void __launch_bounds__(256) k_to_big_endian(const float *__restrict__ in,
+                                                       unsigned int *__restrict__ out,
+                                                       long long n) {
+  for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < n;
+       p += (long long)gridDim.x * blockDim.x)
+    out[p] = __byte_perm(__float_as_uint(in[p]), 0u, 0x0123);
+}
+void p2m_launch_to_big_endian(const float *in, unsigned int *out, long long n, cudaStream_t s,
+                              int nsm) {
+  k_to_big_endian<<<grid_for(n, 256, nsm, 8), 256, 0, s>>>(in, out, n);
 }
 void p2m_launch_map_sum(const float *map, long long n, double *sum, cudaStream_t s, int nsm) {
   k_map_sum<<<grid_for(n, 256, nsm, 8), 256, 0, s>>>(map, n, sum);

@@ -23,6 +23,7 @@
 
 #include "../../include/p2m.h"
 #include "../../include/p2m_tools.h"
+#include "p2m_fits.h"
 
 namespace {
 
@@ -31,7 +32,7 @@ const float kDpdyMax = 1e-4f;
 
 struct File {
   FILE *f;
-  explicit File(const char *path) : f(std::fopen(path, "wb")) {}
+  explicit File(const char *path) : f(path ? std::fopen(path, "wb") : nullptr) {}
   ~File() {
     if (f) std::fclose(f);
   }
@@ -123,12 +124,29 @@ int32_t p2m_write_flatsky(const char *path, const float *map, int32_t npix, floa
 int32_t p2m_write_healpix_fits(const char *path, const float *map, int32_t nside) {
   if (!path || !map || nside < 1) return P2M_ERR_BADARG;
   const long long npix = 12LL * nside * nside;
+  File f(path);
+  if (!f.f) return P2M_ERR_IO;
+  if (p2m_fits_put_header(f.f, nside) != P2M_OK) return P2M_ERR_IO;
+  std::vector<uint32_t> buf(1 << 20);
+  for (long long i0 = 0; i0 < npix; i0 += (long long)buf.size()) {
+    const long long n = std::min<long long>((long long)buf.size(), npix - i0);
+    for (long long k = 0; k < n; k++) buf[(size_t)k] = to_big_endian(map[i0 + k]);
+    if (!f.put(buf.data(), sizeof(uint32_t) * (size_t)n)) return P2M_ERR_IO;
+  }
+  return p2m_fits_put_padding(f.f, nside);
+}
+
+}  // extern "C"
+
+/* the two headers of a HEALPix FITS map (an empty primary HDU, then the BINTABLE) */
+int32_t p2m_fits_put_header(FILE *fp, int32_t nside) {
+  const long long npix = 12LL * nside * nside;
   /* fits_s_inc.f90:904-908: rows of 1024 values (1 for npix < 1024) */
   long long repeat = npix < 1024 ? 1 : 1024;
   if (nside > 1024 * 256) repeat = nside / 256;
   const long long nrows = npix / repeat;
-  File f(path);
-  if (!f.f) return P2M_ERR_IO;
+  File f(nullptr);
+  f.f = fp;
   char date[16];
   std::time_t now = std::time(nullptr);
   std::strftime(date, sizeof date, "%Y-%m-%d", std::gmtime(&now));
@@ -153,17 +171,15 @@ int32_t p2m_write_healpix_fits(const char *path, const float *map, int32_t nside
       card_value("TFORM1", quoted(form), "data format of field: 4-byte REAL"),
       card_value("NSIDE", fixed(nside), "the nside of the map"),
       card_value("ORDERING", quoted("RING"), "the nside of the map")};
-  if (!put_header(f, ext)) return P2M_ERR_IO;
-  std::vector<uint32_t> buf(1 << 20);
-  for (long long i0 = 0; i0 < npix; i0 += (long long)buf.size()) {
-    const long long n = std::min<long long>((long long)buf.size(), npix - i0);
-    for (long long k = 0; k < n; k++) buf[(size_t)k] = to_big_endian(map[i0 + k]);
-    if (!f.put(buf.data(), sizeof(uint32_t) * (size_t)n)) return P2M_ERR_IO;
-  }
-  const long long data = 4 * npix, pad = (data + 2879) / 2880 * 2880 - data;
-  std::vector<char> zeros((size_t)pad, 0);
-  if (pad && !f.put(zeros.data(), (size_t)pad)) return P2M_ERR_IO;
-  return P2M_OK;
+  const bool ok = put_header(f, ext);
+  f.f = nullptr; /* the caller owns the stream */
+  return ok ? P2M_OK : P2M_ERR_IO;
 }
 
-}  // extern "C"
+/* the zero bytes that complete the data of a map's BINTABLE to whole 2880-byte blocks */
+int32_t p2m_fits_put_padding(FILE *fp, int32_t nside) {
+  const long long data = 4 * 12LL * nside * nside, pad = (data + 2879) / 2880 * 2880 - data;
+  std::vector<char> zeros((size_t)pad, 0);
+  if (pad && std::fwrite(zeros.data(), 1, (size_t)pad, fp) != (size_t)pad) return P2M_ERR_IO;
+  return P2M_OK;
+}

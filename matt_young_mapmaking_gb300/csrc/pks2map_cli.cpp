@@ -12,13 +12,21 @@
  * device (P2M_DEVICE, default 0).  scramble and center follow the reference's random
  * stream and rotation; P2M_RANKS (default 1, at most 25) is the MPI rank count whose
  * halo blocks and streams they reproduce (`mpirun -np <ranks> pks2map ...`).
+ *
+ * The catalogue is read in steps of 4M records, each step's file read overlapping the
+ * painting of the step before; the moments, RMS and P(<y) are computed on the device;
+ * the FITS map is written from the device in slices whose copies overlap the file
+ * write.  P2M_TIMING set in the environment prints the phase times to stderr.
  */
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <ctime>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/p2m.h"
@@ -29,6 +37,12 @@
 namespace {
 
 bool is_dot(const char *s) { return std::strcmp(s, ".") == 0; }
+
+double now_s() {
+  struct timespec ts;
+  clock_gettime(CLOCK_MONOTONIC, &ts);
+  return (double)ts.tv_sec + 1e-9 * (double)ts.tv_nsec;
+}
 
 /* textlib.f90 i4arg / r4arg: default when absent, a single dot, or unparsable */
 int i4arg(int argc, char **argv, int k, int def) {
@@ -142,16 +156,28 @@ int main(int argc, char **argv) {
                 f42(p2m_lookup(rofz.data(), cosmo.drofz, zmax) / 1e3f).c_str());
   }
 
-  std::vector<char> table, cat;
+  const double t_start = now_s();
+  std::vector<char> table;
   if (!read_file(tablefile, table)) return fail("cannot read the table file");
-  if (!read_file(filein, cat) || cat.size() < 8) return fail("cannot read the catalogue");
+  FILE *cf = std::fopen(filein, "rb");
+  if (!cf) return fail("cannot read the catalogue");
+  std::fseek(cf, 0, SEEK_END);
+  const long long fsize = std::ftell(cf);
+  std::fseek(cf, 0, SEEK_SET);
   int32_t nhalo = 0;
-  std::memcpy(&nhalo, cat.data(), 4);
+  if (fsize < 8 || std::fread(&nhalo, 4, 1, cf) != 1) {
+    std::fclose(cf);
+    return fail("cannot read the catalogue");
+  }
   /* 7 floats after a 2-word header (pksc.f90:46-66) or 10 after a 3-word header */
   int nfloat = 0, hdr = 0;
-  if (nhalo >= 0 && cat.size() == 8 + 28ull * (size_t)nhalo) nfloat = 7, hdr = 8;
-  else if (nhalo >= 0 && cat.size() == 12 + 40ull * (size_t)nhalo) nfloat = 10, hdr = 12;
-  if (!nfloat) return fail("catalogue size matches neither 8+28N nor 12+40N bytes");
+  if (nhalo >= 0 && fsize == 8 + 28LL * nhalo) nfloat = 7, hdr = 8;
+  else if (nhalo >= 0 && fsize == 12 + 40LL * nhalo) nfloat = 10, hdr = 12;
+  if (!nfloat) {
+    std::fclose(cf);
+    return fail("catalogue size matches neither 8+28N nor 12+40N bytes");
+  }
+  std::fseek(cf, hdr, SEEK_SET);
 
   p2m_config cfg;
   std::memset(&cfg, 0, sizeof cfg);
@@ -171,18 +197,56 @@ int main(int argc, char **argv) {
   cfg.nmaps = 1;
   cfg.map_table[0] = 0;
   cfg.map_profile[0] = profile;
-  cfg.max_records = nhalo < (1 << 22) ? (nhalo > 0 ? nhalo : 1) : (1 << 22);
+  const long long chunk = 1LL << 22; /* records per read and paint step */
+  cfg.max_records = nhalo < chunk ? (nhalo > 0 ? nhalo : 1) : chunk;
   if (scramble || centre) cfg.max_records = nhalo > 0 ? nhalo : 1; /* one pass: one catalogue */
   cfg.device = std::getenv("P2M_DEVICE") ? std::atoi(std::getenv("P2M_DEVICE")) : 0;
   p2m_ctx *ctx = nullptr;
   int st = p2m_create(&cfg, &ctx);
-  if (st) return fail("p2m_create", ctx, st);
-
+  if (st) {
+    std::fclose(cf);
+    return fail("p2m_create", ctx, st);
+  }
   st = p2m_load_table(ctx, 0, table.data(), (int64_t)table.size());
-  if (st) return fail("p2m_load_table", ctx, st);
-  if ((st = p2m_set_preprocess(ctx, scramble, centre, ranks))) return fail("p2m_set_preprocess", ctx, st);
-  st = p2m_paint_records(ctx, (const float *)(cat.data() + hdr), nhalo, nfloat);
-  if (st) return fail("p2m_paint_records", ctx, st);
+  if (st) {
+    std::fclose(cf);
+    return fail("p2m_load_table", ctx, st);
+  }
+  if ((st = p2m_set_preprocess(ctx, scramble, centre, ranks))) {
+    std::fclose(cf);
+    return fail("p2m_set_preprocess", ctx, st);
+  }
+  /* the catalogue is read in steps of max_records records; a reader thread reads step
+     k + 1 from the file while step k is painted */
+  {
+    const long long step = cfg.max_records;
+    std::vector<float> buf[2];
+    bool read_ok[2] = {true, true};
+    auto read_step = [&](int b, long long first) {
+      const long long n = std::min<long long>(step, (long long)nhalo - first);
+      buf[b].resize((size_t)(n * nfloat));
+      read_ok[b] = n <= 0 ||
+                   std::fread(buf[b].data(), sizeof(float) * nfloat, (size_t)n, cf) == (size_t)n;
+    };
+    read_step(0, 0);
+    for (long long first = 0, k = 0; first < nhalo; first += step, k++) {
+      const int b = (int)(k & 1);
+      std::thread reader;
+      if (first + step < nhalo) reader = std::thread(read_step, 1 - b, first + step);
+      if (read_ok[b])
+        st = p2m_paint_records(ctx, buf[b].data(), (int64_t)(buf[b].size() / nfloat), nfloat);
+      if (reader.joinable()) reader.join();
+      if (!read_ok[b]) {
+        std::fclose(cf);
+        return fail("cannot read the catalogue", ctx);
+      }
+      if (st) {
+        std::fclose(cf);
+        return fail("p2m_paint_records", ctx, st);
+      }
+    }
+  }
+  std::fclose(cf);
   if (centre) {
     /* pks2map.f90:205-209 and :250-254 */
     float c[9];
@@ -195,57 +259,46 @@ int main(int argc, char **argv) {
                 e103(c[8]).c_str());
   }
 
-  std::vector<float> hp((size_t)(nside > 0 ? hpnpix : 0)), fs((size_t)npix * (size_t)npix);
-  if (nside > 0 && (st = p2m_get_healpix(ctx, 0, hp.data()))) return fail("p2m_get_healpix", ctx, st);
-  if (npix > 0 && (st = p2m_get_flatsky(ctx, 0, fs.data()))) return fail("p2m_get_flatsky", ctx, st);
+  /* pks2map.f90:318-357: halo count, moments, RMS and mean, P(<y): on the device */
   p2m_stats stats;
   if ((st = p2m_get_stats(ctx, &stats))) return fail("p2m_get_stats", ctx, st);
-  p2m_destroy(ctx);
-
-  /* pks2map.f90:318-338: halo count, moments, RMS and mean */
+  const double t_paint = now_s();
+  p2m_map_stats hs, fss;
+  std::memset(&hs, 0, sizeof hs);
+  std::memset(&fss, 0, sizeof fss);
+  std::vector<float> dpdy(P2M_NDPDY);
+  if (nside > 0 && (st = p2m_get_healpix_stats(ctx, 0, &hs, dpdy.data())))
+    return fail("p2m_get_healpix_stats", ctx, st);
+  if (npix > 0 && (st = p2m_get_flatsky_stats(ctx, 0, &fss)))
+    return fail("p2m_get_flatsky_stats", ctx, st);
+  const double t_stats = now_s();
   std::printf("Number of halos in map:    %lld\n", (long long)stats.n_painted);
-  double fm[3] = {0, 0, 0}, hm[3] = {0, 0, 0};
-  for (float v : fs) {
-    double x = v;
-    fm[0] += x;
-    fm[1] += x * x;
-    fm[2] += x * x * x;
-  }
-  for (float v : hp) {
-    double x = v;
-    hm[0] += x;
-    hm[1] += x * x;
-    hm[2] += x * x * x;
-  }
-  const double nfs = fs.empty() ? 1.0 : (double)fs.size(), nhp = hp.empty() ? 1.0 : (double)hp.size();
-  for (int k = 0; k < 3; k++) {
-    fm[k] /= nfs;
-    hm[k] /= nhp;
-  }
-  std::printf("Flatsky moments:    %s %s %s \n", fe(fm[0], 3).c_str(), fe(fm[1], 3).c_str(),
-              fe(fm[2], 3).c_str());
-  std::printf("Healpix moments:    %s %s %s \n", fe(hm[0], 3).c_str(), fe(hm[1], 3).c_str(),
-              fe(hm[2], 3).c_str());
-  double fv = 0, hv = 0;
-  for (float v : fs) fv += ((double)v - fm[0]) * ((double)v - fm[0]);
-  for (float v : hp) hv += ((double)v - hm[0]) * ((double)v - hm[0]);
+  std::printf("Flatsky moments:    %s %s %s \n", fe(fss.mom[0], 3).c_str(), fe(fss.mom[1], 3).c_str(),
+              fe(fss.mom[2], 3).c_str());
+  std::printf("Healpix moments:    %s %s %s \n", fe(hs.mom[0], 3).c_str(), fe(hs.mom[1], 3).c_str(),
+              fe(hs.mom[2], 3).c_str());
   std::printf("Flatsky RMS:                %s\nFlatsky Mean:               %s\n",
-              fe(std::sqrt(fv / nfs), 3).c_str(), fe(fm[0], 2).c_str());
+              fe(fss.rms, 3).c_str(), fe(fss.mom[0], 2).c_str());
   std::printf("Healpix RMS:                %s\nHealpix Mean:               %s\n\n",
-              fe(std::sqrt(hv / nhp), 3).c_str(), fe(hm[0], 2).c_str());
+              fe(hs.rms, 3).c_str(), fe(hs.mom[0], 2).c_str());
 
-  /* pks2map.f90:340-385: P(<y), then the three files */
+  /* pks2map.f90:359-385: the three files */
   const std::string out = fileout;
-  if (nside > 0) {
-    std::vector<float> dpdy(P2M_NDPDY);
-    if ((st = p2m_dpdy(hp.data(), hpnpix, dpdy.data()))) return fail("p2m_dpdy", nullptr, st);
-    if ((st = p2m_write_dpdy((out + "_dp.bin").c_str(), dpdy.data())))
-      return fail("cannot write _dp.bin", nullptr, st);
-  }
+  if (nside > 0 && (st = p2m_write_dpdy((out + "_dp.bin").c_str(), dpdy.data())))
+    return fail("cannot write _dp.bin", ctx, st);
+  std::vector<float> fs((size_t)npix * (size_t)npix);
+  if (npix > 0 && (st = p2m_get_flatsky(ctx, 0, fs.data()))) return fail("p2m_get_flatsky", ctx, st);
   if ((st = p2m_write_flatsky((out + "_fs.map").c_str(), fs.data(), npix, fov)))
-    return fail("cannot write _fs.map", nullptr, st);
-  if (nside > 0 && (st = p2m_write_healpix_fits((out + "_hp.fits").c_str(), hp.data(), nside)))
-    return fail("cannot write _hp.fits", nullptr, st);
+    return fail("cannot write _fs.map", ctx, st);
+  if (nside > 0 && (st = p2m_write_healpix_fits_device(ctx, 0, (out + "_hp.fits").c_str())))
+    return fail("cannot write _hp.fits", ctx, st);
+  p2m_destroy(ctx);
+  const double t_end = now_s();
   std::printf("\n");
+  if (std::getenv("P2M_TIMING"))
+    std::fprintf(stderr,
+                 "pks2map timing: read + paint %.4f s, statistics %.4f s, writes %.4f s, "
+                 "total %.4f s\n",
+                 t_paint - t_start, t_stats - t_paint, t_end - t_stats, t_end - t_start);
   return 0;
 }

@@ -92,6 +92,8 @@ def lib():
         L.orc_query_disc.restype = I64
         L.orc_paint.argtypes = [VP, VP, I32, VP, I64, VP, VP, VP, VP, VP, I64, VP]
         L.orc_paint.restype = I32
+        L.orc_map_stats.argtypes = [VP, I64, VP, VP, VP]
+        L.orc_map_stats.restype = None
         L.orc_generate_catalogue.argtypes = [ctypes.c_uint64, I64, I64, I32, D, D, D, D, D,
                                              D, VP, I32]
         L.orc_generate_catalogue.restype = I32
@@ -333,6 +335,17 @@ def generate_catalogue(seed, n, nfloat=10, r=(100.0, 3000.0), m=(1e12, 1e15), sl
     if rc:
         raise ValueError("generate_catalogue: bad arguments")
     return out
+
+
+def map_stats(m, dpdy=True):
+    """pks2map.f90:321-357 over a float map: (moments[3], rms, dpdy[10000] or None)"""
+    a = np.ascontiguousarray(m, dtype=np.float32)
+    mom = np.zeros(3)
+    rms = ctypes.c_double()
+    dp = np.zeros(10000, dtype=np.float32) if dpdy else None
+    lib().orc_map_stats(_p(a), a.size, _p(mom), ctypes.byref(rms),
+                        _p(dp) if dp is not None else None)
+    return mom, rms.value, dp
 
 
 def fmath(fn, x, y=None):

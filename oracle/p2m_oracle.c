@@ -1376,3 +1376,42 @@ int orc_generate_catalogue(uint64_t seed, int64_t first, int64_t n, int nfloat, 
   }
   return 0;
 }
+
+/* --------------------------------------------------------- map statistics ------- */
+
+/* pks2map.f90:321-357 over one float map: moments sum(map**k) / n (k = 1..3, :321-327)
+   and RMS sqrt(sum((map - mom1)**2) / n) (:329-334), summed in FP64 in pixel order (the
+   reference's `sum` of a real array accumulates in float in a compiler-chosen order; FP64
+   is the value that rounding approximates); with dpdy, P(<y) (:340-357): bin
+   m = int(y / dpdy_dy) + 1 with dpdy_dy = dpdy_max / ndpdy = 1e-4 / 10000 in float,
+   counted in a float array (a count stops at 2^24), divided by real(n), then cumulated. */
+void orc_map_stats(const float *map, int64_t n, double mom[3], double *rms, float *dpdy) {
+  double s1 = 0.0, s2 = 0.0, s3 = 0.0;
+  for (int64_t i = 0; i < n; i++) {
+    const double x = (double)map[i];
+    s1 = s1 + x;
+    s2 = s2 + x * x;
+    s3 = s3 + (x * x) * x;
+  }
+  mom[0] = s1 / (double)n;
+  mom[1] = s2 / (double)n;
+  mom[2] = s3 / (double)n;
+  double v = 0.0;
+  for (int64_t i = 0; i < n; i++) {
+    const double d = (double)map[i] - mom[0];
+    v = v + d * d;
+  }
+  *rms = sqrt(v / (double)n);
+  if (!dpdy) return;
+  const int ndpdy = 10000;
+  const float dy = 1e-4f / (float)ndpdy;
+  for (int k = 0; k < ndpdy; k++) dpdy[k] = 0.0f;
+  for (int64_t i = 0; i < n; i++) {
+    const float q = map[i] / dy;
+    if (!(q > -1.0f && q < (float)ndpdy)) continue; /* int() of it lies outside 0..ndpdy-1 */
+    const int m = (int)q + 1;
+    if (m > 0 && m <= ndpdy) dpdy[m - 1] = dpdy[m - 1] + 1.0f;
+  }
+  for (int k = 0; k < ndpdy; k++) dpdy[k] = dpdy[k] / (float)n;
+  for (int k = 1; k < ndpdy; k++) dpdy[k] = dpdy[k - 1] + dpdy[k];
+}

@@ -141,6 +141,10 @@ int orc_generate_catalogue(uint64_t seed, int64_t first, int64_t n, int nfloat, 
                            double r_max, double m_min, double m_max, double slope,
                            double sigma_v, float *out, int nthreads);
 
+/* pks2map.f90:321-357 over one float map: moments (k = 1..3), RMS and, with dpdy
+   non-null, the cumulative P(<y) of 10000 bins. */
+void orc_map_stats(const float *map, int64_t n, double mom[3], double *rms, float *dpdy);
+
 #ifdef __cplusplus
 }
 #endif

@@ -24,11 +24,20 @@ def masked_rel(a, b):
     return (np.abs(a[m] - b[m]) / np.abs(b[m])).max()
 
 
-@pytest.mark.parametrize("nfloat,profile,scramble,centre", [(10, 1, 0, 0), (7, 2, 0, 0),
-                                                             (10, 1, 1, 1)])
-def test_pks2map_command_line(tmp_path, nfloat, profile, scramble, centre):
+def fe3(v):
+    """Fortran 1pe9.3 / 1pe10.3 of the report lines"""
+    return "%.3E" % v
+
+
+@pytest.mark.parametrize("nfloat,profile,scramble,centre,n", [(10, 1, 0, 0, 30_000),
+                                                               (7, 2, 0, 0, 30_000),
+                                                               (10, 1, 1, 1, 30_000),
+                                                               (10, 1, 0, 0, 4_500_000)])
+def test_pks2map_command_line(tmp_path, nfloat, profile, scramble, centre, n):
+    """n = 4.5e6: the catalogue is read and painted in two steps of up to 4M records"""
     exe = os.path.join(PKG, "pks2map")
-    rec = catalogs.shell(41, 30_000, nfloat=nfloat)
+    rec = (catalogs.shell(41, n, nfloat=nfloat) if n <= 100_000 else
+           p2m.generate_catalogue(41, n, nfloat, r=(100.0, 3000.0), m=(1e12, 1e15)))
     cat = str(tmp_path / "halos.pksc")
     p2m.write_pksc(cat, rec)
     tab = catalogs.table()
@@ -60,8 +69,18 @@ def test_pks2map_command_line(tmp_path, nfloat, profile, scramble, centre):
     # and against the oracle
     p = oracle.params(nside=nside, npix_fs=npix, fov_deg=fov, zmax=zmax, maps=((0, profile),),
                       nfloat=nfloat, scramble=scramble, centre=centre)
-    ohp, ofs, ost, _ = oracle.paint(p, [oracle.Table(tab)], rec)
+    ohp, ofs, ost, _ = oracle.paint(p, [oracle.Table(tab)], rec, threads=os.cpu_count() or 1)
     assert masked_rel(hp, ohp[0]) <= 1e-5
     assert masked_rel(fs.ravel(), ofs[0]) <= 1e-6
     assert ost["n_painted"] == st["n_painted"]
     assert ("After rotation largest halo is at" in r.stdout) == bool(centre)
+
+    # the report's moments and RMS (computed on the device) and the P(<y) file against
+    # the oracle's restatement of pks2map.f90:321-357 over the written maps
+    hmom, hrms, hdp = oracle.map_stats(hp)
+    fmom, frms, _ = oracle.map_stats(fs.ravel(), dpdy=False)
+    assert np.array_equal(dp.view(np.uint32), hdp.view(np.uint32))
+    assert "Flatsky moments:    %s %s %s \n" % tuple(fe3(v) for v in fmom) in r.stdout
+    assert "Healpix moments:    %s %s %s \n" % tuple(fe3(v) for v in hmom) in r.stdout
+    assert "Healpix RMS:                %s\n" % fe3(hrms) in r.stdout
+    assert "Flatsky RMS:                %s\n" % fe3(frms) in r.stdout

@@ -99,6 +99,21 @@ def test_c2_headline_against_oracle(c2, precision, monkeypatch):
         (gkeys != rkeys).sum())
     for m, name in enumerate(("tSZ y", "kSZ")):
         compare_maps(hp[m], rhp[m], "%s %s" % (precision, name))
+    if precision == "mixed":
+        # the statistics of pks2map.f90:321-357 on the device over the 201M-pixel y map,
+        # whose first P(<y) bin passes the reference's float counter limit of 2^24
+        with p2m.Painter(nside=4096, precision=precision, maps=((0, 1), (0, 2)), zmax=6.0,
+                         max_records=len(rec)) as pt:
+            pt.load_table(0, tab)
+            pt.paint_records(rec)
+            mom, rms, dp = pt.map_stats(0)
+            y = pt.healpix(0)
+        rmom, rrms, rdp = oracle.map_stats(y)
+        for k in range(3):
+            assert abs(mom[k] - rmom[k]) <= 1e-10 * abs(rmom[k])
+        assert abs(rms - rrms) <= 1e-10 * rrms
+        assert np.array_equal(dp.view(np.uint32), rdp.view(np.uint32))
+        assert dp[0] == np.float32(16777216.0) / np.float32(y.size)
 
 
 def test_c2_gpu_table_is_the_oracle_table():
