@@ -57,6 +57,8 @@ def parse():
     ap.add_argument("--nside", type=int, default=NSIDE)
     ap.add_argument("--no-plain", action="store_true", help="skip the FP64 drop-in comparison")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-files", action="store_true",
+                    help="skip the command line's end-to-end run (file read to FITS written)")
     ap.add_argument("--no-parity", action="store_true",
                     help="skip the check of this run's maps and pixel sets against the oracle")
     ap.add_argument("--cl-lmax", type=int, default=2047,
@@ -508,6 +510,51 @@ def parity_vs_oracle(rec, table, nside, maps_mixed, maps_fp64, device):
     return out
 
 
+def e2e_files(rec, table, nside, precision):
+    """The drop-in end to end: the pks2map command line on the headline catalogue, from the
+    .pksc file read to <out>_hp.fits written (tSZ, profile 1, as one reference run paints
+    one profile; flat sky at the reference's default 16^2).  Its own clock (P2M_TIMING):
+    file read + paint, statistics, writes; and the whole process's wall time, CUDA
+    start-up included.  Files in a temporary directory, removed afterwards."""
+    import shutil
+    import tempfile
+
+    import matt_young_mapmaking_gb300 as p2m
+    exe = os.path.join(ROOT, "matt_young_mapmaking_gb300", "pks2map")
+    d = tempfile.mkdtemp(prefix="p2m_e2e_")
+    try:
+        cat, tab, out = os.path.join(d, "c2.pksc"), os.path.join(d, "table.bin"), os.path.join(d, "c2")
+        p2m.write_pksc(cat, rec)
+        p2m.write_table(tab, table)
+        args = [exe, cat, out, tab, "0.0", str(nside), "0", "0", "16", "10.0", str(ZMAX), "0.0",
+                "1", "1"]
+        env = dict(os.environ, P2M_TIMING="1", P2M_PRECISION=precision)
+        runs = []
+        for _ in range(3):
+            t0 = time.perf_counter()
+            r = subprocess.run(args, stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True,
+                               env=env, timeout=600)
+            wall = time.perf_counter() - t0
+            if r.returncode != 0:
+                return {"error": r.stderr.strip()[-300:]}
+            line = [x for x in r.stderr.splitlines() if x.startswith("pks2map timing:")][-1]
+            nums = [float(x) for x in line.replace(",", " ").split() if x[0].isdigit()]
+            runs.append((nums[3], nums[0], nums[1], nums[2], wall))
+        best = min(runs)
+        size = os.path.getsize(out + "_hp.fits")
+        return {"e2e_files_ms": 1e3 * best[0],
+                "read_paint_ms": 1e3 * best[1], "statistics_ms": 1e3 * best[2],
+                "writes_ms": 1e3 * best[3], "process_wall_ms": 1e3 * best[4],
+                "halos_per_s": len(rec) / best[0], "fits_bytes": size,
+                "pksc_bytes": os.path.getsize(cat),
+                "what": "pks2map %s <out> <table> 0.0 %d 0 0 16 10.0 %g 0.0 1 1: file read "
+                        "through _hp.fits written (its own clock, best of 3 runs); "
+                        "process_wall_ms adds process and CUDA start-up" % (
+                            os.path.basename(cat), nside, ZMAX)}
+    finally:
+        shutil.rmtree(d, ignore_errors=True)
+
+
 def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
@@ -784,6 +831,9 @@ def run_ours(args):
             "tuning": tunings.get("fixed"),
             "error_vs_fp64": {name: map_errors(fixed_maps[m], ref_maps[m])
                               for m, name in enumerate(("tsz", "ksz"))}}
+
+    if rank == 0 and ws == 1 and not args.no_files:
+        out["e2e_files"] = e2e_files(rec, table, nside, args.precision)
 
     # the other configurations' reports run in single-GPU runs only (replica runs time
     # the headline workload alone)

@@ -246,6 +246,7 @@ PaintParams make_params(const p2m_ctx *ctx, int nfloat) {
   P.full_grid = ctx->tune.full_grid;
   P.full_chunk = ctx->tune.full_chunk;
   P.halo_batch = ctx->tune.halo_batch;
+  P.err_flag = &ctx->d_ctr->err;
   P.cone_npix = ctx->cone_npix;
   if (ctx->th_set) {
     float fr;
@@ -305,6 +306,10 @@ p2m_status check_errors(p2m_ctx *ctx, cudaStream_t s) {
     return fail(ctx, P2M_ERR_STATE, "candidate walk exceeded its round bound (maps are incomplete)");
   if (err & P2M_DEVERR_FS_OVERFLOW)
     return fail(ctx, P2M_ERR_CAPACITY, "flat-sky row buffer overflow (maps are incomplete)");
+  if (err & P2M_DEVERR_FIXED)
+    return fail(ctx, P2M_ERR_CAPACITY,
+                "fixed-point accumulation out of range (a value or a pixel sum of 128 or more): "
+                "paint these tables with another precision");
   return P2M_OK;
 }
 

@@ -47,7 +47,8 @@ struct DevCounters {
 enum {
   P2M_DEVERR_FS_OVERFLOW = 2,
   P2M_DEVERR_RADIUS = 4,
-  P2M_DEVERR_ITEMS = 8
+  P2M_DEVERR_ITEMS = 8,
+  P2M_DEVERR_FIXED = 16 /* fixed-point accumulation: a value or a pixel sum out of range */
 };
 
 /* one enumerated halo */
@@ -121,6 +122,7 @@ struct PaintParams {
   int full_grid;         /* blocks per SM of k_paint_full */
   int full_chunk;        /* candidates per warp chunk of k_paint_full */
   int halo_batch;        /* halos per warp batch of k_paint_halos (1..32) */
+  unsigned int *err_flag; /* the device error word (DevCounters::err) */
 };
 
 /* buffers of one ingest call */

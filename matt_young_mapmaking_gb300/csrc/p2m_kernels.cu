@@ -874,8 +874,10 @@ __device__ __forceinline__ void accumulate_vals(const PaintParams &P, void *acc,
     unsigned long long *a = (unsigned long long *)acc + slot * P.nmaps;
 #pragma unroll
     for (int m = 0; m < P2M_MAXMAPS; m++)
-      if (m < P.nmaps && vals[m] != 0.0f)
+      if (m < P.nmaps && vals[m] != 0.0f) {
+        if (!(fabsf(vals[m]) < 128.0f)) atomicOr(P.err_flag, (unsigned)P2M_DEVERR_FIXED);
         atomicAdd(a + m, (unsigned long long)float_to_fixed(vals[m]));
+      }
   } else {
     float *a = (float *)acc + 2 * slot * P.nmaps;
     float olds[P2M_MAXMAPS];

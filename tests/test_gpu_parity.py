@@ -653,3 +653,26 @@ def test_cosmology_tables_entry_point():
             pt.set_cosmology_tables(rofz, zofr)
         pt.reset()
         pt.set_cosmology_tables(rofz, zofr)
+
+
+@pytest.mark.parametrize("big_rings", ["0", "1000000"])
+def test_fixed_point_range_is_reported(big_rings, monkeypatch):
+    """P2M_PREC_FIXED holds |value| < 128: a table in units that exceed it makes the
+    read-out fail with P2M_ERR_CAPACITY instead of returning saturated maps (both
+    painting paths); the same table paints normally with the other precisions."""
+    monkeypatch.setenv("P2M_BIG_RINGS", big_rings)
+    rec = catalogs.shell(15, 5_000)
+    tab = bytearray(catalogs.table())
+    vals = np.frombuffer(tab, dtype=np.float32, offset=36)
+    big = (vals * np.float32(1e9)).astype(np.float32)  # y ~ 1e-6 .. 1e-4 -> 1e3 .. 1e5
+    tab[36:] = big.tobytes()
+    with p2m.Painter(nside=128, precision="fixed", max_records=len(rec)) as pt:
+        pt.load_table(0, bytes(tab))
+        pt.paint_records(rec)
+        with pytest.raises(p2m.P2MError) as e:
+            pt.healpix(0)
+        assert e.value.status == p2m.capi.P2M_ERR_CAPACITY
+    with p2m.Painter(nside=128, precision="mixed", max_records=len(rec)) as pt:
+        pt.load_table(0, bytes(tab))
+        pt.paint_records(rec)
+        assert np.abs(pt.healpix(0)).max() >= 128.0
