@@ -76,14 +76,21 @@ typedef struct p2m_tuning {
                          the set-up counts the keys, the paint scans and scatters them), so
                          that the halos in flight cover a narrow band of the maps; 0: in
                          catalogue order; 1 */
+  int32_t halos_threads; /* threads per block of the fused kernel, 128 or 256 (halos_grid
+                            blocks of them per SM); 128 */
+  /* No table-tile field: the profile tables are read through the read-only cache
+     (__ldg), not staged in shared-memory tiles.  A table is 16 MB at the reference's
+     100 x 100 x 200 size and stays in L2; its loads hit L1/L2, and shared memory holds
+     the fused kernel's per-warp stage instead. */
   float ms;           /* p2m_autotune: device time of one paint call with the choice */
 } p2m_tuning;
 int32_t p2m_get_tuning(struct p2m_ctx *ctx, p2m_tuning *out);
 int32_t p2m_set_tuning(struct p2m_ctx *ctx, const p2m_tuning *t);
 /* Autotuner: paints the caller's catalogue (device records, as p2m_paint_records_device)
    with candidate launch parameters and keeps the fastest.  The search is coordinate
-   descent: big_rings, then the fused kernel's grid, then the stored-item kernel's grid,
-   then its chunk, then the painting order, then the fused kernel's batch.  Each candidate is timed by device events around the whole paint call
+   descent: big_rings, then the fused kernel's block size and grid, then the stored-item
+   kernel's grid, then its chunk, then the painting order, then the fused kernel's
+   batch.  Each candidate is timed by device events around the whole paint call
    (reset, ingest, sweep), best of `reps`.  The maps are reset before the first and after
    the last candidate.  Writes the choice to *out when out is not NULL. */
 int32_t p2m_autotune(struct p2m_ctx *ctx, const float *d_records, int64_t nrec, int32_t nfloat,

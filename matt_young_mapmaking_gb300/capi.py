@@ -59,7 +59,7 @@ class P2MTuning(ctypes.Structure):
                 ("full_grid", ctypes.c_int32), ("full_chunk", ctypes.c_int32),
                 ("stream_chunk", ctypes.c_int32), ("stream_paint", ctypes.c_int32),
                 ("halo_batch", ctypes.c_int32), ("sort_halos", ctypes.c_int32),
-                ("ms", ctypes.c_float)]
+                ("halos_threads", ctypes.c_int32), ("ms", ctypes.c_float)]
 
 
 class P2MStats(ctypes.Structure):

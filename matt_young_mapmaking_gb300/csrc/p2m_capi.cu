@@ -51,7 +51,7 @@ struct p2m_ctx {
   bool th_set = false;
   float *d_tab[P2M_MAXTABLES] = {};
   float band_u = 2e-4f;
-  p2m_tuning tune = {P2M_BIG_RINGS, 8, 8, 1024, (int32_t)P2M_STREAM_CHUNK, 1, 16, 1, 0.0f};
+  p2m_tuning tune = {P2M_BIG_RINGS, 8, 8, 1024, (int32_t)P2M_STREAM_CHUNK, 1, 16, 1, 128, 0.0f};
   /* painting order (p2m_tuning.sort_halos): counting sort by first ring */
   int *d_order = nullptr, *d_ring_key = nullptr;
   long long cap_order = 0, cap_ring_key = 0;
@@ -246,6 +246,7 @@ PaintParams make_params(const p2m_ctx *ctx, int nfloat) {
   P.full_grid = ctx->tune.full_grid;
   P.full_chunk = ctx->tune.full_chunk;
   P.halo_batch = ctx->tune.halo_batch;
+  P.halos_threads = ctx->tune.halos_threads;
   P.err_flag = &ctx->d_ctr->err;
   P.cone_npix = ctx->cone_npix;
   if (ctx->th_set) {
@@ -1139,7 +1140,8 @@ bool tuning_ok(const p2m_tuning &t) {
          t.full_grid >= 1 && t.full_grid <= 32 && t.full_chunk >= 32 && t.full_chunk <= 65536 &&
          t.stream_chunk >= 65536 && t.stream_chunk <= (1 << 26) &&
          (t.stream_paint == 0 || t.stream_paint == 1) && t.halo_batch >= 1 &&
-         t.halo_batch <= 32 && (t.sort_halos == 0 || t.sort_halos == 1);
+         t.halo_batch <= 32 && (t.sort_halos == 0 || t.sort_halos == 1) &&
+         (t.halos_threads == 128 || t.halos_threads == 256);
 }
 
 struct EventPair {
@@ -1213,6 +1215,15 @@ int32_t p2m_autotune(p2m_ctx *ctx, const float *d_records, int64_t nrec, int32_t
     return P2M_OK;
   };
   p2m_status st = descend(kBig, 8, &p2m_tuning::big_rings);
+  if (!st) {
+    /* the other block size, with the grid that keeps the same warps per SM */
+    p2m_tuning t = best;
+    t.halos_threads = best.halos_threads == 128 ? 256 : 128;
+    t.halos_grid = t.halos_threads == 256 ? std::max(1, best.halos_grid / 2)
+                                          : std::min(16, best.halos_grid * 2);
+    st = trial(t, &t.ms);
+    if (!st && t.ms < best.ms) best = t;
+  }
   if (!st) st = descend(kHalos, 5, &p2m_tuning::halos_grid);
   if (!st) st = descend(kFull, 4, &p2m_tuning::full_grid);
   if (!st) st = descend(kChunk, 5, &p2m_tuning::full_chunk);

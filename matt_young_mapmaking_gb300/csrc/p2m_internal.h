@@ -122,6 +122,7 @@ struct PaintParams {
   int full_grid;         /* blocks per SM of k_paint_full */
   int full_chunk;        /* candidates per warp chunk of k_paint_full */
   int halo_batch;        /* halos per warp batch of k_paint_halos (1..32) */
+  int halos_threads;     /* threads per block of k_paint_halos (128 or 256) */
   unsigned int *err_flag; /* the device error word (DevCounters::err) */
 };
 

@@ -184,6 +184,14 @@ __device__ __forceinline__ ffloat ff_sqrt(ffloat x) {
   return ff_norm(y, __fdiv_rn(r, __fmul_rn(2.0f, y)));
 }
 
+/* the same with the correction's quotient from the approximate division (its 2-ulp error
+   is ~2^-46 of the root): the painting kernels' per-candidate form */
+__device__ __forceinline__ ffloat ff_sqrt_fast(ffloat x) {
+  const float y = __fsqrt_rn(x.h);
+  const float r = __fadd_rn(__fmaf_rn(-y, y, x.h), x.l);
+  return ff_norm(y, __fdividef(r, __fmul_rn(2.0f, y)));
+}
+
 __device__ __forceinline__ ffloat ff_mul_f(ffloat x, float y) {
   const float p = __fmul_rn(x.h, y);
   return ff_norm(p, __fmaf_rn(x.l, y, __fmaf_rn(x.h, y, -p)));
@@ -1186,7 +1194,7 @@ __device__ __forceinline__ int fast_decide(const PaintParams &P, const RingItem 
   if (c2 >= H.C_out) return 0;
   if (c2 > H.C_in) return 2;
   zero_val = false;
-  const ffloat uf = ff_sqrt(c2f);
+  const ffloat uf = ff_sqrt_fast(c2f);
   const float u = 0.5f * uf.h;
   if (u > 0.25f) return 2; /* discs wider than ~29 degrees: the exact path */
   /* angle = 2 asin(chord / 2) = chord + 2 (asin(u) - u), u = chord / 2 */
@@ -1398,16 +1406,15 @@ __global__ void __launch_bounds__(256) k_paint_full(PaintParams P, SweepBuffers 
 #define P2M_PEND_DEPTH 1 /* rounds of candidates whose atomics are in flight before their
                             TwoSum is finished (compensated path) */
 #endif
-#ifndef P2M_HALOS_THREADS
-/* threads per block of k_paint_halos (a multiple of 32).  128-thread blocks, 8 of them
-   per SM at 64 registers, keep 32 warps resident: measured 6 % faster painting than 24
-   warps of 256-thread blocks at 80 registers, although the 64-register build spills a
-   few words */
-#define P2M_HALOS_THREADS 128
-#endif
-#ifndef P2M_HALOS_MINBLOCKS
-#define P2M_HALOS_MINBLOCKS 8 /* resident blocks per SM the register budget must allow */
-#endif
+/* Threads per block of k_paint_halos: 128 or 256 (p2m_tuning.halos_threads, default
+   128).  The register budget allows 32 resident warps either way (8 blocks of 128 or 4
+   of 256 threads, at 64 registers): 128-thread blocks measured 6 % faster painting than
+   24 warps of 256-thread blocks at 80 registers, although the 64-register build spills
+   a few words. */
+template <int THREADS>
+struct HalosBlocks {
+  static constexpr int min_blocks = 1024 / THREADS; /* 32 warps (1024 threads) per SM */
+};
 
 /* per-warp shared-memory stage of the fused painter: the disc geometry and
    interpolation fields of the warp's batch of halos, and the 32 (halo, ring) items of the
@@ -1431,10 +1438,10 @@ struct WarpStage {
    the warp prefix-sums the spans and paints their candidates 32 at a time, each lane
    finding its item with a 32-wide search.  Nothing goes to global memory between the
    stages. */
-template <int EXACT, int ACC>
-__global__ void __launch_bounds__(P2M_HALOS_THREADS, P2M_HALOS_MINBLOCKS)
+template <int EXACT, int ACC, int THREADS>
+__global__ void __launch_bounds__(THREADS, HalosBlocks<THREADS>::min_blocks)
     k_paint_halos(PaintParams P, SweepBuffers W) {
-  __shared__ WarpStage s_stage[P2M_HALOS_THREADS / 32];
+  __shared__ WarpStage s_stage[THREADS / 32];
   const int lane = threadIdx.x & 31;
   WarpStage &S = s_stage[threadIdx.x >> 5];
   const long long nh = W.n_halos;
@@ -2067,15 +2074,21 @@ void p2m_launch_paint_full(const PaintParams &P, const SweepBuffers &W, cudaStre
   else if (P.precision == 3) k_paint_full<0, 3><<<g, 256, 0, s>>>(P, W);
   else k_paint_full<0, 0><<<g, 256, 0, s>>>(P, W);
 }
+template <int EXACT, int ACC, int THREADS>
+static void launch_paint_halos_t(const PaintParams &P, const SweepBuffers &W, cudaStream_t s,
+                                 int nsm) {
+  /* the shared-memory stage (19 KB per 128 threads) must not be what limits residency,
+     nor take the L1 the table loads use */
+  static std::atomic<unsigned long long> co{0};
+  carveout_once(k_paint_halos<EXACT, ACC, THREADS>, P2M_HALOS_CARVEOUT, co);
+  /* warps claim batches of halo_batch halos until none is left */
+  k_paint_halos<EXACT, ACC, THREADS><<<nsm * P.halos_grid, THREADS, 0, s>>>(P, W);
+}
 template <int EXACT, int ACC>
 static void launch_paint_halos(const PaintParams &P, const SweepBuffers &W, cudaStream_t s,
                                int nsm) {
-  /* the shared-memory stage (17 KB per block) must not be what limits residency, nor
-     take the L1 the table loads use */
-  static std::atomic<unsigned long long> co{0};
-  carveout_once(k_paint_halos<EXACT, ACC>, P2M_HALOS_CARVEOUT, co);
-  /* warps claim batches of halo_batch halos until none is left */
-  k_paint_halos<EXACT, ACC><<<nsm * P.halos_grid, P2M_HALOS_THREADS, 0, s>>>(P, W);
+  if (P.halos_threads == 256) launch_paint_halos_t<EXACT, ACC, 256>(P, W, s, nsm);
+  else launch_paint_halos_t<EXACT, ACC, 128>(P, W, s, nsm);
 }
 void p2m_launch_paint_halos(const PaintParams &P, const SweepBuffers &W, cudaStream_t s, int nsm) {
   if (P.precision == 0) launch_paint_halos<1, 0>(P, W, s, nsm);

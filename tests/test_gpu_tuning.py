@@ -41,7 +41,9 @@ def check(pt, rec, ref):
                                        full_chunk=65536),
                                   dict(sort_halos=0, halo_batch=32),
                                   dict(sort_halos=1, halo_batch=8),
-                                  dict(sort_halos=1, halo_batch=1, big_rings=32)])
+                                  dict(sort_halos=1, halo_batch=1, big_rings=32),
+                                  dict(halos_threads=256, halos_grid=4),
+                                  dict(halos_threads=256, halos_grid=1, halo_batch=32)])
 def test_tuning_extremes_keep_parity(precision, tune):
     rec = catalogue()
     ref = run_oracle(rec, [catalogs.table(nu=0.0)], 512, maps=MAPS, zmax=6.0)
@@ -63,6 +65,7 @@ def test_autotune_choice_and_parity():
         assert t["halos_grid"] in (2, 4, 6, 8, 16) and t["full_grid"] in (2, 4, 8, 16)
         assert t["full_chunk"] in (256, 512, 1024, 2048, 4096) and t["ms"] > 0
         assert t["sort_halos"] in (0, 1) and t["halo_batch"] in (8, 16, 32)
+        assert t["halos_threads"] in (128, 256)
         assert pt.tuning()["big_rings"] == t["big_rings"]
         assert not np.any(pt.healpix(0))  # the autotuner leaves the maps reset
         check(pt, rec, ref)
@@ -71,6 +74,6 @@ def test_autotune_choice_and_parity():
 def test_tuning_rejects_out_of_range():
     with painter("mixed") as pt:
         for bad in (dict(big_rings=-1), dict(halos_grid=0), dict(full_grid=33),
-                    dict(full_chunk=16)):
+                    dict(full_chunk=16), dict(halos_threads=192), dict(halos_threads=512)):
             with pytest.raises(p2m.P2MError):
                 pt.set_tuning(**bad)
