@@ -40,6 +40,7 @@ struct p2m_ctx {
   unsigned int *d_fits[2] = {nullptr, nullptr}, *h_fits[2] = {nullptr, nullptr};
   cudaEvent_t ev_fits[2] = {nullptr, nullptr};
   float4 *d_ringtab = nullptr;
+  float2 *d_ringhd = nullptr;
   float4 *d_phitab = nullptr;
   /* scramble / centre of the catalogue (pks2map.f90:162-262) */
   p2m_pre pre = {};
@@ -236,6 +237,7 @@ PaintParams make_params(const p2m_ctx *ctx, int nfloat) {
   P.rofz = ctx->d_rofz;
   P.zofr = ctx->d_zofr;
   P.ringtab = ctx->d_ringtab;
+  P.ringhd = ctx->d_ringhd;
   P.phitab = ctx->d_phitab;
   P.pre = ctx->pre;
   P.pre_ord = ctx->d_pre_ord;
@@ -758,6 +760,19 @@ p2m_status p2m_create(const p2m_config *cfg, p2m_ctx **out) {
     }
     CK(cudaMalloc((void **)&ctx->d_ringtab, sizeof(float4) * (size_t)nr));
     CK(cudaMemcpy(ctx->d_ringtab, rt.data(), sizeof(float4) * (size_t)nr, cudaMemcpyHostToDevice));
+    /* pi / npr of each ring as a (hi, lo) float pair: the candidates' longitude step */
+    std::vector<float2> hd((size_t)nr);
+    hd[0] = make_float2(0.0f, 0.0f);
+    for (int r = 1; r < nr; r++) {
+      int npr, ks;
+      long long npn;
+      p2m_ring_info(cfg->nside, r, &npr, &ks, &npn);
+      const double v = P2M_HP_PI / (double)npr;
+      const float vh = (float)v;
+      hd[(size_t)r] = make_float2(vh, (float)(v - (double)vh));
+    }
+    CK(cudaMalloc((void **)&ctx->d_ringhd, sizeof(float2) * (size_t)nr));
+    CK(cudaMemcpy(ctx->d_ringhd, hd.data(), sizeof(float2) * (size_t)nr, cudaMemcpyHostToDevice));
     /* cos and sin of the grid angles 2 pi k / M as (hi, lo) float pairs */
     std::vector<float4> pt(P2M_PHITAB);
     for (int k = 0; k < P2M_PHITAB; k++) {
@@ -823,7 +838,7 @@ void p2m_destroy(p2m_ctx *ctx) {
   cudaSetDevice(ctx->cfg.device);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   if (ctx->zstream) cudaStreamSynchronize(ctx->zstream);
-  void *ptrs[] = {ctx->d_rofz, ctx->d_zofr, ctx->d_ringtab, ctx->d_phitab, ctx->d_acc64, ctx->d_fs_acc,
+  void *ptrs[] = {ctx->d_rofz, ctx->d_zofr, ctx->d_ringtab, ctx->d_ringhd, ctx->d_phitab, ctx->d_acc64, ctx->d_fs_acc,
                   ctx->d_fs_out, ctx->d_halos, ctx->d_items_raw,
                   ctx->d_nring, ctx->d_ioff, ctx->d_fs_items, ctx->d_scan_tmp, ctx->d_counts,
                   ctx->d_pix_off, ctx->d_nitems, ctx->d_sums, ctx->d_set_rec, ctx->d_set_pix,

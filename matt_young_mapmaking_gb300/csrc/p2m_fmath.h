@@ -164,6 +164,16 @@ P2M_HD float p2m_logf(float x) {
   return FADD(FMUL(fe, P2M_LN2_HI), FADD(lm, FMUL(fe, P2M_LN2_LO)));
 }
 
+/* p2m_logf for a positive, normal, finite x, without the special-value tests (which
+   such an x never takes): the same result bit for bit */
+P2M_HD float p2m_logf_normal(float x) {
+  int e;
+  float m = p2m_frexp_centered(x, &e);
+  float lm = p2m_log_core(m);
+  float fe = (float)e;
+  return FADD(FMUL(fe, P2M_LN2_HI), FADD(lm, FMUL(fe, P2M_LN2_LO)));
+}
+
 /* ---- exp -------------------------------------------------------------------------- */
 /* exp(r) for |r| <= ~0.36 */
 P2M_HD float p2m_exp_core(float r) {
@@ -367,5 +377,8 @@ P2M_HD float p2m_tanf(float x) {
   float s = p2m_sin_core(r), c = p2m_cos_core(r);
   return (q & 1) ? -FDIV(c, s) : FDIV(s, c);
 }
+/* p2m_tanf for 0 <= x < pi/4: there the reduction is an identity (k = 0, r = x) and the
+   argument tests never fire, so this is the same result bit for bit */
+P2M_HD float p2m_tanf_pio4(float x) { return FDIV(p2m_sin_core(x), p2m_cos_core(x)); }
 
 #endif /* P2M_FMATH_H */

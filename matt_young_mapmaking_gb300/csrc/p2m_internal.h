@@ -114,6 +114,7 @@ struct PaintParams {
   const float *tables[P2M_MAXTABLES];
   const float *rofz, *zofr;
   const float4 *ringtab; /* (z hi, z lo, sin theta hi, sin theta lo) of ring i at index i */
+  const float2 *ringhd;  /* pi / npr of ring i as (hi, lo) */
   const float4 *phitab;  /* (cos hi, cos lo, sin hi, sin lo) of 2 pi k / P2M_PHITAB */
   p2m_pre pre;           /* scramble / centre of the catalogue (pks2map.f90:162-262) */
   const long long *pre_ord; /* with pre: radial-cut survivors before each record */

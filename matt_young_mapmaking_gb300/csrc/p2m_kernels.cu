@@ -676,8 +676,9 @@ __device__ __forceinline__ RingItem make_item(const PaintParams &P, const DiscGe
   /* f0 = ((sh - rf) - d) - ql as a float-float: sh - rf and d are exact */
   const ffloat f0f = ff_add_f(ff_two_sum(sh - rf, -d), -ql);
   const int n0 = lo - (int)a + (int)rf;
-  /* pi / npr as a float-float (pi = 3.14159274f - 8.74227766e-8f to 2^-48) */
-  const ffloat hd = ff_div({3.14159274e+00f, -8.74227766e-08f}, {fn, 0.0f});
+  /* pi / npr as a float-float, from the ring table */
+  const float2 hdv = P.ringhd[ring];
+  const ffloat hd = {hdv.x, hdv.y};
   it.halo = h;
   it.ring_n0 = (ring << 16) | (n0 & 0xffff);
   it.lo = lo;
@@ -1200,7 +1201,7 @@ __device__ __forceinline__ int fast_decide(const PaintParams &P, const RingItem 
   /* angle = 2 asin(chord / 2) = chord + 2 (asin(u) - u), u = chord / 2 */
   const ffloat ang = ff_add_f(uf, 2.0f * asin_minus_arg(u));
   const float angle = ang.h; /* hi = the float nearest hi + lo */
-  const float r = FMUL(H.chi_t, p2m_tanf(angle));
+  const float r = FMUL(H.chi_t, p2m_tanf_pio4(angle)); /* angle <= 2 asin(1/4) < pi/4 */
   const float dr = 1e-5f;
   if (r > P.th.rmaxt * (1.0f + dr)) {
     zero_val = true;
@@ -1217,7 +1218,7 @@ __device__ __forceinline__ int fast_decide(const PaintParams &P, const RingItem 
   /* the reference's log (the same float function as the exact path and the oracle):
      fr is a difference of logs that cancels to ~drt, so a cruder log's error of a few
      ulp of log r would move the value by ~1e-7 relative, and coherently over a disc */
-  const float lr = p2m_logf(r);
+  const float lr = p2m_logf_normal(r); /* rmint < r < rmaxt here */
   const float uu = (lr - P.th.lrmin) * P.inv_drt;
   const int iu = (int)uu;
   const float fu = uu - (float)iu;
@@ -1935,6 +1936,8 @@ __global__ void k_fmath_eval(int fn, const float *x, const float *y, float *out,
     case 5: r = p2m_sinf(a); break;
     case 6: r = p2m_cosf(a); break;
     case 8: r = fixed_to_float(float_to_fixed(a) + float_to_fixed(b)); break;
+    case 9: r = p2m_tanf_pio4(a); break;
+    case 10: r = p2m_logf_normal(a); break;
     default: r = p2m_tanf(a); break;
   }
   out[i] = r;

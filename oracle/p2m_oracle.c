@@ -1142,6 +1142,8 @@ void orc_fmath_eval(int fn, const float *x, const float *y, float *out, int64_t 
       case 4: r = p2m_atanf(a); break;
       case 5: r = p2m_sinf(a); break;
       case 6: r = p2m_cosf(a); break;
+      case 9: r = p2m_tanf_pio4(a); break;
+      case 10: r = p2m_logf_normal(a); break;
       default: r = p2m_tanf(a); break;
     }
     out[i] = r;

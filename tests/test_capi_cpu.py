@@ -129,3 +129,15 @@ def test_pow_accuracy_and_special_cases():
         assert (np.abs(got - ref) / ulp).max() <= 8.0
     one = oracle.fmath(2, np.array([3.7, 0.5], np.float32), np.array([1.0, 0.0], np.float32))
     assert one[0] == np.float32(3.7) and one[1] == 1.0
+
+
+def test_restricted_float_functions_equal_the_general_ones():
+    """The painting path's tan for 0 <= x < pi/4 and log for positive normal x give the
+    general functions' results bit for bit over their ranges (fn 9 / 7, fn 10 / 0)."""
+    rng = np.random.default_rng(3)
+    x = np.concatenate([rng.uniform(0.0, 0.78539, 200_000),
+                        np.float32(0.78539816) * rng.random(1000) ** 8]).astype(np.float32)
+    assert np.array_equal(oracle.fmath(9, x).view(np.uint32), oracle.fmath(7, x).view(np.uint32))
+    y = np.exp(rng.uniform(-80.0, 80.0, 200_000)).astype(np.float32)
+    y = np.concatenate([y, np.array([1.1754944e-38, 1.0, 3.4e38], np.float32)])
+    assert np.array_equal(oracle.fmath(10, y).view(np.uint32), oracle.fmath(0, y).view(np.uint32))

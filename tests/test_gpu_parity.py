@@ -500,7 +500,8 @@ def test_fmath_bit_identical_host_device():
              2: (np.exp(rng.uniform(-8, 8, n)), rng.uniform(-6, 6, n)),
              3: (rng.uniform(-1, 1, n), None), 4: (rng.uniform(-20, 20, n), None),
              5: (rng.uniform(-12, 12, n), None), 6: (rng.uniform(-12, 12, n), None),
-             7: (rng.uniform(0, 3.1, n), None)}
+             7: (rng.uniform(0, 3.1, n), None), 9: (rng.uniform(0, 0.785, n), None),
+             10: (np.exp(rng.uniform(-80, 80, n)), None)}
     lib = p2m.load_library()
     for fn, (x, y) in cases.items():
         x = x.astype(np.float32)
