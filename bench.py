@@ -39,9 +39,9 @@ MAPS = ((0, 1), (0, 2))
 LAUNCHES_PER_STEP = 15
 # DRAM bytes (read + write) per pixel update of k_paint_halos from an ncu capture of the
 # same kernel on 1e7 halos at Nside 2048 (dram__bytes_read.sum + dram__bytes_write.sum)
-PAINT_DRAM_BYTES_PER_UPDATE = 78.0
+PAINT_DRAM_BYTES_PER_UPDATE = 77.7
 # L2 atomic throughput of this GB300 (sectors/s): ncu lts__t_sectors_srcunit_tex_op_atom
-# of the same capture, 27.3 sectors/ns at 7.20 % of peak sustained
+# of the same capture, 26.7 sectors/ns at 7.06 % of peak sustained
 L2_ATOMIC_SECTORS_PER_S = 3.79e11
 METRIC = "halos/sec & pixel-updates/sec at Nside=4096, 1 GB300; rel err vs FP64 oracle"
 
