@@ -549,14 +549,16 @@ def test_fixed_point_conversions_are_exact():
 @pytest.mark.parametrize("model,nu,alpha", [(1, 148.0, 0.0), (1, 0.0, 0.0), (2, 545.0, 0.0),
                                              (3, 218.0, 0.0), (1, 353.0, 1.0)])
 def test_maptable_gpu_matches_oracle(model, nu, alpha):
+    """The GPU table maker gives the oracle's table image bit for bit (the same float
+    sequence and float functions on both sides; the FP64 virial-radius power rounds to
+    the same float)."""
     gpu = p2m.make_maptable(model, nu, alpha, nchit=12, nmht=10, nrt=30)
     ref = oracle.make_maptable(model, nu, alpha, nchit=12, nmht=10, nrt=30)
     assert gpu[:36] == ref[:36]
-    g = p2m.table_array(gpu).astype(np.float64)
-    r = p2m.table_array(ref).astype(np.float64)
-    scale = np.abs(r).max(axis=2, keepdims=True) + 1e-300
-    assert (np.abs(g - r) / scale).max() <= 1e-6
-    assert np.mean(g == r) > 0.99
+    g = p2m.table_array(gpu)
+    r = p2m.table_array(ref)
+    same = (g.view(np.uint32) == r.view(np.uint32)) | (np.isnan(g) & np.isnan(r))
+    assert same.all(), "%d of %d entries differ" % ((~same).sum(), same.size)
 
 
 @pytest.mark.parametrize("big_rings", [None, "0"])
