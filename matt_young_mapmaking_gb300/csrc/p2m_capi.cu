@@ -51,6 +51,12 @@ struct p2m_ctx {
   p2m_tabhdr th;
   bool th_set = false;
   float *d_tab[P2M_MAXTABLES] = {};
+  /* pair tables (PaintParams::pair_tab), set up by the first ingest after a table load:
+     a gathered copy where a pair of maps is not profiles 1 and 2 of one table */
+  float2 *d_pair[P2M_MAXMAPS / 2] = {};
+  long long cap_pair[P2M_MAXMAPS / 2] = {};
+  const float2 *pair_tab[P2M_MAXMAPS / 2] = {};
+  bool pairs_ok = false;
   float band_u = 2e-4f;
   p2m_tuning tune = {P2M_BIG_RINGS, 8, 8, 1024, (int32_t)P2M_STREAM_CHUNK, 1, 16, 1, 128, 0.0f};
   /* painting order (p2m_tuning.sort_halos): counting sort by first ring */
@@ -229,11 +235,10 @@ PaintParams make_params(const p2m_ctx *ctx, int nfloat) {
     P.map_profile[m] = m < c.nmaps ? c.map_profile[m] : 1;
     if (m < c.nmaps && c.map_profile[m] == 2) P.any_ksz = 1;
   }
-  P.paired = c.nmaps == 2 && c.map_table[0] == c.map_table[1] && c.map_profile[0] == 1 &&
-             c.map_profile[1] == 2;
   P.mass_fac = FMUL(FMUL(4.0f / 3.0f, mypi), ctx->cosmo.rho_0);
   P.th = ctx->th;
   for (int t = 0; t < P2M_MAXTABLES; t++) P.tables[t] = ctx->d_tab[t];
+  for (int q = 0; q < P2M_MAXMAPS / 2; q++) P.pair_tab[q] = ctx->pair_tab[q];
   P.rofz = ctx->d_rofz;
   P.zofr = ctx->d_zofr;
   P.ringtab = ctx->d_ringtab;
@@ -286,11 +291,37 @@ IngestBuffers ingest_buffers(const p2m_ctx *ctx, const float *records) {
   return B;
 }
 
+/* checks that every map's table is loaded, and sets up the pair tables after a table
+   load: maps 2q and 2q + 1 read their values from one table of float2 entries, the
+   interleaved table itself when the pair is its profiles 1 and 2 (or a lone last map
+   is its profile 1), else a copy gathered on the context's stream */
 p2m_status check_tables(p2m_ctx *ctx) {
-  for (int m = 0; m < ctx->cfg.nmaps; m++)
-    if (!ctx->d_tab[ctx->cfg.map_table[m]])
-      return fail(ctx, P2M_ERR_STATE, "table slot " + std::to_string(ctx->cfg.map_table[m]) +
+  const p2m_config &c = ctx->cfg;
+  for (int m = 0; m < c.nmaps; m++)
+    if (!ctx->d_tab[c.map_table[m]])
+      return fail(ctx, P2M_ERR_STATE, "table slot " + std::to_string(c.map_table[m]) +
                                           " used by map " + std::to_string(m) + " is not loaded");
+  if (ctx->pairs_ok) return P2M_OK;
+  const long long nent = ctx->th.nelem / 2;
+  for (int q = 0; q < P2M_MAXMAPS / 2; q++) {
+    ctx->pair_tab[q] = nullptr;
+    const int a = 2 * q, b = 2 * q + 1;
+    if (a >= c.nmaps) continue;
+    const int ta = c.map_table[a], pa = c.map_profile[a];
+    const bool two = b < c.nmaps;
+    const int tb = two ? c.map_table[b] : ta;
+    const int pb = two ? c.map_profile[b] : (pa == 1 ? 2 : pa);
+    if (ta == tb && pa == 1 && pb == 2) {
+      ctx->pair_tab[q] = (const float2 *)ctx->d_tab[ta];
+      continue;
+    }
+    CK(grow(&ctx->d_pair[q], &ctx->cap_pair[q], nent));
+    p2m_launch_pair_table(ctx->d_pair[q], ctx->d_tab[ta], pa, ctx->d_tab[tb], pb, nent,
+                          ctx->stream, ctx->nsm);
+    CK(cudaGetLastError());
+    ctx->pair_tab[q] = ctx->d_pair[q];
+  }
+  ctx->pairs_ok = true;
   return P2M_OK;
 }
 
@@ -853,6 +884,8 @@ void p2m_destroy(p2m_ctx *ctx) {
     if (ctx->d_out_own[m]) cudaFree(ctx->d_out_own[m]);
   for (int t = 0; t < P2M_MAXTABLES; t++)
     if (ctx->d_tab[t]) cudaFree(ctx->d_tab[t]);
+  for (int q = 0; q < P2M_MAXMAPS / 2; q++)
+    if (ctx->d_pair[q]) cudaFree(ctx->d_pair[q]);
   if (ctx->h_ctr) cudaFreeHost(ctx->h_ctr);
   for (int b = 0; b < 2; b++) {
     if (ctx->h_fits[b]) cudaFreeHost(ctx->h_fits[b]);
@@ -958,6 +991,7 @@ p2m_status p2m_load_table(p2m_ctx *ctx, int32_t slot, const void *image, int64_t
   CK(cudaMemcpy(ctx->d_tab[slot], b + 36, sizeof(float) * (size_t)t.nelem, cudaMemcpyHostToDevice));
   ctx->th = t;
   ctx->th_set = true;
+  ctx->pairs_ok = false; /* the pair tables follow the tables */
   return P2M_OK;
 }
 

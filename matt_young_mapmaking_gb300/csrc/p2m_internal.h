@@ -102,7 +102,6 @@ struct PaintParams {
   float fov, dpix, hf, cut_low, cut_high, chihview, bbps_delta;
   int map_table[P2M_MAXMAPS], map_profile[P2M_MAXMAPS];
   int any_ksz;
-  int paired;   /* two maps: profiles 1 and 2 of one table */
   float mass_fac; /* (4./3.*mypi)*rho_0 of pks2map.f90:264 */
   p2m_cosmo cosmo;
   p2m_tabhdr th;
@@ -112,6 +111,10 @@ struct PaintParams {
   float inv_drt; /* 1 / drt of the table */
   int big_rings; /* halos spanning more rings are painted from stored items */
   const float *tables[P2M_MAXTABLES];
+  /* maps 2q and 2q + 1 as one table of float2 entries (.x map 2q, .y map 2q + 1) at the
+     tables' float2 index cb / 2 + ir - 1: the table itself where the pair is profiles 1
+     and 2 of one table (or a lone last map of profile 1), else a gathered copy */
+  const float2 *pair_tab[P2M_MAXMAPS / 2];
   const float *rofz, *zofr;
   const float4 *ringtab; /* (z hi, z lo, sin theta hi, sin theta lo) of ring i at index i */
   const float2 *ringhd;  /* pi / npr of ring i as (hi, lo) */
@@ -183,6 +186,8 @@ void p2m_launch_items(const PaintParams &P, const IngestBuffers &B, long long n_
                       cudaStream_t s, int nsm);
 void p2m_launch_fs(const PaintParams &P, const IngestBuffers &B, long long n_max, cudaStream_t s,
                    int nsm);
+void p2m_launch_pair_table(float2 *dst, const float *ta, int pa, const float *tb, int pb,
+                           long long nent, cudaStream_t s, int nsm);
 void p2m_launch_item_counts(const RingItem *items, long long n, unsigned int *counts,
                             cudaStream_t s, int nsm);
 void p2m_launch_paint_halos(const PaintParams &P, const SweepBuffers &W, cudaStream_t s, int nsm);

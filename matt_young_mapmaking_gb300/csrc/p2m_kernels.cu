@@ -850,6 +850,28 @@ __device__ __forceinline__ float fixed_to_float(long long q) {
    sparse (nonzero only where an add rounded) and their tiles flagged; ACC 3: 64-bit
    fixed-point accumulator (value * 2^56 rounded to an integer, fire-and-forget).  All
    maps' adds are issued before any result is used. */
+/* the compensated deposit's second half: the exact rounding error of each map's add
+   (TwoSum of its returned old value and the value) goes to that map's low word, and the
+   pixel's tile is flagged when any error is nonzero */
+__device__ __forceinline__ void compensate_lo(const PaintParams &P, const SweepBuffers *W,
+                                              long long slot, const float *vals,
+                                              const float *olds) {
+  bool any = false;
+#pragma unroll
+  for (int m = 0; m < P2M_MAXMAPS; m++) {
+    if (m >= P.nmaps || vals[m] == 0.0f) continue;
+    float old = olds[m], v = vals[m];
+    float sm = __fadd_rn(old, v);
+    float bb = __fsub_rn(sm, old);
+    float err = __fadd_rn(__fsub_rn(old, __fsub_rn(sm, bb)), __fsub_rn(v, bb));
+    if (err != 0.0f) {
+      atomicAdd(W->lo + (long long)m * W->npix + slot, err);
+      any = true;
+    }
+  }
+  if (any) W->tiles[slot >> P2M_TILE_SHIFT] = 1;
+}
+
 template <int ACC>
 __device__ __forceinline__ void accumulate_vals(const PaintParams &P, void *acc, long long slot,
                                                 const float *vals, const SweepBuffers *W) {
@@ -863,20 +885,7 @@ __device__ __forceinline__ void accumulate_vals(const PaintParams &P, void *acc,
 #pragma unroll
     for (int m = 0; m < P2M_MAXMAPS; m++)
       olds[m] = (m < P.nmaps && vals[m] != 0.0f) ? atomicAdd(W->out[m] + slot, vals[m]) : 0.0f;
-    bool any = false;
-#pragma unroll
-    for (int m = 0; m < P2M_MAXMAPS; m++) {
-      if (m >= P.nmaps || vals[m] == 0.0f) continue;
-      float old = olds[m], v = vals[m];
-      float sm = __fadd_rn(old, v);
-      float bb = __fsub_rn(sm, old);
-      float err = __fadd_rn(__fsub_rn(old, __fsub_rn(sm, bb)), __fsub_rn(v, bb));
-      if (err != 0.0f) {
-        atomicAdd(W->lo + (long long)m * W->npix + slot, err);
-        any = true;
-      }
-    }
-    if (any) W->tiles[slot >> P2M_TILE_SHIFT] = 1;
+    compensate_lo(P, W, slot, vals, olds);
   } else if (ACC == 3) {
     /* 64-bit fixed point: integer adds are associative, so the sums do not depend on the
        order in which the atomics land */
@@ -906,62 +915,9 @@ __device__ __forceinline__ void accumulate_vals(const PaintParams &P, void *acc,
   }
 }
 
-/* profile values of every map at one pixel (maptable.f90:204-212 with known ir, fr: the
-   reference's float sequence), deposited at slot `slot` */
-template <int ACC>
-__device__ __forceinline__ void deposit_maps(const PaintParams &P, const HotHalo &H, void *acc,
-                                             long long slot, int ir, float fr,
-                                             const SweepBuffers *W = nullptr) {
-  float ofr = FSUB(1.0f, fr), ofc = FSUB(1.0f, H.fc), ofm = FSUB(1.0f, H.fm);
-  float fc = H.fc, fm = H.fm;
-  bool fast = H.cb[0] >= 0 && H.cb[1] >= 0 && H.cb[2] >= 0 && H.cb[3] >= 0 &&
-              ir >= 1 && ir < P.th.nrt;
-  float vals[P2M_MAXMAPS];
-#pragma unroll
-  for (int m = 0; m < P2M_MAXMAPS; m++) {
-    vals[m] = 0.0f;
-    if (m >= P.nmaps) continue;
-    int prof = P.map_profile[m];
-    float w = prof == 2 ? H.w2 : H.w1;
-    if (w == 0.0f) continue;
-    const float *tab = P.tables[P.map_table[m]];
-    float v;
-    if (fast) {
-      int rofs = 2 * (ir - 1) + (prof - 1);
-      float t00a = __ldg(tab + H.cb[0] + rofs), t00b = __ldg(tab + H.cb[0] + rofs + 2);
-      float t10a = __ldg(tab + H.cb[1] + rofs), t10b = __ldg(tab + H.cb[1] + rofs + 2);
-      float t01a = __ldg(tab + H.cb[2] + rofs), t01b = __ldg(tab + H.cb[2] + rofs + 2);
-      float t11a = __ldg(tab + H.cb[3] + rofs), t11b = __ldg(tab + H.cb[3] + rofs + 2);
-      v = 0.0f;
-      v = FADD(v, FMUL(FMUL(FMUL(t00a, ofr), ofc), ofm));
-      v = FADD(v, FMUL(FMUL(FMUL(t00b, fr), ofc), ofm));
-      v = FADD(v, FMUL(FMUL(FMUL(t10a, ofr), fc), ofm));
-      v = FADD(v, FMUL(FMUL(FMUL(t10b, fr), fc), ofm));
-      v = FADD(v, FMUL(FMUL(FMUL(t01a, ofr), ofc), fm));
-      v = FADD(v, FMUL(FMUL(FMUL(t01b, fr), ofc), fm));
-      v = FADD(v, FMUL(FMUL(FMUL(t11a, ofr), fc), fm));
-      v = FADD(v, FMUL(FMUL(FMUL(t11b, fr), fc), fm));
-    } else {
-      p2m_hinterp hi;
-      hi.chi_t = H.chi_t;
-      hi.fc = H.fc;
-      hi.fm = H.fm;
-      hi.ichi = H.ichi;
-      hi.imh = H.imh;
-      hi.zero = hot_zero(H);
-      v = p2m_blend8(tab, &P.th, &hi, prof, ir, fr);
-    }
-    vals[m] = FMUL(w, v);
-  }
-  accumulate_vals<ACC>(P, acc, slot, vals, W);
-}
-
-/* Mixed-precision deposit for the common pair of maps, profiles 1 and 2 of one table
-   (tSZ and kSZ): both profiles of a (corner, r-index) entry come from one 8-byte load.
-   The blend is the reference's float sequence (maptable.f90:204-212, every product and
-   sum rounded in source order), so that a pixel whose (ir, fr) equal the reference's
-   gets the reference's value bit for bit.  Other map sets and clamped corners use
-   deposit_maps. */
+/* The eight-term blend of maptable.f90:204-212 for known (ir, fr), in the reference's
+   float sequence: every product and sum rounded in source order, so that a pixel whose
+   (ir, fr) equal the reference's gets the reference's value bit for bit. */
 __device__ __forceinline__ float blend_pair_seq(float a0, float b0, float a1, float b1, float a2,
                                                 float b2, float a3, float b3, float fr,
                                                 float ofr, float fc, float ofc, float fm,
@@ -978,41 +934,77 @@ __device__ __forceinline__ float blend_pair_seq(float a0, float b0, float a1, fl
   return v;
 }
 
-__device__ __forceinline__ bool paired_values(const PaintParams &P, const HotHalo &H, int ir,
-                                              float fr, float &v1, float &v2) {
-  if (!P.paired || H.cb[0] < 0 || H.cb[1] < 0 || H.cb[2] < 0 || H.cb[3] < 0 || ir < 1 ||
-      ir >= P.th.nrt)
-    return false;
-  const float2 *tab = (const float2 *)P.tables[P.map_table[0]];
-  const int r = ir - 1; /* (cb + 2 (ir - 1)) / 2: the (profile 1, profile 2) pair at ir */
+/* the four corners' rows and the r-index pair (ir, ir + 1) lie inside the table */
+__device__ __forceinline__ bool fast_corners(const PaintParams &P, const HotHalo &H, int ir) {
+  return H.cb[0] >= 0 && H.cb[1] >= 0 && H.cb[2] >= 0 && H.cb[3] >= 0 && ir >= 1 &&
+         ir < P.th.nrt;
+}
+
+/* deposit weight of map m: 1 for tSZ (profile 1), -v_los / c for kSZ (profile 2) */
+__device__ __forceinline__ float map_weight(const PaintParams &P, const HotHalo &H, int m) {
+  return P.map_profile[m] == 2 ? H.w2 : H.w1;
+}
+
+/* Profile values of maps 2q and 2q + 1 at one pixel from pair table q, whose entry
+   cb / 2 + ir - 1 (corner row cb) holds map 2q's table value in .x and map 2q + 1's in .y:
+   both values of a (corner, r-index) entry come from one 8-byte load.  `two` false: map
+   2q only (vb = 0).  Needs fast_corners. */
+__device__ __forceinline__ void pair_values(const float2 *tab, const HotHalo &H, int ir,
+                                            float fr, float wa, float wb, bool two, float &va,
+                                            float &vb) {
+  const int r = ir - 1;
   const float2 a0 = __ldg(tab + (H.cb[0] >> 1) + r), b0 = __ldg(tab + (H.cb[0] >> 1) + r + 1);
   const float2 a1 = __ldg(tab + (H.cb[1] >> 1) + r), b1 = __ldg(tab + (H.cb[1] >> 1) + r + 1);
   const float2 a2 = __ldg(tab + (H.cb[2] >> 1) + r), b2 = __ldg(tab + (H.cb[2] >> 1) + r + 1);
   const float2 a3 = __ldg(tab + (H.cb[3] >> 1) + r), b3 = __ldg(tab + (H.cb[3] >> 1) + r + 1);
   const float fc = H.fc, fm = H.fm;
   const float ofr = FSUB(1.0f, fr), ofc = FSUB(1.0f, fc), ofm = FSUB(1.0f, fm);
-  v1 = FMUL(H.w1, blend_pair_seq(a0.x, b0.x, a1.x, b1.x, a2.x, b2.x, a3.x, b3.x, fr, ofr, fc,
-                                 ofc, fm, ofm));
-  v2 = FMUL(H.w2, blend_pair_seq(a0.y, b0.y, a1.y, b1.y, a2.y, b2.y, a3.y, b3.y, fr, ofr, fc,
-                                 ofc, fm, ofm));
-  return true;
+  va = FMUL(wa, blend_pair_seq(a0.x, b0.x, a1.x, b1.x, a2.x, b2.x, a3.x, b3.x, fr, ofr, fc,
+                               ofc, fm, ofm));
+  vb = two ? FMUL(wb, blend_pair_seq(a0.y, b0.y, a1.y, b1.y, a2.y, b2.y, a3.y, b3.y, fr, ofr,
+                                     fc, ofc, fm, ofm))
+           : 0.0f;
 }
 
+/* profile values of every map at one pixel (maptable.f90:204-212 with known ir, fr: the
+   reference's float sequence), deposited at slot `slot`: through the pair tables where
+   the corners lie inside the table, else (clamped corners, the last r-index) through the
+   reference's clamped offsets */
 template <int ACC>
-__device__ __forceinline__ void deposit_mixed(const PaintParams &P, const HotHalo &H,
-                                              long long slot, int ir, float fr,
-                                              const SweepBuffers *W) {
+__device__ __forceinline__ void deposit_maps(const PaintParams &P, const HotHalo &H, void *acc,
+                                             long long slot, int ir, float fr,
+                                             const SweepBuffers *W = nullptr) {
   float vals[P2M_MAXMAPS];
 #pragma unroll
   for (int m = 0; m < P2M_MAXMAPS; m++) vals[m] = 0.0f;
-  if (!paired_values(P, H, ir, fr, vals[0], vals[1])) {
-    deposit_maps<ACC>(P, H, W->acc, slot, ir, fr, W);
-    return;
+  if (fast_corners(P, H, ir)) {
+#pragma unroll
+    for (int q = 0; q < P2M_MAXMAPS / 2; q++) {
+      if (2 * q >= P.nmaps) continue;
+      const bool two = 2 * q + 1 < P.nmaps;
+      pair_values(P.pair_tab[q], H, ir, fr, map_weight(P, H, 2 * q),
+                  two ? map_weight(P, H, 2 * q + 1) : 0.0f, two, vals[2 * q], vals[2 * q + 1]);
+    }
+  } else {
+    p2m_hinterp hi;
+    hi.chi_t = H.chi_t;
+    hi.fc = H.fc;
+    hi.fm = H.fm;
+    hi.ichi = H.ichi;
+    hi.imh = H.imh;
+    hi.zero = hot_zero(H);
+#pragma unroll
+    for (int m = 0; m < P2M_MAXMAPS; m++) {
+      if (m >= P.nmaps) continue;
+      const int prof = P.map_profile[m];
+      vals[m] = FMUL(map_weight(P, H, m),
+                     p2m_blend8(P.tables[P.map_table[m]], &P.th, &hi, prof, ir, fr));
+    }
   }
-  accumulate_vals<ACC>(P, W->acc, slot, vals, W);
+  accumulate_vals<ACC>(P, acc, slot, vals, W);
 }
 
-/* A compensated deposit of the paired maps split in two: the atomic adds are issued at
+/* A compensated deposit of one or two maps split in two: the atomic adds are issued at
    once, the TwoSum of their returned old values is finished one candidate later, so the
    atomics' round trip overlaps the next candidate's decision and table reads. */
 struct PendingDeposit {
@@ -1277,21 +1269,19 @@ __device__ __forceinline__ void paint_pixel(const PaintParams &P, const SweepBuf
   if (zero_val || hot_zero(H)) return;
   /* the halo's cone selects its copy of the maps (always 0 outside ensembles) */
   const long long slot = pix + (long long)hot_cone(H) * P.cone_npix;
-  if (EXACT) {
-    deposit_maps<ACC>(P, H, W.acc, slot, ir, fr, &W);
-  } else if (ACC == 2 && pend) {
+  if (!EXACT && ACC == 2 && pend && P.nmaps <= 2 && fast_corners(P, H, ir)) {
+    /* one or two maps: the values from pair table 0, the adds issued now and their
+       TwoSum finished one round of candidates later */
     float v0, v1;
-    if (paired_values(P, H, ir, fr, v0, v1)) {
-      pend->slot = slot;
-      pend->v0 = v0;
-      pend->v1 = v1;
-      pend->o0 = v0 != 0.0f ? atomicAdd(W.out[0] + slot, v0) : 0.0f;
-      pend->o1 = v1 != 0.0f ? atomicAdd(W.out[1] + slot, v1) : 0.0f;
-    } else {
-      deposit_mixed<ACC>(P, H, slot, ir, fr, &W);
-    }
+    pair_values(P.pair_tab[0], H, ir, fr, map_weight(P, H, 0), map_weight(P, H, 1),
+                P.nmaps == 2, v0, v1);
+    pend->slot = slot;
+    pend->v0 = v0;
+    pend->v1 = v1;
+    pend->o0 = v0 != 0.0f ? atomicAdd(W.out[0] + slot, v0) : 0.0f;
+    pend->o1 = v1 != 0.0f ? atomicAdd(W.out[1] + slot, v1) : 0.0f;
   } else {
-    deposit_mixed<ACC>(P, H, slot, ir, fr, &W);
+    deposit_maps<ACC>(P, H, W.acc, slot, ir, fr, &W);
   }
 }
 
@@ -1568,6 +1558,25 @@ __global__ void __launch_bounds__(THREADS, HalosBlocks<THREADS>::min_blocks)
   warp_count(&W.ctr->hp_updates, nupd);
   warp_count(&W.ctr->n_recheck, nrc);
   warp_count(&W.ctr->n_cand, ncand);
+}
+
+/* pair table of two maps: entry e = (table a's profile pa value, table b's profile pb
+   value) at float2 index e of the (profile 1, profile 2) interleaved tables, for the
+   nent = nelem / 2 (ir, imh, ichi) entries */
+__global__ void __launch_bounds__(256) k_pair_table(float2 *__restrict__ dst,
+                                                    const float *__restrict__ ta, int pa,
+                                                    const float *__restrict__ tb, int pb,
+                                                    long long nent) {
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < nent;
+       e += (long long)gridDim.x * blockDim.x)
+    dst[e] = make_float2(ta[2 * e + (pa - 1)], tb[2 * e + (pb - 1)]);
+}
+
+void p2m_launch_pair_table(float2 *dst, const float *ta, int pa, const float *tb, int pb,
+                           long long nent, cudaStream_t s, int nsm) {
+  const long long need = (nent + 255) / 256;
+  const int grid = (int)std::max(1LL, std::min(need, (long long)nsm * 8));
+  k_pair_table<<<grid, 256, 0, s>>>(dst, ta, pa, tb, pb, nent);
 }
 
 /* candidate counts of items (input of the candidate-offset scan) */
