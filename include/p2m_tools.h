@@ -49,7 +49,8 @@ int32_t p2m_get_timings(struct p2m_ctx *ctx, double *ms, int32_t n);
    address is cached per device and is not valid across a cudaDeviceReset: do not call
    this function after the device has been reset in the same process.  Calls on one
    device share the scratch, so overlapping calls race and must be serialised by the
-   caller.  Synchronous.  nmaps > P2M_NOALLOC_MAXMAPS: P2M_ERR_CAPACITY. */
+   caller.  Synchronous: a stream under capture is refused with P2M_ERR_STATE, nothing
+   queued.  nmaps > P2M_NOALLOC_MAXMAPS: P2M_ERR_CAPACITY. */
 #define P2M_NOALLOC_MAXMAPS 8
 int32_t p2m_map_sums_noalloc(const float *const *d_maps, int32_t nmaps, int64_t npix,
                              double *sums, void *stream);

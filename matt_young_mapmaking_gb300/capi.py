@@ -18,6 +18,7 @@ LIB_PATH = os.path.join(_HERE, "libp2m_gb300.so")
 MAXMAPS = 8
 NOALLOC_MAXMAPS = 8  # P2M_NOALLOC_MAXMAPS of include/p2m_tools.h
 P2M_OK, P2M_ERR_BADARG, P2M_ERR_CUDA, P2M_ERR_CAPACITY = 0, 1, 2, 3
+P2M_ERR_IO, P2M_ERR_STATE, P2M_ERR_NOMEM = 5, 6, 7
 PREC_FP64, PREC_MIXED, PREC_MIXED_F64, PREC_FIXED = 0, 1, 2, 3
 FLAG_RECORD_SETS, FLAG_ALL_HALOS, FLAG_TIMING, FLAG_VALIDATE = 1, 2, 4, 8
 STATUS = {0: "OK", 1: "BADARG", 2: "CUDA", 3: "CAPACITY", 4: "TIMEOUT", 5: "IO", 6: "STATE",

@@ -20,7 +20,9 @@
  *  - the looked-up address belongs to the device's current context: after a
  *    cudaDeviceReset (by this process or a host framework) it is stale and later calls
  *    would write through a freed address, so the call must not be used across a reset;
- *  - the call is synchronous: it returns after the sums have reached the host;
+ *  - the call is synchronous: it returns after the sums have reached the host, which a
+ *    stream under capture cannot do, so a capturing stream is refused with
+ *    P2M_ERR_STATE before anything is queued;
  *  - more than P2M_NOALLOC_MAXMAPS maps is rejected with P2M_ERR_CAPACITY.
  */
 #include <cuda_runtime.h>
@@ -93,6 +95,9 @@ extern "C" p2m_status p2m_map_sums_noalloc(const float *const *d_maps, int32_t n
     if (!d_maps[m] && npix > 0) return P2M_ERR_BADARG;
     maps.p[m] = d_maps[m];
   }
+  cudaStreamCaptureStatus cap_st = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing((cudaStream_t)stream, &cap_st) != cudaSuccess) return P2M_ERR_CUDA;
+  if (cap_st != cudaStreamCaptureStatusNone) return P2M_ERR_STATE;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return P2M_ERR_CUDA;
   if (dev < 0 || dev >= P2M_NOALLOC_MAX_DEVICES) return P2M_ERR_CAPACITY;

@@ -80,3 +80,22 @@ def test_noalloc_rejects_bad_sizes():
     assert st == p2m.capi.P2M_ERR_BADARG
     st, empty = sums_noalloc(lib, [buf.data_ptr()], 0)
     assert st == 0 and empty[0] == 0.0
+
+
+def test_noalloc_refuses_a_capturing_stream():
+    """The call ends in a copy to host memory and a stream synchronisation, neither of
+    which a stream under capture allows: it returns P2M_ERR_STATE and queues nothing, so
+    the capture ends cleanly (an empty graph)."""
+    import torch
+    lib = p2m.load_library()
+    buf = torch.zeros(1024, dtype=torch.float32, device="cuda")
+    st, _ = sums_noalloc(lib, [buf.data_ptr()], 1024)  # the one-time set-up, uncaptured
+    assert st == 0
+    side = torch.cuda.Stream()
+    graph = torch.cuda.CUDAGraph()
+    results = []
+    with torch.cuda.graph(graph, stream=side):
+        results.append(sums_noalloc(lib, [buf.data_ptr()], 1024, stream=side.cuda_stream)[0])
+    assert results == [p2m.capi.P2M_ERR_STATE]
+    st, out = sums_noalloc(lib, [buf.data_ptr()], 1024)  # usable after the capture
+    assert st == 0 and out[0] == 0.0
