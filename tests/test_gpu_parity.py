@@ -273,6 +273,31 @@ def test_eight_maps_eight_tables(precision):
         assert_maps_close(fs[m], rfs[m], rel=1e-6, what="flat sky %d" % m)
 
 
+MAP_SETS = {
+    "lone_ksz": ((0, 2),),
+    "ksz_then_tsz": ((0, 2), (0, 1)),
+    "same_map_twice": ((0, 1), (0, 1)),
+    "three_maps": ((0, 1), (1, 2), (1, 1)),
+    "three_maps_lone_ksz": ((1, 2), (0, 1), (0, 2)),
+}
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed", "fixed"])
+@pytest.mark.parametrize("name", list(MAP_SETS))
+def test_map_sets_through_pair_tables(name, precision):
+    """Map sets whose pairs are not profiles 1 and 2 of one table read gathered pair
+    tables (a lone kSZ map, swapped profiles, a map repeated, an odd last map); every map
+    must equal the oracle's painting of that (table, profile)."""
+    maps = MAP_SETS[name]
+    rec = catalogs.shell(27, 20_000, r=(100.0, 3000.0), m=(1e12, 3e15))
+    tabs = [catalogs.table(nu=0.0), catalogs.table(nu=148.0)]
+    hp, _, st, sets = run_gpu(rec, tabs, precision, 1024, maps=maps)
+    rhp, _, rst, rsets = run_oracle(rec, tabs, 1024, maps=maps)
+    assert_sets_equal(sets, rsets)
+    for m in range(len(maps)):
+        assert_maps_close(hp[m], rhp[m], what="%s map %d" % (name, m))
+
+
 def test_large_flatsky_field():
     """A 1024^2 flat-sky map over 10 degrees (the flat-sky form at reduced side)."""
     rec = catalogs.cone(26, 40_000, (1.0, 0.0, 0.0), 8.0)
