@@ -37,9 +37,10 @@ SEED = 2
 ZMAX = 6.0
 MAPS = ((0, 1), (0, 2))
 LAUNCHES_PER_STEP = 15
-# DRAM bytes (read + write) per pixel update of k_paint_halos from an ncu capture of the
-# same kernel on 1e7 halos at Nside 2048 (dram__bytes_read.sum + dram__bytes_write.sum)
-PAINT_DRAM_BYTES_PER_UPDATE = 77.7
+# DRAM bytes (read + write) per pixel update of k_paint_halos from an ncu capture of this
+# workload's launch (1e7 halos at Nside 4096, one pass: dram__bytes_read.sum +
+# dram__bytes_write.sum = 1.20 GB + 0.61 GB for 3.51e7 updates on each of two maps)
+PAINT_DRAM_BYTES_PER_UPDATE = 51.6
 # L2 atomic throughput of this GB300 (sectors/s): ncu lts__t_sectors_srcunit_tex_op_atom
 # of the same capture, 26.7 sectors/ns at 7.06 % of peak sustained
 L2_ATOMIC_SECTORS_PER_S = 3.79e11
@@ -740,8 +741,8 @@ def run_ours(args):
     paint_ms = phases["paint"]
     alg_paint = upd * 16
     achieved = alg_paint / (paint_ms * 1e-3) / 1e9 if paint_ms > 0 else None
-    # DRAM traffic of the paint from the ncu capture of a smaller case (1e7 halos at
-    # Nside 2048), scaled by the pixel updates processed
+    # DRAM traffic of the paint from the ncu capture of this workload's launch, per pixel
+    # update processed
     traffic = PAINT_DRAM_BYTES_PER_UPDATE * st["hp_updates"] if args.precision == "mixed" else None
     roof = {"bound": "hbm", "kernel": "k_paint_halos + k_paint_full", "achieved": achieved,
             "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak if achieved else None,
