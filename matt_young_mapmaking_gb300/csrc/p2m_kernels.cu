@@ -843,13 +843,6 @@ __device__ __forceinline__ float fixed_to_float(long long q) {
   return __uint_as_float(sign | ((unsigned int)(e - 56 + 127) << 23) | (unsigned int)(top & 0x7fffffu));
 }
 
-/* adds one pixel's values (nmaps of them) at slot `slot`.  ACC 0: FP64 accumulator
-   (fire-and-forget red.add.f64); ACC 1: two-float (hi, lo) FP32 accumulator, hi by an
-   atomic add that returns the old value, lo the exact TwoSum rounding error; ACC 2:
-   compensated accumulation with the float output map as the high word, the low words
-   sparse (nonzero only where an add rounded) and their tiles flagged; ACC 3: 64-bit
-   fixed-point accumulator (value * 2^56 rounded to an integer, fire-and-forget).  All
-   maps' adds are issued before any result is used. */
 /* the compensated deposit's second half: the exact rounding error of each map's add
    (TwoSum of its returned old value and the value) goes to that map's low word, and the
    pixel's tile is flagged when any error is nonzero */
@@ -872,6 +865,13 @@ __device__ __forceinline__ void compensate_lo(const PaintParams &P, const SweepB
   if (any) W->tiles[slot >> P2M_TILE_SHIFT] = 1;
 }
 
+/* adds one pixel's values (nmaps of them) at slot `slot`.  ACC 0: FP64 accumulator
+   (fire-and-forget red.add.f64); ACC 1: two-float (hi, lo) FP32 accumulator, hi by an
+   atomic add that returns the old value, lo the exact TwoSum rounding error; ACC 2:
+   compensated accumulation with the float output map as the high word, the low words
+   sparse (nonzero only where an add rounded) and their tiles flagged; ACC 3: 64-bit
+   fixed-point accumulator (value * 2^56 rounded to an integer, fire-and-forget).  All
+   maps' adds are issued before any result is used. */
 template <int ACC>
 __device__ __forceinline__ void accumulate_vals(const PaintParams &P, void *acc, long long slot,
                                                 const float *vals, const SweepBuffers *W) {
