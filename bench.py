@@ -752,17 +752,17 @@ def run_ours(args):
             "atomic_updates_per_s": upd / (paint_ms * 1e-3) if paint_ms > 0 else None,
             "atomic_peak_per_s": L2_ATOMIC_SECTORS_PER_S,
             "atomic_frac": upd / (paint_ms * 1e-3) / L2_ATOMIC_SECTORS_PER_S if paint_ms > 0 else None}
-    # The DRAM floor of a scatter by atomics: every 32-byte sector of the maps that the
-    # paint touches is read from DRAM once and written back once, in any painting order
-    # (ncu: the paint's L2 atomic misses equal the touched sectors, and painting a narrower
-    # band of rings at a time changed neither the misses nor the DRAM bytes).  Counted
-    # here from the maps of the last resident step: the sectors holding a nonzero value;
-    # the low words' sectors come on top.
-    if npix % 8 == 0 and paint_ms > 0:
-        touched = sum(int(o.view(-1, 8).ne(0).any(dim=1).sum()) for o in outs)
-        floor = touched * 64
-        roof["sector_floor"] = {"touched_sectors": touched, "bytes": floor,
-                                "bytes_per_update": floor / upd,
+    # The DRAM floor of a scatter by atomics, in any painting order: every part of the
+    # maps that the paint touches is read from DRAM once and written back once.  Counted
+    # from the maps of the last resident step (the parts holding a nonzero value): reads
+    # of the touched 64-byte blocks, write-back of the touched 32-byte sectors.  The low
+    # words' sectors and the halo records come on top.
+    if npix % 16 == 0 and paint_ms > 0:
+        sec = sum(int(o.view(-1, 8).ne(0).any(dim=1).sum()) for o in outs)
+        blk = sum(int(o.view(-1, 16).ne(0).any(dim=1).sum()) for o in outs)
+        floor = blk * 64 + sec * 32
+        roof["sector_floor"] = {"touched_sectors_32b": sec, "touched_blocks_64b": blk,
+                                "bytes": floor, "bytes_per_update": floor / upd,
                                 "achieved_gbs": floor / (paint_ms * 1e-3) / 1e9,
                                 "frac": floor / (paint_ms * 1e-3) / 1e9 / hbm_peak}
     # the whole step (ingest through maps ready): the algorithmic bytes of the path with a
