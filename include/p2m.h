@@ -146,6 +146,15 @@ p2m_status p2m_reset_maps(p2m_ctx *ctx);
    p2m_tuning.stream_chunk; the steps before it stay painted); the context stays
    usable, and p2m_reset_maps starts over. */
 p2m_status p2m_paint_records(p2m_ctx *ctx, const float *records, int64_t nrec, int32_t nfloat);
+/* Page-locked host memory for catalogue records (no counterpart in the reference, whose
+   loadpksc reads into an allocatable array): p2m_paint_records copies from it straight
+   to the device, each step's copy overlapping the previous step's painting, where
+   records in ordinary memory are first staged by the CUDA driver.  p2m_paint_records
+   returns once its records are on the device, so the block can be refilled at once.
+   *out = the block, or NULL and P2M_ERR_NOMEM; free it with p2m_host_free (NULL is a
+   no-op). */
+p2m_status p2m_host_alloc(int64_t bytes, void **out);
+p2m_status p2m_host_free(void *p);
 /* The pks2map command-line flags scramble and center (pks2map.f90:75-76, :162-262): 1
    gives every halo that survives the radial cut a random direction from the reference's
    ranf stream (seed 13579*(rank+1), two draws per halo in catalogue order), resp. flips

@@ -142,6 +142,19 @@ module p2m_iface
        integer(c_int), value       :: nfloat
      end function p2m_paint_records
 
+     ! page-locked host memory for the records (c_f_pointer gives the Fortran array);
+     ! p2m_paint_records copies from it without the driver's staging
+     integer(c_int) function p2m_host_alloc(bytes, ptr) bind(C, name="p2m_host_alloc")
+       import :: c_int, c_ptr, c_long_long
+       integer(c_long_long), value :: bytes
+       type(c_ptr), intent(out)    :: ptr
+     end function p2m_host_alloc
+
+     integer(c_int) function p2m_host_free(ptr) bind(C, name="p2m_host_free")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: ptr
+     end function p2m_host_free
+
      ! projecthalo_flatsky + projecthalo_healpix (haloproject.f90:38,83) with their
      ! by-reference arguments; x, y, z come back divided by chi
      integer(c_int) function p2m_project_halo(ctx, x, y, z, r, chi, m, redshift, v, &

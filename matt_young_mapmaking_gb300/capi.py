@@ -104,6 +104,8 @@ def load_library():
         "p2m_load_table": (I32, [VP, I32, VP, I64]),
         "p2m_reset_maps": (I32, [VP]),
         "p2m_paint_records": (I32, [VP, VP, I64, I32]),
+        "p2m_host_alloc": (I32, [I64, ctypes.POINTER(VP)]),
+        "p2m_host_free": (I32, [VP]),
         "p2m_paint_records_device": (I32, [VP, VP, I64, I32, VP]),
         "p2m_project_halo": (I32, [VP, FP, FP, FP, FP, FP, FP, FP, FP,
                                    ctypes.POINTER(ctypes.c_int32)]),
@@ -164,7 +166,8 @@ def exported_symbols():
             "p2m_dpdy", "p2m_write_dpdy",
             "p2m_write_flatsky", "p2m_write_healpix_fits", "p2m_cl_healpix", "p2m_cl_flatsky",
             "p2m_paint_ensemble", "p2m_paint_ensemble_device", "p2m_get_healpix_cone",
-            "p2m_get_tuning", "p2m_set_tuning", "p2m_autotune", "p2m_get_healpix_async"]
+            "p2m_get_tuning", "p2m_set_tuning", "p2m_autotune", "p2m_get_healpix_async",
+            "p2m_host_alloc", "p2m_host_free"]
 
 
 PHASES = ["cut", "setup", "big_scan", "big_items", "flatsky", "big_offsets", "paint", "paint_big",

@@ -1122,6 +1122,23 @@ p2m_status p2m_paint_records(p2m_ctx *ctx, const float *records, int64_t nrec, i
   return stream_host_records(ctx, records, nrec, nfloat, nullptr, 0);
 }
 
+p2m_status p2m_host_alloc(int64_t bytes, void **out) {
+  if (!out) return P2M_ERR_BADARG;
+  *out = nullptr;
+  if (bytes < 0) return P2M_ERR_BADARG;
+  if (cudaHostAlloc(out, (size_t)std::max<int64_t>(bytes, 1), cudaHostAllocDefault) != cudaSuccess) {
+    cudaGetLastError(); /* a failed allocation leaves its error as the last error */
+    *out = nullptr;
+    return P2M_ERR_NOMEM;
+  }
+  return P2M_OK;
+}
+
+p2m_status p2m_host_free(void *p) {
+  if (p && cudaFreeHost(p) != cudaSuccess) return P2M_ERR_CUDA;
+  return P2M_OK;
+}
+
 p2m_status p2m_paint_records_device(p2m_ctx *ctx, const float *d_records, int64_t nrec,
                                     int32_t nfloat, void *stream) {
   if (!ctx) return P2M_ERR_BADARG;
@@ -1500,7 +1517,9 @@ p2m_status p2m_write_healpix_fits_device(p2m_ctx *ctx, int32_t map, const char *
   FILE *fp = std::fopen(path, "wb");
   if (!fp) return fail(ctx, P2M_ERR_IO, std::string("cannot open ") + path);
   bool ok = p2m_fits_put_header(fp, ctx->cfg.nside) == P2M_OK;
-  /* slice k is converted and copied while slice k - 1 is written to the file */
+  /* slice k is converted and copied while slice k - 1 is written to the file (one
+     writer: writes into one file from several threads measured slower, as the file
+     system serialises them) */
   const long long nslice = (n + slice - 1) / slice;
   cudaError_t e = cudaSuccess;
   for (long long k = 0; k <= nslice && ok && e == cudaSuccess; k++) {

@@ -141,3 +141,14 @@ def test_restricted_float_functions_equal_the_general_ones():
     y = np.exp(rng.uniform(-80.0, 80.0, 200_000)).astype(np.float32)
     y = np.concatenate([y, np.array([1.1754944e-38, 1.0, 3.4e38], np.float32)])
     assert np.array_equal(oracle.fmath(10, y).view(np.uint32), oracle.fmath(0, y).view(np.uint32))
+
+
+def test_host_alloc_argument_checks():
+    """p2m_host_alloc refuses a negative size or a null result pointer before any CUDA
+    call; p2m_host_free of NULL is a no-op."""
+    lib = p2m.load_library()
+    ptr = ctypes.c_void_p(1234)
+    assert lib.p2m_host_alloc(-1, ctypes.byref(ptr)) == p2m.capi.P2M_ERR_BADARG
+    assert ptr.value is None
+    assert lib.p2m_host_alloc(16, None) == p2m.capi.P2M_ERR_BADARG
+    assert lib.p2m_host_free(None) == p2m.capi.P2M_OK

@@ -1,6 +1,8 @@
 """GPU painter vs the oracle (same seeded inputs): per-halo pixel sets bit-exact, map
 values within 1e-5 relative wherever |value| > 1e-3 of the map maximum, map totals within
 1e-7 relative.  All calls go through the C ABI."""
+import ctypes
+
 import numpy as np
 import pytest
 
@@ -704,3 +706,37 @@ def test_fixed_point_range_is_reported(big_rings, monkeypatch):
         pt.load_table(0, bytes(tab))
         pt.paint_records(rec)
         assert np.abs(pt.healpix(0)).max() >= 128.0
+
+
+def test_records_from_page_locked_memory():
+    """p2m_host_alloc: records painted from a page-locked block (streamed in three steps per
+    call, each step's copy overlapping the painting) give the maps of the same records
+    painted from ordinary memory; the block is refilled as soon as p2m_paint_records
+    returns."""
+    lib = p2m.load_library()
+    recs = [catalogs.shell(41 + i, 30_000, r=(100.0, 3000.0), m=(1e12, 3e15)) for i in range(2)]
+    tab = catalogs.table(nu=0.0)
+    maps = ((0, 1), (0, 2))
+    ptr = ctypes.c_void_p()
+    assert lib.p2m_host_alloc(recs[0].nbytes, ctypes.byref(ptr)) == p2m.capi.P2M_OK
+    assert ptr.value
+    try:
+        blk = np.ctypeslib.as_array((ctypes.c_float * recs[0].size).from_address(ptr.value))
+        blk = blk.reshape(recs[0].shape)
+        out = []
+        for pinned in (True, False):
+            with p2m.Painter(nside=512, precision="mixed", maps=maps, zmax=6.0,
+                             max_records=10_000) as pt:
+                pt.load_table(0, tab)
+                for r in recs:
+                    if pinned:
+                        blk[:] = r
+                        pt.paint_records(blk)
+                    else:
+                        pt.paint_records(r)
+                out.append([pt.healpix(m) for m in range(len(maps))])
+    finally:
+        assert lib.p2m_host_free(ptr) == p2m.capi.P2M_OK
+    for m in range(len(maps)):
+        assert np.abs(out[1][m]).max() > 0
+        assert_maps_close(out[0][m], out[1][m], rel=1e-6, what="map %d" % m, sum_tol=1e-9)
