@@ -3,7 +3,8 @@
 c2 (the headline): 1e7 records (seed 2, shell 100-8000 Mpc, masses 1e12-3e15 Msun/h),
 HEALPix Nside 4096, tSZ y (nu = 0 table, profile 1) and kSZ (profile 2), zmax 6, the full
 100 x 100 x 200 make_maptable table; the mixed and the plain FP64 paths against the
-oracle's FP64 halo loop (pks2map.f90:276-303) on the same records and table image:
+oracle's FP64 halo loop (pks2map.f90:276-303) on the same records and table image
+(and the mixed decisions with FP64 or 64-bit fixed-point accumulation):
   - every (record, pixel) pair of every enumerated disc identical (FLAG_ALL_HALOS:
     also the discs whose table value is zero), ~4e7 pairs;
   - map values within 1e-5 relative wherever |v| > 1e-3 of the map's largest |v|;
@@ -80,7 +81,7 @@ def compare_maps(gpu, ref, what):
     return worst, tot
 
 
-@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+@pytest.mark.parametrize("precision", ["mixed", "fp64", "mixed64", "fixed"])
 def test_c2_headline_against_oracle(c2, precision, monkeypatch):
     rec, tab, rhp, rst, rkeys = c2
     monkeypatch.setenv("P2M_SET_CAP", str(SET_CAP))
